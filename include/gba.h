@@ -1,0 +1,279 @@
+/*
+ * gba.h -- C ABI of the GB300 bundle-adjustment engine (libgba.so).
+ *
+ * The engine replaces the Levenberg-Marquardt bundle-adjustment path of
+ * hs_sfm (include/hs_sfm/bundle_adjustment/camera_shared_*): the
+ * camera-shared projection model, its analytical Jacobian, the block
+ * normal equations, the Schur-complement reduced camera system and the
+ * damped LM driver.  Everything here is plain C: pointers, sizes and status
+ * codes, no C++ or torch types, no exceptions.
+ *
+ * Layout conventions follow the reference exactly so that a caller holding
+ * the reference containers can pass them without copying:
+ *   - feature_maps  = std::vector<std::pair<Index,Index>> (image_id, point_id)
+ *     (camera_shared_vector_function.hpp:36-37), Index = ptrdiff_t (int64);
+ *   - image_camera_map = std::vector<Index> (camera_shared_vector_function.hpp:39);
+ *   - x = [points 3P][images 6I][cameras cC], each block dropped when fixed
+ *     (camera_shared_vector_function.hpp:349-410);
+ *   - image = (angle-axis r[3], translation t[3]), camera point = R(r) X + t
+ *     (camera_shared_vector_function.hpp:688-710);
+ *   - camera = [k1 k2 k3][d1 d2][f s cx cy a], each group present when its
+ *     bit of the intrinsic mask is set (camera_shared_vector_function.hpp:247-263);
+ *   - y = [keys 2K][point constraints][image constraints][camera constraints]
+ *     (camera_shared_vector_function.hpp:412-632).
+ */
+#ifndef GBA_H_
+#define GBA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (0 / -1 are the reference's Err values) ------------- */
+#define GBA_OK                 0
+#define GBA_ERR               -1  /* generic failure (reference's -1)       */
+#define GBA_ERR_INVALID       -2  /* size mismatch / bad argument           */
+#define GBA_ERR_BAD_INDEX     -3  /* image/point/camera id out of range     */
+#define GBA_ERR_DUPLICATE     -4  /* the same (image, point) key twice      */
+#define GBA_ERR_UNSUPPORTED   -5  /* model variant not built on the GPU     */
+#define GBA_ERR_NOT_SPD       -6  /* reduced system not positive definite   */
+#define GBA_ERR_NAN           -7  /* non-finite residual or cost            */
+#define GBA_ERR_OOM           -8  /* device allocation failed               */
+#define GBA_ERR_CUDA          -9  /* CUDA runtime error                     */
+#define GBA_ERR_TIMEOUT      -10  /* a bounded device wait ran out          */
+#define GBA_ERR_NO_DEVICE    -11  /* no CUDA device visible                 */
+#define GBA_ERR_BUSY         -12  /* admission refused (slots or memory)    */
+#define GBA_ERR_CANCELLED    -13  /* request cancelled before it finished   */
+
+/* ---- masks (camera_shared_common_types.hpp:14-104) --------------------- */
+#define GBA_COMPUTE_RADIAL_DISTORTION       (1u << 0)
+#define GBA_COMPUTE_DECENTERING_DISTORTION  (1u << 1)
+#define GBA_COMPUTE_INTRINSIC_PARAMS        (1u << 2)
+
+#define GBA_FIX_POINTS   (1u << 0)
+#define GBA_FIX_IMAGES   (1u << 1)
+#define GBA_FIX_CAMERAS  (1u << 2)
+
+#define GBA_POINT_CONSTRAIN_X  (1u << 0)
+#define GBA_POINT_CONSTRAIN_Y  (1u << 1)
+#define GBA_POINT_CONSTRAIN_Z  (1u << 2)
+
+#define GBA_IMAGE_CONSTRAIN_ROTATION    (1u << 0)
+#define GBA_IMAGE_CONSTRAIN_POSITION_X  (1u << 1)
+#define GBA_IMAGE_CONSTRAIN_POSITION_Y  (1u << 2)
+#define GBA_IMAGE_CONSTRAIN_POSITION_Z  (1u << 3)
+
+typedef struct gba_point_constraint {   /* PointConstraint, :30-34 */
+  int64_t point_id;
+  uint32_t mask;                        /* GBA_POINT_CONSTRAIN_* */
+  uint32_t pad_;
+} gba_point_constraint;
+
+typedef struct gba_image_constraint {   /* ImageConstraint, :45-49 */
+  int64_t image_id;
+  uint32_t mask;                        /* GBA_IMAGE_CONSTRAIN_* */
+  uint32_t pad_;
+} gba_image_constraint;
+
+typedef struct gba_camera_constraint {  /* CameraConstraint, :88-94 */
+  int64_t camera_id;
+  uint32_t radial_mask;                 /* bits k1 k2 k3 */
+  uint32_t decentering_mask;            /* bits d1 d2 */
+  uint32_t intrinsic_mask;              /* bits f s cx cy a */
+  uint32_t pad_;
+} gba_camera_constraint;
+
+/*
+ * One bundle-adjustment problem: the content of a
+ * CameraSharedVectorFunction<double> (camera_shared_vector_function.hpp:746-763)
+ * plus the inverse observation covariance of
+ * CameraSharedYCovarianceInverse<double> (camera_shared_y_covariance_inverse.hpp:146-148).
+ * All pointers are host pointers owned by the caller; the library copies
+ * what it needs and never keeps them past the call that received them.
+ */
+typedef struct gba_problem {
+  int64_t number_of_points;
+  int64_t number_of_images;
+  int64_t number_of_cameras;
+  int64_t number_of_keys;
+  const int64_t* feature_maps;      /* [2*K] (image_id, point_id) per key   */
+  const int64_t* image_camera_map;  /* [I] camera id of each image          */
+  uint32_t intrinsic_computations_mask;
+  uint32_t fix_mask;
+  const double* fix_points;         /* [3P]  used when GBA_FIX_POINTS       */
+  const double* fix_images;         /* [6I]  used when GBA_FIX_IMAGES       */
+  const double* fix_cameras;        /* [cC]  used when GBA_FIX_CAMERAS      */
+  int64_t number_of_point_constraints;
+  const gba_point_constraint* point_constraints;
+  int64_t number_of_image_constraints;
+  const gba_image_constraint* image_constraints;
+  int64_t number_of_camera_constraints;
+  const gba_camera_constraint* camera_constraints;
+  /* Inverse covariance: per-key 2x2 row-major blocks [4K] (NULL = identity
+   * for every key) and one weight per constraint row [y_size - 2K]
+   * (NULL = 1 for every constraint row). */
+  const double* key_covariance_inverse;
+  const double* constraint_weights;
+} gba_problem;
+
+/* Sizes derived from a problem (GetXSize / GetYSize,
+ * camera_shared_vector_function.hpp:237-362). */
+int64_t gba_params_per_camera(uint32_t intrinsic_computations_mask);
+int64_t gba_x_size(const gba_problem* problem);
+int64_t gba_y_size(const gba_problem* problem);
+
+/* ---- solver options ------------------------------------------------------ */
+#define GBA_PRECISION_FP64   0   /* every stage in FP64 (the drop-in path)  */
+#define GBA_PRECISION_MIXED  1   /* FP32 Jacobian/Schur, FP64 master x,
+                                    cost sum and reduced-system factor     */
+
+#define GBA_LOSS_TRIVIAL 0
+#define GBA_LOSS_HUBER   1       /* rho(s)=s (s<=d^2), 2d*sqrt(s)-d^2 else */
+
+#define GBA_LINEAR_DENSE_CHOLESKY 0
+#define GBA_LINEAR_PCG            1  /* block-Jacobi PCG on the explicit
+                                        block-sparse reduced system        */
+
+typedef struct gba_options {
+  /* LevenbergMarquardt(max_itr_num, tau, eps1, eps2)
+   * (camera_shared_levenberg_marquardt_optimizor.hpp:36-41). */
+  int32_t max_iterations;
+  double tau;
+  double eps1;
+  double eps2;
+  int32_t precision;          /* GBA_PRECISION_*                            */
+  int32_t loss;               /* GBA_LOSS_*                                 */
+  double huber_delta;         /* pixels (whitened)                          */
+  int32_t linear_solver;      /* GBA_LINEAR_*                               */
+  int32_t pcg_max_iterations;
+  double pcg_relative_tolerance;
+  int32_t use_cuda_graph;     /* capture each LM iteration once, replay     */
+  int32_t profile;            /* record per-stage CUDA events               */
+  int32_t device;             /* CUDA device ordinal                        */
+  int32_t reserved_[7];
+} gba_options;
+
+/* Fills the defaults used by the reference's relative-pair test
+ * (test_camera_shared_relative_pair.cpp:976-979): 50 iterations,
+ * tau 1e-3, eps1 1e-8, eps2 1e-8, FP64, trivial loss, dense Cholesky. */
+void gba_default_options(gba_options* options);
+
+#define GBA_STOP_MAX_ITERATIONS 0
+#define GBA_STOP_SMALL_GRADIENT 1
+#define GBA_STOP_SMALL_STEP     2
+#define GBA_STOP_ERROR          3
+
+#define GBA_NUM_STAGES 8
+/* stage indices of gba_report.stage_ms */
+#define GBA_STAGE_LINEARIZE   0
+#define GBA_STAGE_POINT_SCHUR 1
+#define GBA_STAGE_ASSEMBLE    2
+#define GBA_STAGE_FACTOR      3
+#define GBA_STAGE_BACKSUB     4
+#define GBA_STAGE_COST        5
+#define GBA_STAGE_CONTROL     6
+#define GBA_STAGE_OTHER       7
+
+typedef struct gba_report {
+  int32_t status;             /* GBA_OK or an error code                    */
+  int32_t stop_reason;        /* GBA_STOP_*                                 */
+  int32_t iterations;         /* LM iterations (accepted + rejected)        */
+  int32_t accepted;
+  int32_t rejected;
+  int32_t factor_failures;    /* non-SPD reduced systems (step rejected)    */
+  int32_t pcg_iterations;     /* total over the solve                       */
+  int32_t pad_;
+  double initial_cost;        /* sum r^T Lambda r (Mahalanobis, no 1/2)     */
+  double final_cost;
+  double final_rmse;          /* sqrt(sum ||r_key||^2 / K), pixels          */
+  double final_mu;
+  double final_gradient_inf_norm;
+  double setup_ms;            /* structure build + upload                   */
+  double solve_ms;            /* LM loop, device time                       */
+  double stage_ms[GBA_NUM_STAGES];  /* with options.profile                 */
+} gba_report;
+
+/* ---- one-shot solve: the drop-in for
+ * CameraSharedLevenbergMarquardtOptimizor::operator()
+ * (camera_shared_levenberg_marquardt_optimizor.hpp:43-58).
+ * near_y [y_size] is the observed y; x_inout [x_size] holds the initial x on
+ * entry and the optimized x on return.  Host buffers. */
+int gba_solve(const gba_problem* problem, const double* near_y,
+              const gba_options* options, double* x_inout,
+              gba_report* report);
+
+/* ---- resident plans: one or many problems kept on the device ----------- */
+typedef struct gba_plan gba_plan;
+
+int gba_plan_create(const gba_problem* problems, const double* const* near_ys,
+                    int32_t number_of_problems, const gba_options* options,
+                    gba_plan** plan);
+int gba_plan_destroy(gba_plan* plan);
+int gba_plan_number_of_problems(const gba_plan* plan);
+/* Copies x0 of every problem (host) to the device and remembers it. */
+int gba_plan_set_initial_x(gba_plan* plan, int32_t problem, const double* x0);
+/* Resets every problem to its remembered x0 and runs the LM solve of all
+ * problems together (asynchronous on the plan's stream). */
+int gba_plan_run(gba_plan* plan);
+/* Waits for the plan's stream; returns the first device status seen. */
+int gba_plan_synchronize(gba_plan* plan);
+int gba_plan_get_x(gba_plan* plan, int32_t problem, double* x_out);
+int gba_plan_get_report(gba_plan* plan, int32_t problem, gba_report* report);
+/* Device time of the last gba_plan_run in milliseconds (CUDA events on the
+ * plan's stream), and the average duration of the named kernel's launches
+ * in that run when options.profile was set (0 when not recorded). */
+int gba_plan_last_run_ms(gba_plan* plan, double* ms);
+int gba_plan_kernel_stats(gba_plan* plan, int32_t stage, double* total_ms,
+                          int32_t* launches);
+/* Counts of this library's kernel launches in the last run. */
+int gba_plan_last_run_launches(gba_plan* plan, int64_t* launches);
+
+/* ---- batched one-shot solve (independent problems, one plan) ----------- */
+int gba_solve_batch(const gba_problem* problems, const double* const* near_ys,
+                    int32_t number_of_problems, const gba_options* options,
+                    double* const* x_inout, gba_report* reports);
+
+/* ---- single-stage entry points (the trait plug-ins of
+ * camera_shared_nllso_meta_levenberg_marquardt.hpp:33-106), used for parity
+ * checks of each stage.  Host buffers in and out. ------------------------- */
+
+/* CameraSharedVectorFunction::operator() (:412-632): y [y_size]. */
+int gba_vector_function(const gba_problem* problem, const double* x,
+                        double* y, int32_t precision);
+
+/* CameraSharedAnalyticalJacobianMatrixCalculator (:66-332): per key, in key
+ * order, the 2x3 point block, the 2x6 image block and the 2xc camera block,
+ * row-major; blocks of fixed parameter groups are not written (pass NULL). */
+int gba_jacobian(const gba_problem* problem, const double* x,
+                 double* point_blocks, double* image_blocks,
+                 double* camera_blocks, int32_t precision);
+
+/* Mahalanobis distance sum r^T Lambda r of r = f(x) - near_y
+ * (camera_shared_mahalanobis_distance_calculator.hpp:28-58); with a Huber
+ * loss each key's term s becomes rho(s). */
+int gba_cost(const gba_problem* problem, const double* x,
+             const double* near_y, const gba_options* options, double* cost);
+
+/* One damped Gauss-Newton step: builds the normal equations at x
+ * (camera_shared_normal_equation_builder.hpp:92-108), augments them with mu
+ * (camera_shared_augmentor.hpp:22-26) and solves (N + mu I) delta = g by the
+ * Schur complement (camera_shared_normal_equation_solver.hpp:75-114).
+ * delta_x [x_size]; the LM update is x - delta_x. */
+int gba_schur_step(const gba_problem* problem, const double* x,
+                   const double* near_y, double mu,
+                   const gba_options* options, double* delta_x);
+
+/* ---- library ------------------------------------------------------------ */
+const char* gba_status_string(int status);
+const char* gba_version(void);
+/* Number of kernels this library has launched since load (all threads). */
+int64_t gba_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* GBA_H_ */

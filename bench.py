@@ -1,0 +1,371 @@
+"""Benchmark: LM iterations/s of bundle adjustment on one GB300.
+
+Workload (default): 200 cameras on a jittered grid over a 100,000-point slab,
+4-12 keys per point (~800k keys), shared intrinsics with radial distortion
+(fixed), points and images free; 20 Levenberg-Marquardt iterations per solve
+(eps1 = eps2 = 0 so every iteration runs) on the mixed FP32/FP64 path with
+the dense FP64 Cholesky of the 1,200-unknown reduced camera system.
+
+A step is one full solve (20 LM iterations) with the problem resident in HBM;
+`value` = LM iterations / device time over the K timed steps (CUDA events on
+the solver's stream, L2 flushed by a 256 MB write between steps).  `e2e` is the
+same metric through gba_solve() with host buffers: structure build, host->device
+copies, the solve and the device->host copy of x inside the timed region.
+
+--impl reference times the CPU restatement of the reference path (the oracle,
+faithful O(I^2 P) reduced-system loop, single thread as the reference is) on a
+bounded sample of the same workload: the reduced-system double loop runs over
+every `stride`-th weighted image and its time is scaled by the stride.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+ITERS_PER_SOLVE = 20
+METRIC = "LM iters/s"
+UNIT = "iter/s"
+WORKLOAD = "grid BA 200 cameras / 100k points / ~800k keys, radial+intrinsics fixed, 20 LM iterations"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gba", choices=["gba", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample-stride", type=int, default=40)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--points", type=int, default=100_000)
+    ap.add_argument("--images", type=int, default=200)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed (replicas only: each rank solves its own problem)
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    dist.init_process_group(backend)
+    return dist
+
+
+def allreduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, v):
+    if dist is None:
+        return v
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        sm = [r[0] for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[2]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# per-stage algorithmic bytes (contract inputs once + outputs once)
+# ---------------------------------------------------------------------------
+def stage_bytes(K, P, I, pairs, items, tsz):
+    """Per launch, for the stages of one LM iteration."""
+    return {
+        "linearize": K * (4 + 4 * tsz + 20 * tsz + 4) + P * (24 + 4 + 12 * tsz) + I * 42 * 8,
+        "point_schur": K * (20 * tsz + 18 * tsz) + P * (12 * tsz + 12 * tsz + 4),
+        "assemble": K * 18 * tsz + pairs * 8 + items * (16 + 42 * 8) + P * 3 * tsz,
+        "backsub": K * (18 * tsz + 4) + P * (12 * tsz + 24 + 24 + 4) + I * 6 * 8 * 3,
+        "cost": K * (16 + 8 + 4 * tsz) + P * 24 + I * 12 * 8,
+    }
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def pair_count(scene):
+    fm = scene.feature_maps
+    k = np.bincount(fm[:, 1], minlength=scene.number_of_points)
+    pairs = int(np.sum(k * (k + 1) // 2))
+    return pairs
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle, faithful loop, sampled)
+# ---------------------------------------------------------------------------
+def cpu_sample(scene, stride):
+    import oracle
+    from hs_sfm_gb300 import abi
+    N, g = None, None
+    mu = 1e-3 * 1e6
+    t0 = time.perf_counter()
+    sec = oracle.time_faithful_iteration(scene, scene.x0, mu, row_stride=stride)
+    wall = time.perf_counter() - t0
+    del abi, N, g
+    return float(sec[0]), wall, sec
+
+
+def make_scene(args, rank=0):
+    from hs_sfm_gb300 import synthetic
+    return synthetic.grid_scene(num_images=args.images, num_points=args.points, seed=1 + rank,
+                                name="cfg1")
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    import oracle  # noqa: F401
+    scene = make_scene(args)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(scene, args.cpu_sample_stride)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        est, wall, _ = cpu_sample(scene, args.cpu_sample_stride)
+        vals.append(1.0 / est)
+    elapsed = time.perf_counter() - t0
+    value = float(statistics.mean(vals))
+    sample = (f"one LM iteration per step (linearize, faithful O(I^2 P) reduced system over every "
+              f"{args.cpu_sample_stride}th weighted image scaled by {args.cpu_sample_stride}, "
+              f"LDL^T, back-substitution, candidate cost)")
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded grid scene)",
+        "config": {"workload": WORKLOAD, "points": scene.number_of_points,
+                   "images": scene.number_of_images, "keys": scene.number_of_keys},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_gba(args, ws, rank, local):
+    import torch
+    from hs_sfm_gb300 import abi, gba
+    dist = dist_init(ws)
+    torch.cuda.set_device(local)
+    precision = abi.PRECISION_MIXED if args.precision == "mixed" else abi.PRECISION_FP64
+    tsz = 4 if precision == abi.PRECISION_MIXED else 8
+    scene = make_scene(args, rank)
+    opt = abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0, eps2=0.0,
+                           precision=precision, profile=1, use_cuda_graph=1, device=local)
+    plan = gba.Plan([scene], opt)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    for _ in range(args.warmup):
+        plan.run()
+        plan.synchronize()
+    rep0 = plan.report(0)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms, stage_tot = [], np.zeros(abi.NUM_STAGES)
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        plan.run()
+        plan.synchronize()
+        step_ms.append(plan.last_run_ms())
+        r = plan.report(0)
+        stage_tot += np.array(r.stage_ms)
+    torch.cuda.synchronize()
+    barrier(dist)
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    rep = plan.report(0)
+    launches_per_run = plan.launches()
+    total_ms = float(sum(step_ms))
+    total_ms_max = allreduce_max(dist, total_ms)
+    iters = ITERS_PER_SOLVE * args.steps
+    iters_all = allreduce_sum(dist, iters)
+    value = iters_all / (total_ms_max / 1e3)
+
+    # per-stage roofline (the stage's kernels, CUDA events on the solver stream)
+    K, P, I = scene.number_of_keys, scene.number_of_points, scene.number_of_images
+    pairs = pair_count(scene)
+    items = None
+    peak, peak_kind = load_peaks()
+    names = abi.STAGE_NAMES
+    per_launch_ms = {names[s]: stage_tot[s] / (args.steps * ITERS_PER_SOLVE) for s in range(len(names))}
+    n_items_est = int(np.ceil(pairs / 256)) + I * (I + 1) // 2
+    sb = stage_bytes(K, P, I, pairs, n_items_est, tsz)
+    stages = {}
+    for name, ms in per_launch_ms.items():
+        entry = {"ms_per_iteration": ms}
+        if name in sb and ms > 0:
+            entry["algorithmic_bytes"] = sb[name]
+            entry["achieved_gbs"] = sb[name] / (ms / 1e3) / 1e9
+        stages[name] = entry
+    hbm_stages = {k: v for k, v in stages.items() if "achieved_gbs" in v}
+    dom = max(hbm_stages, key=lambda k: hbm_stages[k]["ms_per_iteration"])
+    achieved = hbm_stages[dom]["achieved_gbs"]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                "traffic": None}
+
+    # end to end through the C ABI with host buffers
+    e2e_ms, h2d, d2h = [], 0, 0
+    opt_e2e = abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0, eps2=0.0,
+                               precision=precision, device=local)
+    for _ in range(max(1, args.e2e_steps)):
+        t0 = time.perf_counter()
+        x, r = gba.solve(scene, opt_e2e)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+        h2d, d2h = r.h2d_bytes, r.d2h_bytes
+    e2e_max = allreduce_max(dist, float(sum(e2e_ms)))
+    e2e_value = allreduce_sum(dist, ITERS_PER_SOLVE * len(e2e_ms)) / (e2e_max / 1e3)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        est, wall, sec = cpu_sample(scene, args.cpu_sample_stride)
+        cpu = {"value": 1.0 / est, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": (f"one LM iteration of the faithful restatement at x0; the O(I^2 P) "
+                          f"reduced-system loop over every {args.cpu_sample_stride}th weighted image, "
+                          f"time scaled by {args.cpu_sample_stride} ({wall:.1f} s wall)"),
+               "seconds_per_iteration": est}
+
+    if rank == 0:
+        lat = sorted(step_ms)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if precision == abi.PRECISION_MIXED else "f64",
+            "data": "synthetic (seeded grid scene, noise 1 px, float32-exact keys)",
+            "config": {"workload": WORKLOAD, "points": P, "images": I, "keys": K, "pairs": pairs,
+                       "precision": args.precision, "iterations_per_step": ITERS_PER_SOLVE,
+                       "linear_solver": "dense FP64 Cholesky (1,200 unknowns)",
+                       "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas{ws}"},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "solve": {"initial_cost": rep.initial_cost, "final_cost": rep.final_cost,
+                      "final_rmse": rep.final_rmse, "accepted": rep.accepted,
+                      "rejected": rep.rejected, "setup_ms": rep0.setup_ms},
+            "roofline": roofline,
+            "stages": stages,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms))},
+            "gpu_launches": int(launches_per_run * args.steps),
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(out), flush=True)
+    plan.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_gba(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -103,6 +103,7 @@ class Report(C.Structure):
         ("final_mu", C.c_double), ("final_gradient_inf_norm", C.c_double),
         ("setup_ms", C.c_double), ("solve_ms", C.c_double),
         ("stage_ms", C.c_double * NUM_STAGES),
+        ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
     ]
 
     def as_dict(self):

@@ -1,0 +1,162 @@
+// gba_internal.h -- device data layout of a plan (a batch of bundle-adjustment
+// problems resident on one GPU) shared by the kernels and the host planner.
+//
+// Every problem of a batch is concatenated into global arrays; a single
+// problem is a batch of one.  Keys are stored point-major (all keys of a
+// point contiguous, sorted by image id), which makes the per-point
+// quantities of the Schur complement (V_p, g_p, V_p^-1) register-local.
+// Indices on the device are int32 (global key, point, image ids), offsets
+// into the dense reduced systems are int64.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gba.h"
+
+namespace gba {
+
+constexpr int kTile = 32;          // dense Cholesky tile (FP64)
+constexpr int kKeyChunk = 1024;    // keys per cost work chunk
+constexpr int kPointChunk = 128;   // points per point work chunk
+constexpr int kImageChunk = 8;     // images per image work chunk (warp each)
+constexpr int kPairItem = 256;     // pairs per Schur-assembly work item
+constexpr int kJRStride = 20;      // per key: Jp(6) Ji(12) rw(2)
+constexpr int kZStride = 20;       // per key: Z(18) + pad
+constexpr int kItemStride = 44;    // per work item: 36 block + 6 rhs + pad
+
+// Per-problem LM state (device).  Written only by the control kernels.
+struct LMState {
+  double mu, nu;
+  double F, F_new;                 // current / candidate cost
+  double dn2, xn2, gd;             // ||delta||^2, ||x||^2, g^T delta
+  unsigned long long ginf_bits;    // max |g| as ordered bits (non-negative)
+  unsigned long long maxdiag_bits; // max diag(N) as ordered bits
+  double initial_cost;
+  int iter, accepted, rejected, factor_fail, stop, status;
+  int active;     // still iterating
+  int parity;     // which x / residual buffer is current
+  int relin;      // a linearization is pending
+  int evaluate;   // a candidate is pending evaluation
+  int factor_ok;  // reduced system factored this iteration
+  int first;      // the first linearization (sets mu0)
+  int pcg_iters;
+  int pad_;
+};
+
+// Per-problem constant description (device).
+struct ProbInfo {
+  int point_begin, num_points;
+  int image_begin, num_images;
+  int key_begin, num_keys;
+  int n;              // reduced system size = 6 * num_images
+  int nt;             // number of kTile tiles of the reduced system
+  long long s_off;    // offset of the n x n dense system (row-major)
+  int item_begin, num_items;
+  int block_begin, num_blocks;
+};
+
+struct Chunk {       // a contiguous range of one problem's entities
+  int prob, begin, end, pad_;
+};
+
+struct DevPlan {
+  int B;
+  int precision;      // GBA_PRECISION_*
+  int loss;
+  double huber_delta;
+  double tau, eps1, eps2;
+  int max_iterations;
+  int has_key_weights;
+  int max_n, max_nt;  // largest reduced system in the batch
+
+  const ProbInfo* prob;
+  LMState* state;
+
+  // keys
+  int K;
+  const int* key_img;        // global image id
+  const int* key_pt;         // global point id
+  const double2* key_obs;    // observed key
+  const double* key_wl;      // [3K] upper factor of the key weight (l00,l10,l11) or null
+  // points
+  int P;
+  const int* pt_key_off;     // [P+1]
+  const int* pt_prob;
+  // images
+  int I;
+  const int* img_key_off;    // [I+1]
+  const int* img_keys;       // keys of each image, by point
+  const int* img_prob;
+  const int* img_cam;        // global camera id
+  const double* cam64;       // [C*10]  k1 k2 k3 d1 d2 f s cx cy a
+  const float* cam32;        // [C*10]
+  // parameters (double buffered by LMState::parity)
+  double* x_pt[2];           // [3P]
+  double* x_img[2];          // [6I]
+  const double* x0_pt;
+  const double* x0_img;
+  double* img_rot[2];        // [12I] R (9) + t (3), FP64
+  void* img_lin[2];          // [12I] T: r(3) t(3) ct s c a1 a2 pad
+  // per key
+  void* RW[2];               // [4K] T: rw0 rw1 sqrt(w) pad  (whitened, weighted residual)
+  void* JR;                  // [20K] T
+  void* Z;                   // [20K] T
+  // per point
+  void* PV;                  // [12P] T: V(6) g(3) pad
+  void* PS;                  // [12P] T: Cinv(6) h(3) pad
+  // per image (FP64)
+  double* U;                 // [36I]
+  double* gi;                // [6I]
+  // reduced systems
+  double* S;                 // sum n^2 over problems
+  double* b;                 // [6I]  rhs -> forward solution -> delta (images)
+  double* Linv;              // [B * max_nt * kTile^2] inverses of diagonal tiles
+  int* factor_flag;          // [B] 0 ok, 1 failed
+  // Schur assembly
+  const int2* pairs;         // (key_a, key_b) per pair, grouped by block
+  const int4* items;         // (block, pair_begin, pair_end, prob)
+  const int2* blk_ij;        // (i, j) local image ids per block, i <= j
+  const int* blk_item_off;   // [num_blocks_total + 1] items of each block
+  int n_items, n_blocks;
+  const int* blk_map;        // per problem I*I dense map (j*I + i), j <= i -> block or -1
+  const long long* blk_map_off; // [B]
+  double* item_partial;      // [items * kItemStride]
+  // work chunks and their partial sums (FP64)
+  int n_key_chunks, n_pt_chunks, n_img_chunks;
+  const Chunk* key_chunks;
+  const Chunk* pt_chunks;
+  const Chunk* img_chunks;
+  const int* prob_key_chunk_off;  // [B+1]
+  const int* prob_pt_chunk_off;   // [B+1]
+  const int* prob_img_chunk_off;  // [B+1]
+  double* key_chunk_sum;          // [n_key_chunks] cost
+  double* pt_chunk_sum;           // [3 * n_pt_chunks] dn2, xn2, gd
+  double* img_chunk_sum;          // [3 * n_img_chunks]
+  unsigned long long* launch_counter; // device-side count (unused: host counts)
+};
+
+// Host launchers (gba_kernels.cu).  `T` selects the working precision of
+// the Jacobian / Schur stages: float (mixed) or double (plain FP64).
+int launch_init(const DevPlan& d, cudaStream_t s);
+int launch_image_prep(const DevPlan& d, int which, cudaStream_t s);
+int launch_cost(const DevPlan& d, int which, cudaStream_t s);
+int launch_ctrl_initial_cost(const DevPlan& d, cudaStream_t s);
+int launch_linearize(const DevPlan& d, cudaStream_t s);
+int launch_image_reduce(const DevPlan& d, cudaStream_t s);
+int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s);
+int launch_point_schur(const DevPlan& d, cudaStream_t s);
+int launch_assemble(const DevPlan& d, cudaStream_t s);
+int launch_assemble_items(const DevPlan& d, cudaStream_t s);
+int launch_assemble_S(const DevPlan& d, cudaStream_t s);
+int launch_cholesky(const DevPlan& d, cudaStream_t s);
+int launch_backsub(const DevPlan& d, cudaStream_t s);
+int launch_ctrl_step(const DevPlan& d, cudaStream_t s);
+int launch_ctrl_accept(const DevPlan& d, cudaStream_t s);
+
+// Stage entry points on a plan (gba_kernels.cu): Jacobian blocks in sorted
+// key order (T precision), vector function (FP64).
+int launch_vector_function(const DevPlan& d, double* y_sorted, cudaStream_t s);
+int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, cudaStream_t s);
+
+}  // namespace gba

@@ -1,0 +1,1031 @@
+// gba_plan.cu -- host side of libgba.so: builds the device layout of a batch
+// of problems (point-major keys, per-image key lists, reduced-system block
+// structure with its pair lists, work chunks), owns the device buffers and
+// drives the Levenberg-Marquardt iterations, and implements the C ABI of
+// include/gba.h.
+//
+// The LM decisions are taken on the device (gba_kernels.cu, k_ctrl_*), so a
+// whole solve is a fixed sequence of launches with no host synchronization;
+// that sequence is captured once into a CUDA graph and replayed.
+#include "gba_internal.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+namespace gba {
+
+struct CudaError {
+  int status;
+};
+
+namespace {
+
+std::atomic<long long> g_launches{0};
+
+#define GBA_CUDA(call)                                                      \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) {                                                \
+      std::fprintf(stderr, "gba: %s failed: %s (%s:%d)\n", #call,          \
+                   cudaGetErrorString(e_), __FILE__, __LINE__);             \
+      throw ::gba::CudaError{e_ == cudaErrorMemoryAllocation ? GBA_ERR_OOM         \
+                                                      : GBA_ERR_CUDA};      \
+    }                                                                       \
+  } while (0)
+
+int64_t params_per_camera(uint32_t m) {
+  return ((m & GBA_COMPUTE_RADIAL_DISTORTION) ? 3 : 0) +
+         ((m & GBA_COMPUTE_DECENTERING_DISTORTION) ? 2 : 0) +
+         ((m & GBA_COMPUTE_INTRINSIC_PARAMS) ? 5 : 0);
+}
+
+// Full 10-parameter camera [k1 k2 k3 d1 d2 f s cx cy a] from the masked one.
+void expand_camera(uint32_t mask, const double* c, double out[10]) {
+  const double ident[10] = {0, 0, 0, 0, 0, 1, 0, 0, 0, 1};
+  std::memcpy(out, ident, sizeof(ident));
+  int o = 0;
+  if (mask & GBA_COMPUTE_RADIAL_DISTORTION) {
+    out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
+    o += 3;
+  }
+  if (mask & GBA_COMPUTE_DECENTERING_DISTORTION) {
+    out[3] = c[o]; out[4] = c[o + 1];
+    o += 2;
+  }
+  if (mask & GBA_COMPUTE_INTRINSIC_PARAMS) {
+    for (int j = 0; j < 5; ++j) out[5 + j] = c[o + j];
+  }
+}
+
+// Device buffer registry.
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  size_t bytes = 0;
+  long long uploaded = 0;
+  template <typename T>
+  T* alloc(size_t count) {
+    if (count == 0) count = 1;
+    void* p = nullptr;
+    GBA_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    ptrs.push_back(p);
+    bytes += count * sizeof(T);
+    return static_cast<T*>(p);
+  }
+  template <typename T>
+  T* upload(const std::vector<T>& h) {
+    T* p = alloc<T>(h.size());
+    if (!h.empty()) GBA_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    uploaded += (long long)(h.size() * sizeof(T));
+    return p;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Plan
+// ---------------------------------------------------------------------------
+struct Plan {
+  gba_options opt{};
+  int B = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DeviceArena arena;
+  DevPlan d{};
+  // host layout
+  std::vector<ProbInfo> prob;
+  std::vector<std::vector<int32_t>> key_sorted_to_orig;  // per problem
+  std::vector<int64_t> x_size;
+  // run state
+  cudaGraphExec_t graph_exec = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool ran = false;
+  long long launches_last_run = 0;
+  double setup_ms = 0;
+  long long h2d_bytes = 0, d2h_bytes = 0;
+  // profiling: per stage event pairs per iteration
+  std::vector<cudaEvent_t> prof_events;
+  std::vector<int> prof_stage;
+  double stage_ms[GBA_NUM_STAGES] = {};
+  int stage_launches[GBA_NUM_STAGES] = {};
+  double* d_rmse_scratch = nullptr;
+
+  ~Plan() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (cudaEvent_t e : prof_events) cudaEventDestroy(e);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    arena.release();
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int build(const gba_problem* problems, const double* const* near_ys, int nprob,
+            const gba_options* options);
+  void enqueue(bool profile);
+  int run();
+  int sync();
+};
+
+namespace {
+
+// Validates a problem for the device path.  The device path covers the
+// configuration of the benchmark workloads: points and images free, cameras
+// (shared intrinsics) fixed, no soft constraints.
+int validate(const gba_problem& p) {
+  if (p.number_of_points < 0 || p.number_of_images < 0 || p.number_of_cameras < 0 ||
+      p.number_of_keys < 0)
+    return GBA_ERR_INVALID;
+  if (p.number_of_keys > 0 && !p.feature_maps) return GBA_ERR_INVALID;
+  if (p.number_of_images > 0 && !p.image_camera_map) return GBA_ERR_INVALID;
+  if (p.fix_mask != GBA_FIX_CAMERAS) return GBA_ERR_UNSUPPORTED;
+  if (p.number_of_cameras > 0 && params_per_camera(p.intrinsic_computations_mask) > 0 &&
+      !p.fix_cameras)
+    return GBA_ERR_INVALID;
+  if (p.number_of_point_constraints > 0 || p.number_of_image_constraints > 0)
+    return GBA_ERR_UNSUPPORTED;
+  if (p.number_of_points > INT32_MAX / 4 || p.number_of_keys > INT32_MAX / 4)
+    return GBA_ERR_INVALID;
+  // the dense reduced system of one problem is at most 12288^2 doubles
+  if (p.number_of_images > 2048) return GBA_ERR_UNSUPPORTED;
+  for (int64_t i = 0; i < p.number_of_images; ++i) {
+    int64_t c = p.image_camera_map[i];
+    if (c < 0 || c >= p.number_of_cameras) return GBA_ERR_BAD_INDEX;
+  }
+  for (int64_t k = 0; k < p.number_of_keys; ++k) {
+    int64_t im = p.feature_maps[2 * k], pt = p.feature_maps[2 * k + 1];
+    if (im < 0 || im >= p.number_of_images || pt < 0 || pt >= p.number_of_points)
+      return GBA_ERR_BAD_INDEX;
+  }
+  return GBA_OK;
+}
+
+}  // namespace
+
+int Plan::build(const gba_problem* problems, const double* const* near_ys, int nprob,
+                const gba_options* options) {
+  auto t0 = std::chrono::steady_clock::now();
+  opt = *options;
+  B = nprob;
+  device = opt.device;
+  GBA_CUDA(cudaSetDevice(device));
+  GBA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  GBA_CUDA(cudaEventCreate(&ev0));
+  GBA_CUDA(cudaEventCreate(&ev1));
+  const bool mixed = opt.precision == GBA_PRECISION_MIXED;
+  const size_t tsz = mixed ? sizeof(float) : sizeof(double);
+
+  for (int q = 0; q < nprob; ++q) {
+    int err = validate(problems[q]);
+    if (err) return err;
+    if (!near_ys || !near_ys[q]) return GBA_ERR_INVALID;
+  }
+  // ---- global sizes
+  int64_t P = 0, I = 0, K = 0, C = 0;
+  for (int q = 0; q < nprob; ++q) {
+    P += problems[q].number_of_points;
+    I += problems[q].number_of_images;
+    K += problems[q].number_of_keys;
+    C += problems[q].number_of_cameras;
+  }
+  if (P > INT32_MAX / 4 || K > INT32_MAX / 4 || I > INT32_MAX / 64) return GBA_ERR_INVALID;
+
+  std::vector<int> key_img(K), key_pt(K);
+  std::vector<double2> key_obs(K);
+  std::vector<double> key_wl;
+  bool any_weights = false;
+  for (int q = 0; q < nprob; ++q) any_weights |= problems[q].key_covariance_inverse != nullptr;
+  if (any_weights) key_wl.assign(3 * K, 0.0);
+  std::vector<int> pt_key_off(P + 1, 0), pt_prob(P), img_key_off(I + 1, 0), img_keys(K),
+      img_prob(I), img_cam(I);
+  std::vector<double> cam64(10 * std::max<int64_t>(C, 1), 0.0);
+  std::vector<float> cam32(cam64.size(), 0.0f);
+  std::vector<int2> pairs;
+  std::vector<int4> items;
+  std::vector<int2> blk_ij;
+  std::vector<int> blk_item_off(1, 0);
+  std::vector<int> blk_map;
+  std::vector<long long> blk_map_off(nprob, 0);
+  std::vector<Chunk> key_chunks, pt_chunks, img_chunks;
+  std::vector<int> prob_key_chunk_off(1, 0), prob_pt_chunk_off(1, 0), prob_img_chunk_off(1, 0);
+  prob.resize(nprob);
+  key_sorted_to_orig.resize(nprob);
+  x_size.resize(nprob);
+
+  int64_t pb = 0, ib = 0, kb = 0, cb = 0;
+  long long s_off = 0;
+  int max_n = 0, max_nt = 0;
+  for (int q = 0; q < nprob; ++q) {
+    const gba_problem& p = problems[q];
+    const int np = int(p.number_of_points), ni = int(p.number_of_images), nk = int(p.number_of_keys);
+    const int64_t cps = params_per_camera(p.intrinsic_computations_mask);
+    ProbInfo& pi = prob[q];
+    pi.point_begin = int(pb);
+    pi.num_points = np;
+    pi.image_begin = int(ib);
+    pi.num_images = ni;
+    pi.key_begin = int(kb);
+    pi.num_keys = nk;
+    pi.n = 6 * ni;
+    pi.nt = (pi.n + kTile - 1) / kTile;
+    pi.s_off = s_off;
+    s_off += (long long)pi.n * pi.n;
+    max_n = std::max(max_n, pi.n);
+    max_nt = std::max(max_nt, pi.nt);
+    x_size[q] = 3LL * np + 6LL * ni;
+    // cameras
+    for (int64_t c = 0; c < p.number_of_cameras; ++c) {
+      double full[10];
+      expand_camera(p.intrinsic_computations_mask, p.fix_cameras + cps * c, full);
+      for (int j = 0; j < 10; ++j) {
+        cam64[10 * (cb + c) + j] = full[j];
+        cam32[10 * (cb + c) + j] = float(full[j]);
+      }
+    }
+    for (int i = 0; i < ni; ++i) {
+      img_cam[ib + i] = int(cb + p.image_camera_map[i]);
+      img_prob[ib + i] = q;
+    }
+    // point-major order: counting sort by point, then image within point
+    std::vector<int> cnt(np + 1, 0);
+    for (int k = 0; k < nk; ++k) cnt[p.feature_maps[2 * k + 1] + 1]++;
+    for (int i = 0; i < np; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> order(nk);
+    {
+      std::vector<int> cur(cnt.begin(), cnt.end() - 1);
+      for (int k = 0; k < nk; ++k) order[cur[p.feature_maps[2 * k + 1]]++] = k;
+    }
+    for (int i = 0; i < np; ++i) {
+      std::sort(order.begin() + cnt[i], order.begin() + cnt[i + 1], [&](int a, int b) {
+        return p.feature_maps[2 * a] < p.feature_maps[2 * b];
+      });
+      for (int t = cnt[i] + 1; t < cnt[i + 1]; ++t)
+        if (p.feature_maps[2 * order[t]] == p.feature_maps[2 * order[t - 1]]) return GBA_ERR_DUPLICATE;
+    }
+    key_sorted_to_orig[q] = order;
+    const double* y = near_ys[q];
+    for (int t = 0; t < nk; ++t) {
+      const int k = order[t];
+      key_img[kb + t] = int(ib + p.feature_maps[2 * k]);
+      key_pt[kb + t] = int(pb + p.feature_maps[2 * k + 1]);
+      key_obs[kb + t] = make_double2(y[2 * k], y[2 * k + 1]);
+      if (any_weights) {
+        double l00 = 1, l10 = 0, l11 = 1;
+        if (p.key_covariance_inverse) {
+          const double* L = p.key_covariance_inverse + 4 * k;
+          double a = L[0], bb = 0.5 * (L[1] + L[2]), dd = L[3];
+          if (!(a > 0)) return GBA_ERR_INVALID;
+          l00 = std::sqrt(a);
+          l10 = bb / l00;
+          double r = dd - l10 * l10;
+          if (!(r > 0)) return GBA_ERR_INVALID;
+          l11 = std::sqrt(r);
+        }
+        key_wl[3 * (kb + t)] = l00;
+        key_wl[3 * (kb + t) + 1] = l10;
+        key_wl[3 * (kb + t) + 2] = l11;
+      }
+    }
+    for (int i = 0; i < np; ++i) {
+      pt_key_off[pb + i + 1] = int(kb + cnt[i + 1]);
+      pt_prob[pb + i] = q;
+    }
+    pt_key_off[pb] = int(kb);
+    // per-image key lists (by point, since keys are point-major)
+    {
+      std::vector<int> ic(ni + 1, 0);
+      for (int t = 0; t < nk; ++t) ic[key_img[kb + t] - ib + 1]++;
+      for (int i = 0; i < ni; ++i) ic[i + 1] += ic[i];
+      std::vector<int> cur(ic.begin(), ic.end() - 1);
+      for (int t = 0; t < nk; ++t) {
+        int li = key_img[kb + t] - int(ib);
+        img_keys[kb + cur[li]++] = int(kb + t);
+      }
+      for (int i = 0; i <= ni; ++i) img_key_off[ib + i] = int(kb + ic[i]);
+    }
+    // reduced-system blocks: (i <= j) with their key pairs, point order
+    {
+      std::vector<long long> bcount((size_t)ni * ni, 0);  // index j*ni + i? use (lo*ni + hi)
+      for (int i = 0; i < np; ++i) {
+        const int b0 = cnt[i], b1 = cnt[i + 1];
+        for (int a = b0; a < b1; ++a) {
+          const int ia = key_img[kb + a] - int(ib);
+          for (int c = a; c < b1; ++c) {
+            const int ic2 = key_img[kb + c] - int(ib);
+            bcount[(size_t)ia * ni + ic2]++;
+          }
+        }
+      }
+      // every image gets a diagonal block (so S keeps U_i + mu I even for an
+      // image without keys)
+      std::vector<int> bid((size_t)ni * ni, -1);
+      const int block_begin = int(blk_ij.size());
+      std::vector<long long> boff;
+      long long pair_base = (long long)pairs.size();
+      long long acc = pair_base;
+      for (int a = 0; a < ni; ++a)
+        for (int c = a; c < ni; ++c) {
+          const long long n_ = bcount[(size_t)a * ni + c];
+          if (n_ == 0 && a != c) continue;
+          bid[(size_t)a * ni + c] = int(blk_ij.size());
+          blk_ij.push_back(make_int2(a, c));
+          boff.push_back(acc);
+          acc += n_;
+        }
+      const int nblk = int(blk_ij.size()) - block_begin;
+      if (acc > INT32_MAX) return GBA_ERR_INVALID;
+      pairs.resize(acc);
+      std::vector<long long> cur(boff);
+      for (int i = 0; i < np; ++i) {
+        const int b0 = cnt[i], b1 = cnt[i + 1];
+        for (int a = b0; a < b1; ++a) {
+          const int ia = key_img[kb + a] - int(ib);
+          for (int c = a; c < b1; ++c) {
+            const int ic2 = key_img[kb + c] - int(ib);
+            const int blk = bid[(size_t)ia * ni + ic2] - block_begin;
+            pairs[cur[blk]++] = make_int2(int(kb + a), int(kb + c));
+          }
+        }
+      }
+      pi.block_begin = block_begin;
+      pi.num_blocks = nblk;
+      pi.item_begin = int(items.size());
+      for (int t = 0; t < nblk; ++t) {
+        const long long s0 = boff[t], s1 = (t + 1 < nblk) ? boff[t + 1] : acc;
+        long long s = s0;
+        do {
+          long long e = std::min(s1, s + kPairItem);
+          items.push_back(make_int4(block_begin + t, int(s), int(e), q));
+          s = e;
+        } while (s < s1);
+        blk_item_off.push_back(int(items.size()));
+      }
+      pi.num_items = int(items.size()) - pi.item_begin;
+      // dense map for the assembly of the lower triangle: map[j*ni + i], j <= i
+      blk_map_off[q] = (long long)blk_map.size();
+      blk_map.resize(blk_map.size() + (size_t)ni * ni, -1);
+      for (int a = 0; a < ni; ++a)
+        for (int c = a; c < ni; ++c)
+          blk_map[blk_map_off[q] + (size_t)a * ni + c] = bid[(size_t)a * ni + c];
+    }
+    // work chunks
+    for (int s = 0; s < nk; s += kKeyChunk)
+      key_chunks.push_back(Chunk{q, int(kb + s), int(kb + std::min(nk, s + kKeyChunk)), 0});
+    prob_key_chunk_off.push_back(int(key_chunks.size()));
+    for (int s = 0; s < np; s += kPointChunk)
+      pt_chunks.push_back(Chunk{q, int(pb + s), int(pb + std::min(np, s + kPointChunk)), 0});
+    prob_pt_chunk_off.push_back(int(pt_chunks.size()));
+    for (int s = 0; s < ni; s += kImageChunk)
+      img_chunks.push_back(Chunk{q, int(ib + s), int(ib + std::min(ni, s + kImageChunk)), 0});
+    prob_img_chunk_off.push_back(int(img_chunks.size()));
+    pb += np;
+    ib += ni;
+    kb += nk;
+    cb += p.number_of_cameras;
+  }
+
+  // ---- device allocations
+  DevPlan& D = d;
+  D.B = nprob;
+  D.precision = opt.precision;
+  D.loss = opt.loss;
+  D.huber_delta = opt.huber_delta;
+  D.tau = opt.tau;
+  D.eps1 = opt.eps1;
+  D.eps2 = opt.eps2;
+  D.max_iterations = opt.max_iterations;
+  D.has_key_weights = any_weights;
+  D.max_n = max_n;
+  D.max_nt = max_nt;
+  D.prob = arena.upload(prob);
+  D.state = arena.alloc<LMState>(nprob);
+  D.K = int(K);
+  D.key_img = arena.upload(key_img);
+  D.key_pt = arena.upload(key_pt);
+  D.key_obs = arena.upload(key_obs);
+  D.key_wl = any_weights ? arena.upload(key_wl) : nullptr;
+  D.P = int(P);
+  D.pt_key_off = arena.upload(pt_key_off);
+  D.pt_prob = arena.upload(pt_prob);
+  D.I = int(I);
+  D.img_key_off = arena.upload(img_key_off);
+  D.img_keys = arena.upload(img_keys);
+  D.img_prob = arena.upload(img_prob);
+  D.img_cam = arena.upload(img_cam);
+  D.cam64 = arena.upload(cam64);
+  D.cam32 = arena.upload(cam32);
+  for (int t = 0; t < 2; ++t) {
+    D.x_pt[t] = arena.alloc<double>(3 * P);
+    D.x_img[t] = arena.alloc<double>(6 * I);
+    D.img_rot[t] = arena.alloc<double>(12 * I);
+    D.img_lin[t] = arena.alloc<char>(12 * I * tsz);
+    D.RW[t] = arena.alloc<char>(4 * K * tsz);
+  }
+  D.x0_pt = arena.alloc<double>(3 * P);
+  D.x0_img = arena.alloc<double>(6 * I);
+  D.JR = arena.alloc<char>(size_t(kJRStride) * K * tsz);
+  D.Z = arena.alloc<char>(size_t(kZStride) * K * tsz);
+  D.PV = arena.alloc<char>(12 * P * tsz);
+  D.PS = arena.alloc<char>(12 * P * tsz);
+  D.U = arena.alloc<double>(36 * I);
+  D.gi = arena.alloc<double>(6 * I);
+  D.S = arena.alloc<double>(size_t(std::max<long long>(s_off, 1)));
+  D.b = arena.alloc<double>(6 * I);
+  D.Linv = arena.alloc<double>(size_t(nprob) * std::max(max_nt, 1) * kTile * kTile);
+  D.factor_flag = arena.alloc<int>(nprob);
+  D.pairs = arena.upload(pairs);
+  D.items = arena.upload(items);
+  D.blk_ij = arena.upload(blk_ij);
+  D.blk_item_off = arena.upload(blk_item_off);
+  D.n_items = int(items.size());
+  D.n_blocks = int(blk_ij.size());
+  D.blk_map = arena.upload(blk_map);
+  D.blk_map_off = arena.upload(blk_map_off);
+  D.item_partial = arena.alloc<double>(size_t(kItemStride) * std::max<size_t>(items.size(), 1));
+  D.n_key_chunks = int(key_chunks.size());
+  D.n_pt_chunks = int(pt_chunks.size());
+  D.n_img_chunks = int(img_chunks.size());
+  D.key_chunks = arena.upload(key_chunks);
+  D.pt_chunks = arena.upload(pt_chunks);
+  D.img_chunks = arena.upload(img_chunks);
+  D.prob_key_chunk_off = arena.upload(prob_key_chunk_off);
+  D.prob_pt_chunk_off = arena.upload(prob_pt_chunk_off);
+  D.prob_img_chunk_off = arena.upload(prob_img_chunk_off);
+  D.key_chunk_sum = arena.alloc<double>(std::max<size_t>(key_chunks.size(), 1));
+  D.pt_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(pt_chunks.size(), 1));
+  D.img_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(img_chunks.size(), 1));
+  D.launch_counter = nullptr;
+  GBA_CUDA(cudaMemset(D.state, 0, sizeof(LMState) * nprob));
+  GBA_CUDA(cudaDeviceSynchronize());
+  setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return GBA_OK;
+}
+
+// The launch sequence of one solve.  When profiling, an event is recorded
+// after each stage and tagged with it.
+void Plan::enqueue(bool profile) {
+  cudaStream_t s = stream;
+  long long n = 0;
+  size_t ev_i = 0;
+  auto mark = [&](int stage) {
+    if (!profile) return;
+    GBA_CUDA(cudaEventRecord(prof_events[ev_i], s));
+    prof_stage[ev_i] = stage;
+    ++ev_i;
+  };
+  mark(-1);
+  n += launch_init(d, s);
+  n += launch_image_prep(d, 0, s);
+  n += launch_cost(d, 0, s);
+  n += launch_ctrl_initial_cost(d, s);
+  mark(GBA_STAGE_COST);
+  n += launch_linearize(d, s);
+  n += launch_image_reduce(d, s);
+  n += launch_ctrl_after_linearize(d, s);
+  mark(GBA_STAGE_LINEARIZE);
+  for (int it = 0; it < opt.max_iterations; ++it) {
+    n += launch_point_schur(d, s);
+    mark(GBA_STAGE_POINT_SCHUR);
+    n += launch_assemble_items(d, s);
+    mark(GBA_STAGE_ASSEMBLE);
+    n += launch_assemble_S(d, s);
+    mark(GBA_STAGE_OTHER);
+    n += launch_cholesky(d, s);
+    mark(GBA_STAGE_FACTOR);
+    n += launch_backsub(d, s);
+    mark(GBA_STAGE_BACKSUB);
+    n += launch_ctrl_step(d, s);
+    mark(GBA_STAGE_CONTROL);
+    n += launch_image_prep(d, 1, s);
+    n += launch_cost(d, 1, s);
+    mark(GBA_STAGE_COST);
+    n += launch_ctrl_accept(d, s);
+    mark(GBA_STAGE_CONTROL);
+    n += launch_linearize(d, s);
+    n += launch_image_reduce(d, s);
+    n += launch_ctrl_after_linearize(d, s);
+    mark(GBA_STAGE_LINEARIZE);
+  }
+  GBA_CUDA(cudaGetLastError());
+  launches_last_run = n;
+}
+
+int Plan::run() {
+  const bool profile = opt.profile != 0;
+  if (profile) {
+    const size_t need = 8 + size_t(opt.max_iterations) * 12;
+    while (prof_events.size() < need) {
+      cudaEvent_t e;
+      GBA_CUDA(cudaEventCreate(&e));
+      prof_events.push_back(e);
+    }
+    prof_stage.assign(prof_events.size(), -2);
+  }
+  GBA_CUDA(cudaSetDevice(device));
+  GBA_CUDA(cudaEventRecord(ev0, stream));
+  if (opt.use_cuda_graph) {
+    if (!graph_exec) {
+      cudaGraph_t g;
+      GBA_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        enqueue(profile);
+      } catch (...) {
+        cudaStreamEndCapture(stream, &g);
+        throw;
+      }
+      GBA_CUDA(cudaStreamEndCapture(stream, &g));
+      GBA_CUDA(cudaGraphInstantiate(&graph_exec, g, 0));
+      cudaGraphDestroy(g);
+    }
+    GBA_CUDA(cudaGraphLaunch(graph_exec, stream));
+  } else {
+    enqueue(profile);
+  }
+  GBA_CUDA(cudaEventRecord(ev1, stream));
+  g_launches += launches_last_run;
+  ran = true;
+  return GBA_OK;
+}
+
+int Plan::sync() {
+  GBA_CUDA(cudaStreamSynchronize(stream));
+  GBA_CUDA(cudaGetLastError());
+  if (opt.profile) {
+    std::fill(stage_ms, stage_ms + GBA_NUM_STAGES, 0.0);
+    for (size_t i = 1; i < prof_stage.size(); ++i) {
+      if (prof_stage[i] < 0) break;
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, prof_events[i - 1], prof_events[i]) != cudaSuccess) {
+        cudaGetLastError();
+        ms = 0;
+      }
+      stage_ms[prof_stage[i]] += ms;
+    }
+  }
+  return GBA_OK;
+}
+
+}  // namespace gba
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+struct gba_plan {
+  gba::Plan impl;
+};
+
+namespace {
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const gba::CudaError& e) {
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    return GBA_ERR_OOM;
+  } catch (...) {
+    return GBA_ERR;
+  }
+}
+
+int check_device() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return GBA_ERR_NO_DEVICE;
+  }
+  return GBA_OK;
+}
+
+double bits_to_double(unsigned long long b) {
+  double v;
+  std::memcpy(&v, &b, sizeof(v));
+  return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t gba_params_per_camera(uint32_t m) { return gba::params_per_camera(m); }
+
+int64_t gba_x_size(const gba_problem* p) {
+  if (!p) return -1;
+  int64_t n = 0;
+  if (!(p->fix_mask & GBA_FIX_POINTS)) n += 3 * p->number_of_points;
+  if (!(p->fix_mask & GBA_FIX_IMAGES)) n += 6 * p->number_of_images;
+  if (!(p->fix_mask & GBA_FIX_CAMERAS))
+    n += gba::params_per_camera(p->intrinsic_computations_mask) * p->number_of_cameras;
+  return n;
+}
+
+int64_t gba_y_size(const gba_problem* p) {
+  if (!p) return -1;
+  int64_t n = 2 * p->number_of_keys;
+  if (!(p->fix_mask & GBA_FIX_POINTS))
+    for (int64_t c = 0; c < p->number_of_point_constraints; ++c) {
+      uint32_t m = p->point_constraints[c].mask;
+      n += ((m & 1) != 0) + ((m & 2) != 0) + ((m & 4) != 0);
+    }
+  if (!(p->fix_mask & GBA_FIX_IMAGES))
+    for (int64_t c = 0; c < p->number_of_image_constraints; ++c) {
+      uint32_t m = p->image_constraints[c].mask;
+      n += ((m & 1) ? 3 : 0) + ((m & 2) != 0) + ((m & 4) != 0) + ((m & 8) != 0);
+    }
+  if (!(p->fix_mask & GBA_FIX_CAMERAS))
+    for (int64_t c = 0; c < p->number_of_camera_constraints; ++c) {
+      const gba_camera_constraint& cc = p->camera_constraints[c];
+      n += __builtin_popcount(cc.radial_mask & 7u) + __builtin_popcount(cc.decentering_mask & 3u) +
+           __builtin_popcount(cc.intrinsic_mask & 31u);
+    }
+  return n;
+}
+
+void gba_default_options(gba_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->max_iterations = 50;
+  o->tau = 1e-3;
+  o->eps1 = 1e-8;
+  o->eps2 = 1e-8;
+  o->precision = GBA_PRECISION_FP64;
+  o->loss = GBA_LOSS_TRIVIAL;
+  o->huber_delta = 1.0;
+  o->linear_solver = GBA_LINEAR_DENSE_CHOLESKY;
+  o->pcg_max_iterations = 100;
+  o->pcg_relative_tolerance = 1e-6;
+  o->use_cuda_graph = 1;
+  o->profile = 0;
+  o->device = 0;
+}
+
+const char* gba_status_string(int s) {
+  switch (s) {
+    case GBA_OK: return "ok";
+    case GBA_ERR: return "failure";
+    case GBA_ERR_INVALID: return "invalid argument or size mismatch";
+    case GBA_ERR_BAD_INDEX: return "image/point/camera id out of range";
+    case GBA_ERR_DUPLICATE: return "duplicate (image, point) key";
+    case GBA_ERR_UNSUPPORTED: return "model variant not supported on the device path";
+    case GBA_ERR_NOT_SPD: return "reduced system not positive definite";
+    case GBA_ERR_NAN: return "non-finite cost";
+    case GBA_ERR_OOM: return "device out of memory";
+    case GBA_ERR_CUDA: return "CUDA runtime error";
+    case GBA_ERR_TIMEOUT: return "bounded device wait ran out";
+    case GBA_ERR_NO_DEVICE: return "no CUDA device";
+    case GBA_ERR_BUSY: return "admission refused";
+    case GBA_ERR_CANCELLED: return "cancelled";
+    default: return "unknown status";
+  }
+}
+
+const char* gba_version(void) { return "gba 0.1 (sm_103a)"; }
+
+int64_t gba_kernel_launch_count(void) { return gba::g_launches.load(); }
+
+int gba_plan_create(const gba_problem* problems, const double* const* near_ys, int32_t n,
+                    const gba_options* options, gba_plan** out) {
+  if (!problems || !options || !out || n <= 0) return GBA_ERR_INVALID;
+  *out = nullptr;
+  if (int e = check_device()) return e;
+  if (options->linear_solver != GBA_LINEAR_DENSE_CHOLESKY) return GBA_ERR_UNSUPPORTED;
+  if (options->precision != GBA_PRECISION_FP64 && options->precision != GBA_PRECISION_MIXED)
+    return GBA_ERR_INVALID;
+  if (options->max_iterations < 0) return GBA_ERR_INVALID;
+  gba_plan* p = nullptr;
+  try {
+    p = new gba_plan();
+  } catch (...) {
+    return GBA_ERR_OOM;
+  }
+  int err = guarded([&] { return p->impl.build(problems, near_ys, n, options); });
+  if (err) {
+    delete p;
+    return err;
+  }
+  *out = p;
+  return GBA_OK;
+}
+
+int gba_plan_destroy(gba_plan* p) {
+  delete p;
+  return GBA_OK;
+}
+
+int gba_plan_number_of_problems(const gba_plan* p) { return p ? p->impl.B : 0; }
+
+int gba_plan_set_initial_x(gba_plan* p, int32_t q, const double* x0) {
+  if (!p || !x0 || q < 0 || q >= p->impl.B) return GBA_ERR_INVALID;
+  return guarded([&] {
+    gba::Plan& P = p->impl;
+    const gba::ProbInfo& pi = P.prob[q];
+    GBA_CUDA(cudaMemcpy(const_cast<double*>(P.d.x0_pt) + 3LL * pi.point_begin, x0,
+                        sizeof(double) * 3 * pi.num_points, cudaMemcpyHostToDevice));
+    GBA_CUDA(cudaMemcpy(const_cast<double*>(P.d.x0_img) + 6LL * pi.image_begin,
+                        x0 + 3LL * pi.num_points, sizeof(double) * 6 * pi.num_images,
+                        cudaMemcpyHostToDevice));
+    P.h2d_bytes += (long long)sizeof(double) * (3LL * pi.num_points + 6LL * pi.num_images);
+    return GBA_OK;
+  });
+}
+
+int gba_plan_run(gba_plan* p) {
+  if (!p) return GBA_ERR_INVALID;
+  return guarded([&] { return p->impl.run(); });
+}
+
+int gba_plan_synchronize(gba_plan* p) {
+  if (!p) return GBA_ERR_INVALID;
+  return guarded([&] { return p->impl.sync(); });
+}
+
+int gba_plan_get_x(gba_plan* p, int32_t q, double* x) {
+  if (!p || !x || q < 0 || q >= p->impl.B) return GBA_ERR_INVALID;
+  return guarded([&] {
+    gba::Plan& P = p->impl;
+    gba::LMState st;
+    GBA_CUDA(cudaMemcpy(&st, P.d.state + q, sizeof(st), cudaMemcpyDeviceToHost));
+    const gba::ProbInfo& pi = P.prob[q];
+    const int par = P.ran ? st.parity : 0;
+    const double* xp = P.ran ? P.d.x_pt[par] : P.d.x0_pt;
+    const double* xi = P.ran ? P.d.x_img[par] : P.d.x0_img;
+    GBA_CUDA(cudaMemcpy(x, xp + 3LL * pi.point_begin, sizeof(double) * 3 * pi.num_points,
+                        cudaMemcpyDeviceToHost));
+    GBA_CUDA(cudaMemcpy(x + 3LL * pi.num_points, xi + 6LL * pi.image_begin,
+                        sizeof(double) * 6 * pi.num_images, cudaMemcpyDeviceToHost));
+    P.d2h_bytes += (long long)sizeof(st) +
+                   (long long)sizeof(double) * (3LL * pi.num_points + 6LL * pi.num_images);
+    return GBA_OK;
+  });
+}
+
+int gba_plan_get_report(gba_plan* p, int32_t q, gba_report* r) {
+  if (!p || !r || q < 0 || q >= p->impl.B) return GBA_ERR_INVALID;
+  return guarded([&] {
+    gba::Plan& P = p->impl;
+    gba::LMState st;
+    GBA_CUDA(cudaMemcpy(&st, P.d.state + q, sizeof(st), cudaMemcpyDeviceToHost));
+    std::memset(r, 0, sizeof(*r));
+    r->status = st.status;
+    r->stop_reason = st.stop;
+    r->iterations = st.iter;
+    r->accepted = st.accepted;
+    r->rejected = st.rejected;
+    r->factor_failures = st.factor_fail;
+    r->pcg_iterations = st.pcg_iters;
+    r->initial_cost = st.initial_cost;
+    r->final_cost = st.F;
+    const int K = P.prob[q].num_keys;
+    r->final_rmse = K > 0 ? std::sqrt(std::max(st.F, 0.0) / K) : 0.0;
+    r->final_mu = st.mu;
+    r->final_gradient_inf_norm = bits_to_double(st.ginf_bits);
+    r->setup_ms = P.setup_ms;
+    float ms = 0;
+    if (P.ran) cudaEventElapsedTime(&ms, P.ev0, P.ev1);
+    r->solve_ms = ms;
+    for (int s = 0; s < GBA_NUM_STAGES; ++s) r->stage_ms[s] = P.stage_ms[s];
+    P.d2h_bytes += (long long)sizeof(st);
+    r->h2d_bytes = P.h2d_bytes + P.arena.uploaded;
+    r->d2h_bytes = P.d2h_bytes;
+    return GBA_OK;
+  });
+}
+
+int gba_plan_last_run_ms(gba_plan* p, double* ms) {
+  if (!p || !ms) return GBA_ERR_INVALID;
+  return guarded([&] {
+    float f = 0;
+    GBA_CUDA(cudaEventElapsedTime(&f, p->impl.ev0, p->impl.ev1));
+    *ms = f;
+    return GBA_OK;
+  });
+}
+
+int gba_plan_kernel_stats(gba_plan* p, int32_t stage, double* total_ms, int32_t* launches) {
+  if (!p || stage < 0 || stage >= GBA_NUM_STAGES) return GBA_ERR_INVALID;
+  if (total_ms) *total_ms = p->impl.stage_ms[stage];
+  if (launches) *launches = p->impl.opt.max_iterations;
+  return GBA_OK;
+}
+
+int gba_plan_last_run_launches(gba_plan* p, int64_t* n) {
+  if (!p || !n) return GBA_ERR_INVALID;
+  *n = p->impl.launches_last_run;
+  return GBA_OK;
+}
+
+int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, int32_t n,
+                    const gba_options* options, double* const* x_inout, gba_report* reports) {
+  if (!x_inout) return GBA_ERR_INVALID;
+  gba_plan* plan = nullptr;
+  int err = gba_plan_create(problems, near_ys, n, options, &plan);
+  if (err) return err;
+  for (int q = 0; q < n && !err; ++q) err = gba_plan_set_initial_x(plan, q, x_inout[q]);
+  if (!err) err = gba_plan_run(plan);
+  if (!err) err = gba_plan_synchronize(plan);
+  for (int q = 0; q < n && !err; ++q) {
+    err = gba_plan_get_x(plan, q, x_inout[q]);
+    if (!err && reports) err = gba_plan_get_report(plan, q, &reports[q]);
+  }
+  int first_status = GBA_OK;
+  if (!err && reports)
+    for (int q = 0; q < n; ++q)
+      if (reports[q].status != GBA_OK) { first_status = reports[q].status; break; }
+  gba_plan_destroy(plan);
+  return err ? err : first_status;
+}
+
+int gba_solve(const gba_problem* problem, const double* near_y, const gba_options* options,
+              double* x_inout, gba_report* report) {
+  const double* ys[1] = {near_y};
+  double* xs[1] = {x_inout};
+  gba_report local;
+  return gba_solve_batch(problem, ys, 1, options, xs, report ? report : &local);
+}
+
+// ---- single-stage entry points ---------------------------------------------
+namespace {
+
+// A plan for one problem at x, brought to the point where the image
+// rotations of x exist on the device.
+int stage_plan(const gba_problem* problem, const double* near_y, const double* x,
+               int precision, gba_plan** out, gba_options* opt_out) {
+  gba_options o;
+  gba_default_options(&o);
+  o.precision = precision;
+  o.max_iterations = 1;
+  o.eps1 = -1.0;
+  o.eps2 = -1.0;
+  o.use_cuda_graph = 0;
+  std::vector<double> zeros;
+  if (!near_y) {
+    zeros.assign(std::max<int64_t>(gba_y_size(problem), 0), 0.0);
+    near_y = zeros.data();
+  }
+  int err = gba_plan_create(problem, &near_y, 1, &o, out);
+  if (err) return err;
+  err = gba_plan_set_initial_x(*out, 0, x);
+  if (err) {
+    gba_plan_destroy(*out);
+    return err;
+  }
+  if (opt_out) *opt_out = o;
+  return GBA_OK;
+}
+
+}  // namespace
+
+int gba_vector_function(const gba_problem* problem, const double* x, double* y, int32_t precision) {
+  if (!problem || !x || !y) return GBA_ERR_INVALID;
+  gba_plan* plan = nullptr;
+  int err = stage_plan(problem, nullptr, x, precision, &plan, nullptr);
+  if (err) return err;
+  err = guarded([&] {
+    gba::Plan& P = plan->impl;
+    cudaStream_t s = P.stream;
+    gba::launch_init(P.d, s);
+    gba::launch_image_prep(P.d, 0, s);
+    double* dy = P.arena.alloc<double>(2 * std::max(P.d.K, 1));
+    gba::launch_vector_function(P.d, dy, s);
+    gba::g_launches += 4;
+    GBA_CUDA(cudaStreamSynchronize(s));
+    GBA_CUDA(cudaGetLastError());
+    std::vector<double> ys(2 * P.d.K);
+    GBA_CUDA(cudaMemcpy(ys.data(), dy, sizeof(double) * ys.size(), cudaMemcpyDeviceToHost));
+    const auto& perm = P.key_sorted_to_orig[0];
+    for (int t = 0; t < P.d.K; ++t) {
+      y[2 * perm[t]] = ys[2 * t];
+      y[2 * perm[t] + 1] = ys[2 * t + 1];
+    }
+    return GBA_OK;
+  });
+  gba_plan_destroy(plan);
+  return err;
+}
+
+int gba_jacobian(const gba_problem* problem, const double* x, double* point_blocks,
+                 double* image_blocks, double* camera_blocks, int32_t precision) {
+  (void)camera_blocks;
+  if (!problem || !x) return GBA_ERR_INVALID;
+  gba_plan* plan = nullptr;
+  int err = stage_plan(problem, nullptr, x, precision, &plan, nullptr);
+  if (err) return err;
+  err = guarded([&] {
+    gba::Plan& P = plan->impl;
+    cudaStream_t s = P.stream;
+    gba::launch_init(P.d, s);
+    gba::launch_image_prep(P.d, 0, s);
+    const int K = std::max(P.d.K, 1);
+    double* jp = P.arena.alloc<double>(6 * K);
+    double* ji = P.arena.alloc<double>(12 * K);
+    gba::launch_jacobian_out(P.d, jp, ji, s);
+    gba::g_launches += 4;
+    GBA_CUDA(cudaStreamSynchronize(s));
+    GBA_CUDA(cudaGetLastError());
+    std::vector<double> hp(6 * P.d.K), hi(12 * P.d.K);
+    GBA_CUDA(cudaMemcpy(hp.data(), jp, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost));
+    GBA_CUDA(cudaMemcpy(hi.data(), ji, sizeof(double) * hi.size(), cudaMemcpyDeviceToHost));
+    const auto& perm = P.key_sorted_to_orig[0];
+    for (int t = 0; t < P.d.K; ++t) {
+      if (point_blocks) std::copy(&hp[6 * t], &hp[6 * t] + 6, point_blocks + 6LL * perm[t]);
+      if (image_blocks) std::copy(&hi[12 * t], &hi[12 * t] + 12, image_blocks + 12LL * perm[t]);
+    }
+    return GBA_OK;
+  });
+  gba_plan_destroy(plan);
+  return err;
+}
+
+int gba_cost(const gba_problem* problem, const double* x, const double* near_y,
+             const gba_options* options, double* cost) {
+  if (!problem || !x || !near_y || !cost) return GBA_ERR_INVALID;
+  gba_options o;
+  gba_default_options(&o);
+  if (options) o = *options;
+  gba_plan* plan = nullptr;
+  int err = stage_plan(problem, near_y, x, o.precision, &plan, nullptr);
+  if (err) return err;
+  err = guarded([&] {
+    gba::Plan& P = plan->impl;
+    P.d.loss = o.loss;
+    P.d.huber_delta = o.huber_delta;
+    cudaStream_t s = P.stream;
+    gba::launch_init(P.d, s);
+    gba::launch_image_prep(P.d, 0, s);
+    gba::launch_cost(P.d, 0, s);
+    gba::launch_ctrl_initial_cost(P.d, s);
+    gba::g_launches += 5;
+    GBA_CUDA(cudaStreamSynchronize(s));
+    GBA_CUDA(cudaGetLastError());
+    gba::LMState st;
+    GBA_CUDA(cudaMemcpy(&st, P.d.state, sizeof(st), cudaMemcpyDeviceToHost));
+    *cost = st.F;
+    return std::isfinite(st.F) ? GBA_OK : GBA_ERR_NAN;
+  });
+  gba_plan_destroy(plan);
+  return err;
+}
+
+int gba_schur_step(const gba_problem* problem, const double* x, const double* near_y, double mu,
+                   const gba_options* options, double* delta_x) {
+  if (!problem || !x || !near_y || !delta_x) return GBA_ERR_INVALID;
+  gba_options o;
+  gba_default_options(&o);
+  if (options) o = *options;
+  gba_plan* plan = nullptr;
+  int err = stage_plan(problem, near_y, x, o.precision, &plan, nullptr);
+  if (err) return err;
+  err = guarded([&] {
+    gba::Plan& P = plan->impl;
+    P.d.loss = o.loss;
+    P.d.huber_delta = o.huber_delta;
+    cudaStream_t s = P.stream;
+    gba::launch_init(P.d, s);
+    gba::launch_image_prep(P.d, 0, s);
+    gba::launch_cost(P.d, 0, s);
+    gba::launch_ctrl_initial_cost(P.d, s);
+    gba::launch_linearize(P.d, s);
+    gba::launch_image_reduce(P.d, s);
+    gba::launch_ctrl_after_linearize(P.d, s);
+    GBA_CUDA(cudaStreamSynchronize(s));
+    // override mu
+    GBA_CUDA(cudaMemcpy(reinterpret_cast<char*>(P.d.state) + offsetof(gba::LMState, mu), &mu,
+                        sizeof(double), cudaMemcpyHostToDevice));
+    gba::launch_point_schur(P.d, s);
+    gba::launch_assemble(P.d, s);
+    gba::launch_cholesky(P.d, s);
+    gba::launch_backsub(P.d, s);
+    gba::g_launches += 12;
+    GBA_CUDA(cudaStreamSynchronize(s));
+    GBA_CUDA(cudaGetLastError());
+    int flag = 0;
+    GBA_CUDA(cudaMemcpy(&flag, P.d.factor_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return GBA_ERR_NOT_SPD;
+    const gba::ProbInfo& pi = P.prob[0];
+    std::vector<double> x0p(3 * pi.num_points), x1p(3 * pi.num_points), di(6 * pi.num_images);
+    GBA_CUDA(cudaMemcpy(x0p.data(), P.d.x_pt[0], sizeof(double) * x0p.size(), cudaMemcpyDeviceToHost));
+    GBA_CUDA(cudaMemcpy(x1p.data(), P.d.x_pt[1], sizeof(double) * x1p.size(), cudaMemcpyDeviceToHost));
+    GBA_CUDA(cudaMemcpy(di.data(), P.d.b, sizeof(double) * di.size(), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < x0p.size(); ++i) delta_x[i] = x0p[i] - x1p[i];
+    std::copy(di.begin(), di.end(), delta_x + x0p.size());
+    return GBA_OK;
+  });
+  gba_plan_destroy(plan);
+  return err;
+}
+
+}  // extern "C"

@@ -1,0 +1,219 @@
+"""ctypes binding of libgba.so (include/gba.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+visible, every call raises.  The library is built in-tree by
+hs_sfm_gb300/build.py (``python -c "import __graft_entry__ as g; g.build()"``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libgba.so")
+_lib = None
+
+
+class GbaError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = lib().gba_status_string(status).decode() if _lib is not None else str(status)
+        super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libgba.so is not built ({LIB_PATH}); run hs_sfm_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    P = C.POINTER(abi.Problem)
+    d = C.POINTER(C.c_double)
+    O = C.POINTER(abi.Options)
+    R = C.POINTER(abi.Report)
+    vp = C.c_void_p
+    L.gba_status_string.restype = C.c_char_p
+    L.gba_status_string.argtypes = [C.c_int]
+    L.gba_version.restype = C.c_char_p
+    L.gba_kernel_launch_count.restype = C.c_int64
+    L.gba_x_size.restype = C.c_int64
+    L.gba_x_size.argtypes = [P]
+    L.gba_y_size.restype = C.c_int64
+    L.gba_y_size.argtypes = [P]
+    L.gba_params_per_camera.restype = C.c_int64
+    L.gba_params_per_camera.argtypes = [C.c_uint32]
+    L.gba_default_options.argtypes = [O]
+    L.gba_solve.argtypes = [P, d, O, d, R]
+    L.gba_solve_batch.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(d), R]
+    L.gba_plan_create.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(vp)]
+    L.gba_plan_destroy.argtypes = [vp]
+    L.gba_plan_number_of_problems.argtypes = [vp]
+    L.gba_plan_set_initial_x.argtypes = [vp, C.c_int32, d]
+    L.gba_plan_run.argtypes = [vp]
+    L.gba_plan_synchronize.argtypes = [vp]
+    L.gba_plan_get_x.argtypes = [vp, C.c_int32, d]
+    L.gba_plan_get_report.argtypes = [vp, C.c_int32, R]
+    L.gba_plan_last_run_ms.argtypes = [vp, d]
+    L.gba_plan_kernel_stats.argtypes = [vp, C.c_int32, d, C.POINTER(C.c_int32)]
+    L.gba_plan_last_run_launches.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.gba_vector_function.argtypes = [P, d, d, C.c_int32]
+    L.gba_jacobian.argtypes = [P, d, d, d, d, C.c_int32]
+    L.gba_cost.argtypes = [P, d, d, O, d]
+    L.gba_schur_step.argtypes = [P, d, d, C.c_double, O, d]
+    _lib = L
+    return L
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _check(status, what):
+    if status != abi.GBA_OK:
+        raise GbaError(status, what)
+
+
+def solve(scene, options=None, x0=None, near_y=None):
+    """One problem through gba_solve (host buffers).  Returns (x, report)."""
+    L = lib()
+    cp = abi.CProblem(scene)
+    x = _f64(scene.x0 if x0 is None else x0).copy()
+    y = _f64(scene.near_y if near_y is None else near_y)
+    opt = options if options is not None else abi.make_options()
+    rep = abi.Report()
+    st = L.gba_solve(cp.ref, abi.dptr(y), C.byref(opt), abi.dptr(x), C.byref(rep))
+    _check(st, "gba_solve")
+    return x, rep
+
+
+def solve_batch(scenes, options=None):
+    L = lib()
+    cps = [abi.CProblem(s) for s in scenes]
+    arr = (abi.Problem * len(cps))(*[c.problem for c in cps])
+    ys = [_f64(s.near_y) for s in scenes]
+    xs = [_f64(s.x0).copy() for s in scenes]
+    yp = (C.POINTER(C.c_double) * len(ys))(*[abi.dptr(y) for y in ys])
+    xp = (C.POINTER(C.c_double) * len(xs))(*[abi.dptr(x) for x in xs])
+    reps = (abi.Report * len(scenes))()
+    opt = options if options is not None else abi.make_options()
+    st = L.gba_solve_batch(arr, yp, len(scenes), C.byref(opt), xp, reps)
+    _check(st, "gba_solve_batch")
+    return xs, list(reps)
+
+
+class Plan:
+    """A batch of problems resident on the device (gba_plan_*)."""
+
+    def __init__(self, scenes, options=None):
+        L = lib()
+        if not isinstance(scenes, (list, tuple)):
+            scenes = [scenes]
+        self.scenes = list(scenes)
+        self._cps = [abi.CProblem(s) for s in self.scenes]
+        self._arr = (abi.Problem * len(self._cps))(*[c.problem for c in self._cps])
+        self._ys = [_f64(s.near_y) for s in self.scenes]
+        yp = (C.POINTER(C.c_double) * len(self._ys))(*[abi.dptr(y) for y in self._ys])
+        self.options = options if options is not None else abi.make_options()
+        h = C.c_void_p()
+        _check(L.gba_plan_create(self._arr, yp, len(self.scenes), C.byref(self.options),
+                                 C.byref(h)), "gba_plan_create")
+        self.h = h
+        for q, s in enumerate(self.scenes):
+            self.set_initial_x(q, s.x0)
+
+    def set_initial_x(self, q, x0):
+        x0 = _f64(x0)
+        _check(lib().gba_plan_set_initial_x(self.h, q, abi.dptr(x0)), "set_initial_x")
+
+    def run(self):
+        _check(lib().gba_plan_run(self.h), "gba_plan_run")
+
+    def synchronize(self):
+        _check(lib().gba_plan_synchronize(self.h), "gba_plan_synchronize")
+
+    def x(self, q=0):
+        out = np.zeros(self._cps[q].x_size)
+        _check(lib().gba_plan_get_x(self.h, q, abi.dptr(out)), "get_x")
+        return out
+
+    def report(self, q=0):
+        r = abi.Report()
+        _check(lib().gba_plan_get_report(self.h, q, C.byref(r)), "get_report")
+        return r
+
+    def last_run_ms(self):
+        v = C.c_double()
+        _check(lib().gba_plan_last_run_ms(self.h, C.byref(v)), "last_run_ms")
+        return v.value
+
+    def stage_ms(self, stage):
+        v = C.c_double()
+        n = C.c_int32()
+        _check(lib().gba_plan_kernel_stats(self.h, stage, C.byref(v), C.byref(n)), "kernel_stats")
+        return v.value
+
+    def launches(self):
+        v = C.c_int64()
+        _check(lib().gba_plan_last_run_launches(self.h, C.byref(v)), "launches")
+        return v.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gba_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def vector_function(scene, x, precision=abi.PRECISION_FP64):
+    cp = abi.CProblem(scene)
+    x = _f64(x)
+    y = np.zeros(2 * scene.number_of_keys)
+    _check(lib().gba_vector_function(cp.ref, abi.dptr(x), abi.dptr(y), precision),
+           "gba_vector_function")
+    return y
+
+
+def jacobian(scene, x, precision=abi.PRECISION_FP64):
+    cp = abi.CProblem(scene)
+    x = _f64(x)
+    K = scene.number_of_keys
+    jp = np.zeros((K, 2, 3))
+    ji = np.zeros((K, 2, 6))
+    _check(lib().gba_jacobian(cp.ref, abi.dptr(x), abi.dptr(jp), abi.dptr(ji), None, precision),
+           "gba_jacobian")
+    return jp, ji
+
+
+def cost(scene, x, near_y=None, options=None):
+    cp = abi.CProblem(scene)
+    x = _f64(x)
+    y = _f64(scene.near_y if near_y is None else near_y)
+    out = C.c_double()
+    opt = options if options is not None else abi.make_options()
+    _check(lib().gba_cost(cp.ref, abi.dptr(x), abi.dptr(y), C.byref(opt), C.byref(out)), "gba_cost")
+    return out.value
+
+
+def schur_step(scene, x, mu, near_y=None, options=None):
+    cp = abi.CProblem(scene)
+    x = _f64(x)
+    y = _f64(scene.near_y if near_y is None else near_y)
+    dx = np.zeros(cp.x_size)
+    opt = options if options is not None else abi.make_options()
+    _check(lib().gba_schur_step(cp.ref, abi.dptr(x), abi.dptr(y), mu, C.byref(opt), abi.dptr(dx)),
+           "gba_schur_step")
+    return dx
+
+
+def kernel_launch_count():
+    return lib().gba_kernel_launch_count()

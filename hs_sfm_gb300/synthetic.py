@@ -107,6 +107,30 @@ def project(points, images, cameras, mask):
     return n, pc[:, 2]
 
 
+def _distort_intrinsic(n, cam, mask):
+    """Distortion and intrinsics of camera_shared_vector_function.hpp:645-685
+    applied to normalized keys n [..., 2] of a single camera."""
+    off = 0
+    x, y = n[..., 0], n[..., 1]
+    r2 = x * x + y * y
+    dx = np.zeros_like(x)
+    dy = np.zeros_like(y)
+    if mask & COMPUTE_RADIAL:
+        coeff = cam[0] * r2 + cam[1] * r2 ** 2 + cam[2] * r2 ** 3
+        dx, dy = dx + coeff * x, dy + coeff * y
+        off += 3
+    if mask & COMPUTE_DECENTERING:
+        d1, d2 = cam[off], cam[off + 1]
+        dx = dx + 2 * d1 * x * y + d2 * (r2 + 2 * x * x)
+        dy = dy + 2 * d2 * x * y + d1 * (r2 + 2 * y * y)
+        off += 2
+    x, y = x + dx, y + dy
+    if mask & COMPUTE_INTRINSIC:
+        f, sk, cx, cy, a = cam[off:off + 5]
+        return np.stack([f * x + sk * y + cx, f * a * y + cy], axis=-1)
+    return np.stack([x, y], axis=-1)
+
+
 # ---------------------------------------------------------------------------
 # Scene container.
 # ---------------------------------------------------------------------------
@@ -167,10 +191,28 @@ def _perturb(rng, points, images, rot_sigma=0.01, t_sigma=0.05, p_sigma=0.05):
     return p0, np.concatenate([r0, t0], axis=1)
 
 
+def project_keys(points, images, cameras, image_camera_map, feature_maps, mask):
+    """Keys of every (image, point) pair of feature_maps, one rotation matrix
+    per image."""
+    Rm = rotvec_to_matrix(images[:, :3])
+    im, pt = feature_maps[:, 0], feature_maps[:, 1]
+    pc = np.einsum('nij,nj->ni', Rm[im], points[pt]) + images[im, 3:]
+    n = pc[:, :2] / pc[:, 2:3]
+    cams = cameras[image_camera_map[im]]
+    if len(cameras) == 1:
+        return _distort_intrinsic(n, cameras[0], mask)
+    out = np.empty_like(n)
+    for c in range(len(cameras)):
+        sel = image_camera_map[im] == c
+        out[sel] = _distort_intrinsic(n[sel], cameras[c], mask)
+    del cams
+    return out
+
+
 def _finish(name, rng, points, images, cameras, icm, fm, mask, fix_mask,
             noise=1.0, outlier_fraction=0.0, width=1920.0, height=1080.0):
     P = len(points)
-    keys, _ = project(points[fm[:, 1]], images[fm[:, 0]], cameras[icm[fm[:, 0]]], mask)
+    keys = project_keys(points, images, cameras, icm, fm, mask)
     obs = keys + rng.normal(0.0, noise, size=keys.shape)
     outlier = None
     if outlier_fraction > 0:
@@ -227,7 +269,7 @@ def ring_scene(num_images=10, num_points=1000, obs_per_point=5, seed=0, scale=1.
         k = rng.integers(obs_range[0], obs_range[1] + 1, size=num_points)
         k = np.minimum(k, num_images)
     rows = np.repeat(np.arange(num_points), k)
-    cols = np.concatenate([np.arange(kk) for kk in k]) if num_points else np.zeros(0, int)
+    cols = np.arange(len(rows)) - np.repeat(np.cumsum(k) - k, k)
     img = order[rows, cols]
     fm = np.stack([img, rows], axis=1)
     cameras = default_intrinsics(mask)[None, :]
@@ -262,29 +304,29 @@ def grid_scene(num_images=200, num_points=100_000, seed=1, height=12.0,
     points = np.stack([rng.uniform(-20, 20, num_points), rng.uniform(-20, 20, num_points),
                        rng.uniform(-2, 2, num_points)], axis=1)
     want = rng.integers(obs_range[0], obs_range[1] + 1, size=num_points)
+    Rm = rotvec_to_matrix(images[:, :3])
     rows_all, cols_all = [], []
-    chunk = 20_000
+    chunk = 10_000
     for s in range(0, num_points, chunk):
         e = min(num_points, s + chunk)
         Pn = e - s
-        pts = np.repeat(points[s:e], num_images, axis=0)
-        ims = np.tile(images, (Pn, 1))
-        keys, depth = project(pts, ims, np.tile(cameras, (Pn * num_images, 1)), mask)
-        vis = (depth > 0.1) & (keys[:, 0] > 0) & (keys[:, 0] < 1920) & (keys[:, 1] > 0) & (keys[:, 1] < 1080)
-        vis = vis.reshape(Pn, num_images)
+        pc = np.einsum('pj,cij->pci', points[s:e], Rm) + images[None, :, 3:]
+        depth = pc[..., 2]
+        keys = _distort_intrinsic(pc[..., :2] / pc[..., 2:3], cameras[0], mask)
+        vis = (depth > 0.1) & (keys[..., 0] > 0) & (keys[..., 0] < 1920) & \
+              (keys[..., 1] > 0) & (keys[..., 1] < 1080)
         pr = rng.random((Pn, num_images))
         pr[~vis] = 2.0
         order = np.argsort(pr, axis=1)
-        nvis = vis.sum(axis=1)
-        k = np.minimum(want[s:e], nvis)
-        for j in range(Pn):
-            kk = int(k[j])
-            if kk >= 2:
-                sel = np.sort(order[j, :kk])
-                rows_all.append(np.full(kk, s + j))
-                cols_all.append(sel)
+        k = np.minimum(want[s:e], vis.sum(axis=1))
+        k[k < 2] = 0
+        take = np.arange(num_images)[None, :] < k[:, None]
+        rows_all.append(np.repeat(np.arange(s, e), k))
+        cols_all.append(order[take])
     rows = np.concatenate(rows_all)
     cols = np.concatenate(cols_all)
+    o = np.lexsort((cols, rows))
+    rows, cols = rows[o], cols[o]
     fm = np.stack([cols, rows], axis=1)
     # points without two observations are dropped (reindexed)
     used = np.unique(rows)

@@ -28,6 +28,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define GBA_API __attribute__((visibility("default")))
+#else
+#define GBA_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -121,9 +127,9 @@ typedef struct gba_problem {
 
 /* Sizes derived from a problem (GetXSize / GetYSize,
  * camera_shared_vector_function.hpp:237-362). */
-int64_t gba_params_per_camera(uint32_t intrinsic_computations_mask);
-int64_t gba_x_size(const gba_problem* problem);
-int64_t gba_y_size(const gba_problem* problem);
+GBA_API int64_t gba_params_per_camera(uint32_t intrinsic_computations_mask);
+GBA_API int64_t gba_x_size(const gba_problem* problem);
+GBA_API int64_t gba_y_size(const gba_problem* problem);
 
 /* ---- solver options ------------------------------------------------------ */
 #define GBA_PRECISION_FP64   0   /* every stage in FP64 (the drop-in path)  */
@@ -159,7 +165,7 @@ typedef struct gba_options {
 /* Fills the defaults used by the reference's relative-pair test
  * (test_camera_shared_relative_pair.cpp:976-979): 50 iterations,
  * tau 1e-3, eps1 1e-8, eps2 1e-8, FP64, trivial loss, dense Cholesky. */
-void gba_default_options(gba_options* options);
+GBA_API void gba_default_options(gba_options* options);
 
 #define GBA_STOP_MAX_ITERATIONS 0
 #define GBA_STOP_SMALL_GRADIENT 1
@@ -194,6 +200,8 @@ typedef struct gba_report {
   double setup_ms;            /* structure build + upload                   */
   double solve_ms;            /* LM loop, device time                       */
   double stage_ms[GBA_NUM_STAGES];  /* with options.profile                 */
+  int64_t h2d_bytes;          /* host->device bytes copied for this solve   */
+  int64_t d2h_bytes;          /* device->host bytes copied for this solve   */
 } gba_report;
 
 /* ---- one-shot solve: the drop-in for
@@ -201,38 +209,38 @@ typedef struct gba_report {
  * (camera_shared_levenberg_marquardt_optimizor.hpp:43-58).
  * near_y [y_size] is the observed y; x_inout [x_size] holds the initial x on
  * entry and the optimized x on return.  Host buffers. */
-int gba_solve(const gba_problem* problem, const double* near_y,
+GBA_API int gba_solve(const gba_problem* problem, const double* near_y,
               const gba_options* options, double* x_inout,
               gba_report* report);
 
 /* ---- resident plans: one or many problems kept on the device ----------- */
 typedef struct gba_plan gba_plan;
 
-int gba_plan_create(const gba_problem* problems, const double* const* near_ys,
+GBA_API int gba_plan_create(const gba_problem* problems, const double* const* near_ys,
                     int32_t number_of_problems, const gba_options* options,
                     gba_plan** plan);
-int gba_plan_destroy(gba_plan* plan);
-int gba_plan_number_of_problems(const gba_plan* plan);
+GBA_API int gba_plan_destroy(gba_plan* plan);
+GBA_API int gba_plan_number_of_problems(const gba_plan* plan);
 /* Copies x0 of every problem (host) to the device and remembers it. */
-int gba_plan_set_initial_x(gba_plan* plan, int32_t problem, const double* x0);
+GBA_API int gba_plan_set_initial_x(gba_plan* plan, int32_t problem, const double* x0);
 /* Resets every problem to its remembered x0 and runs the LM solve of all
  * problems together (asynchronous on the plan's stream). */
-int gba_plan_run(gba_plan* plan);
+GBA_API int gba_plan_run(gba_plan* plan);
 /* Waits for the plan's stream; returns the first device status seen. */
-int gba_plan_synchronize(gba_plan* plan);
-int gba_plan_get_x(gba_plan* plan, int32_t problem, double* x_out);
-int gba_plan_get_report(gba_plan* plan, int32_t problem, gba_report* report);
+GBA_API int gba_plan_synchronize(gba_plan* plan);
+GBA_API int gba_plan_get_x(gba_plan* plan, int32_t problem, double* x_out);
+GBA_API int gba_plan_get_report(gba_plan* plan, int32_t problem, gba_report* report);
 /* Device time of the last gba_plan_run in milliseconds (CUDA events on the
  * plan's stream), and the average duration of the named kernel's launches
  * in that run when options.profile was set (0 when not recorded). */
-int gba_plan_last_run_ms(gba_plan* plan, double* ms);
-int gba_plan_kernel_stats(gba_plan* plan, int32_t stage, double* total_ms,
+GBA_API int gba_plan_last_run_ms(gba_plan* plan, double* ms);
+GBA_API int gba_plan_kernel_stats(gba_plan* plan, int32_t stage, double* total_ms,
                           int32_t* launches);
 /* Counts of this library's kernel launches in the last run. */
-int gba_plan_last_run_launches(gba_plan* plan, int64_t* launches);
+GBA_API int gba_plan_last_run_launches(gba_plan* plan, int64_t* launches);
 
 /* ---- batched one-shot solve (independent problems, one plan) ----------- */
-int gba_solve_batch(const gba_problem* problems, const double* const* near_ys,
+GBA_API int gba_solve_batch(const gba_problem* problems, const double* const* near_ys,
                     int32_t number_of_problems, const gba_options* options,
                     double* const* x_inout, gba_report* reports);
 
@@ -241,20 +249,20 @@ int gba_solve_batch(const gba_problem* problems, const double* const* near_ys,
  * checks of each stage.  Host buffers in and out. ------------------------- */
 
 /* CameraSharedVectorFunction::operator() (:412-632): y [y_size]. */
-int gba_vector_function(const gba_problem* problem, const double* x,
+GBA_API int gba_vector_function(const gba_problem* problem, const double* x,
                         double* y, int32_t precision);
 
 /* CameraSharedAnalyticalJacobianMatrixCalculator (:66-332): per key, in key
  * order, the 2x3 point block, the 2x6 image block and the 2xc camera block,
  * row-major; blocks of fixed parameter groups are not written (pass NULL). */
-int gba_jacobian(const gba_problem* problem, const double* x,
+GBA_API int gba_jacobian(const gba_problem* problem, const double* x,
                  double* point_blocks, double* image_blocks,
                  double* camera_blocks, int32_t precision);
 
 /* Mahalanobis distance sum r^T Lambda r of r = f(x) - near_y
  * (camera_shared_mahalanobis_distance_calculator.hpp:28-58); with a Huber
  * loss each key's term s becomes rho(s). */
-int gba_cost(const gba_problem* problem, const double* x,
+GBA_API int gba_cost(const gba_problem* problem, const double* x,
              const double* near_y, const gba_options* options, double* cost);
 
 /* One damped Gauss-Newton step: builds the normal equations at x
@@ -262,15 +270,15 @@ int gba_cost(const gba_problem* problem, const double* x,
  * (camera_shared_augmentor.hpp:22-26) and solves (N + mu I) delta = g by the
  * Schur complement (camera_shared_normal_equation_solver.hpp:75-114).
  * delta_x [x_size]; the LM update is x - delta_x. */
-int gba_schur_step(const gba_problem* problem, const double* x,
+GBA_API int gba_schur_step(const gba_problem* problem, const double* x,
                    const double* near_y, double mu,
                    const gba_options* options, double* delta_x);
 
 /* ---- library ------------------------------------------------------------ */
-const char* gba_status_string(int status);
-const char* gba_version(void);
+GBA_API const char* gba_status_string(int status);
+GBA_API const char* gba_version(void);
 /* Number of kernels this library has launched since load (all threads). */
-int64_t gba_kernel_launch_count(void);
+GBA_API int64_t gba_kernel_launch_count(void);
 
 #ifdef __cplusplus
 }  /* extern "C" */

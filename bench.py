@@ -300,11 +300,13 @@ def run_gba(args, ws, rank, local):
             entry["achieved_gbs"] = sb[name] / (ms / 1e3) / 1e9
         stages[name] = entry
     hbm_stages = {k: v for k, v in stages.items() if "achieved_gbs" in v}
-    dom = max(hbm_stages, key=lambda k: hbm_stages[k]["ms_per_iteration"])
-    achieved = hbm_stages[dom]["achieved_gbs"]
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
-                "traffic": None}
+    roofline = None
+    if hbm_stages:
+        dom = max(hbm_stages, key=lambda k: hbm_stages[k]["ms_per_iteration"])
+        achieved = hbm_stages[dom]["achieved_gbs"]
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                    "unit": "GB/s", "frac": achieved / peak,
+                    "peak_kind": f"{peak_kind} hbm_gbs", "traffic": None}
 
     # end to end through the C ABI with host buffers
     e2e_ms, h2d, d2h = [], 0, 0

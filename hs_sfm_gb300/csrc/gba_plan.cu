@@ -482,7 +482,7 @@ void Plan::enqueue(bool profile) {
   size_t ev_i = 0;
   auto mark = [&](int stage) {
     if (!profile) return;
-    GBA_CUDA(cudaEventRecord(prof_events[ev_i], s));
+    GBA_CUDA(cudaEventRecordWithFlags(prof_events[ev_i], s, cudaEventRecordExternal));
     prof_stage[ev_i] = stage;
     ++ev_i;
   };
@@ -532,7 +532,7 @@ int Plan::run() {
       GBA_CUDA(cudaEventCreate(&e));
       prof_events.push_back(e);
     }
-    prof_stage.assign(prof_events.size(), -2);
+    if (!graph_exec) prof_stage.assign(prof_events.size(), -2);
   }
   GBA_CUDA(cudaSetDevice(device));
   GBA_CUDA(cudaEventRecord(ev0, stream));

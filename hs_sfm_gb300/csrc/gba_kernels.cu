@@ -799,6 +799,7 @@ __global__ void __launch_bounds__(256) k_chol_diag0(DevPlan d) {
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p]) return;
   const ProbInfo pi = d.prob[p];
+  if (pi.nt <= 0) return;
   if (threadIdx.x == 0) fail = 0;
   load_tile_sym(d.S + pi.s_off, pi.n, 0, tile_rows(pi.n, 0), a);
   diag_factor(d, p, pi, 0, a, inv, &fail);
@@ -857,9 +858,9 @@ __global__ void __launch_bounds__(256) k_chol_update(DevPlan d, int k) {
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p]) return;
   const ProbInfo pi = d.prob[p];
-  const int T = pi.nt - k - 1;
+  const int T = pi.nt - k - 1;   // trailing tiles of this problem (may be <= 0)
   const int lin = blockIdx.x;
-  if (lin >= T * (T + 1) / 2) return;
+  if (T <= 0 || lin >= T * (T + 1) / 2) return;
   // decode lin -> (ti, tj), tj <= ti
   int ti = int((sqrt(8.0 * lin + 1.0) - 1.0) * 0.5);
   while ((ti + 1) * (ti + 2) / 2 <= lin) ++ti;

@@ -1,0 +1,138 @@
+"""CPU model of the dense-Cholesky launches of libgba.so: for batches of
+problems of uneven size, every S / b / Linv element a kernel touches must
+lie inside that problem's own region.  The model restates each kernel's
+grid and early-exit guards (hs_sfm_gb300/csrc/gba_kernels.cu: k_chol_diag0,
+k_chol_panel, k_chol_update with its fused diagonal factorization,
+k_chol_backward, k_assemble_S)."""
+import math
+
+import numpy as np
+import pytest
+
+TILE = 32
+
+
+def rows(n, t):
+    return min(TILE, n - TILE * t)
+
+
+def decode(lin):
+    ti = int((math.sqrt(8.0 * lin + 1.0) - 1.0) * 0.5)
+    while (ti + 1) * (ti + 2) // 2 <= lin:
+        ti += 1
+    while ti * (ti + 1) // 2 > lin:
+        ti -= 1
+    return ti, lin - ti * (ti + 1) // 2
+
+
+class Batch:
+    def __init__(self, images):
+        self.I = list(images)
+        self.n = [6 * i for i in images]
+        self.nt = [(n + TILE - 1) // TILE for n in self.n]
+        self.s_off = np.concatenate([[0], np.cumsum([n * n for n in self.n])]).tolist()
+        self.img_begin = np.concatenate([[0], np.cumsum(images)]).tolist()
+        self.max_nt = max(self.nt)
+        self.max_n = max(self.n)
+        self.B = len(images)
+
+    def check_S(self, p, r0, nr, c0, nc):
+        n = self.n[p]
+        assert nr >= 0 and nc >= 0
+        if nr == 0 or nc == 0:
+            return
+        assert 0 <= r0 and r0 + nr <= n and 0 <= c0 and c0 + nc <= n, (p, r0, nr, c0, nc, n)
+        lo = self.s_off[p] + r0 * n + c0
+        hi = self.s_off[p] + (r0 + nr - 1) * n + c0 + nc - 1
+        assert self.s_off[p] <= lo and hi < self.s_off[p + 1]
+
+    def check_b(self, p, e0, ne):
+        lo = 6 * self.img_begin[p] + e0
+        assert 0 <= e0 and e0 + ne <= self.n[p], (p, e0, ne)
+        assert 6 * self.img_begin[p] <= lo and lo + ne <= 6 * self.img_begin[p + 1]
+
+    def check_linv(self, p, k):
+        assert 0 <= k < self.max_nt
+        assert 0 <= p * self.max_nt + k < self.B * self.max_nt
+
+    def diag(self, p, k):
+        m = rows(self.n[p], k)
+        self.check_S(p, TILE * k, m, TILE * k, m)
+        self.check_linv(p, k)
+        self.check_b(p, TILE * k, m)
+
+    def run(self):
+        touched = 0
+        for p in range(self.B):                      # k_chol_diag0
+            if self.nt[p] <= 0:
+                continue
+            self.diag(p, 0)
+        for k in range(self.max_nt - 1):
+            for bx in range(self.max_nt - 1 - k):    # k_chol_panel
+                for p in range(self.B):
+                    i = k + 1 + bx
+                    if i >= self.nt[p]:
+                        continue
+                    mi, m = rows(self.n[p], i), rows(self.n[p], k)
+                    self.check_S(p, TILE * i, mi, TILE * k, m)
+                    self.check_linv(p, k)
+                    self.check_b(p, TILE * k, m)
+                    self.check_b(p, TILE * i, mi)
+                    touched += 1
+            Tg = self.max_nt - k - 1                 # k_chol_update
+            for lin in range(Tg * (Tg + 1) // 2):
+                for p in range(self.B):
+                    T = self.nt[p] - k - 1
+                    if T <= 0 or lin >= T * (T + 1) // 2:
+                        continue
+                    ti, tj = decode(lin)
+                    i, j = k + 1 + ti, k + 1 + tj
+                    assert j <= i < self.nt[p]
+                    n = self.n[p]
+                    mi, mj, m = rows(n, i), rows(n, j), rows(n, k)
+                    self.check_S(p, TILE * i, mi, TILE * k, m)
+                    self.check_S(p, TILE * j, mj, TILE * k, m)
+                    self.check_S(p, TILE * i, mi, TILE * j, mj)
+                    if i == j == k + 1:
+                        self.diag(p, k + 1)
+                    touched += 1
+        for k in range(self.max_nt - 1, 0, -1):     # k_chol_backward
+            for j in range(k):
+                for p in range(self.B):
+                    if k >= self.nt[p]:
+                        continue
+                    n = self.n[p]
+                    m = rows(n, k)
+                    self.check_S(p, TILE * k, m, TILE * j, TILE)
+                    self.check_b(p, TILE * k, m)
+                    self.check_b(p, TILE * j, TILE)
+                    self.check_linv(p, j)
+        # k_assemble_S: thread (row, col) of the lower triangle
+        for p in range(self.B):
+            n, I = self.n[p], self.I[p]
+            assert (self.max_n * self.max_n + 255) // 256 * 256 >= n * n
+            if n:
+                self.check_S(p, 0, n, 0, n)
+                self.check_b(p, 0, n)
+                assert (n - 1) // 6 < I
+        return touched
+
+
+@pytest.mark.parametrize("images", [
+    [14, 32], [15, 39], [39, 15], [5, 40, 5, 40], [1, 2, 3], [200], [40] * 3,
+    [14, 32, 15, 34, 34, 39],
+])
+def test_cholesky_accesses_stay_inside_each_problem(images):
+    Batch(images).run()
+
+
+def test_random_batches():
+    rng = np.random.default_rng(0)
+    for _ in range(40):
+        Batch(list(rng.integers(1, 48, size=rng.integers(1, 9)))).run()
+
+
+def test_decode_covers_the_lower_triangle():
+    for T in range(1, 40):
+        seen = {decode(lin) for lin in range(T * (T + 1) // 2)}
+        assert seen == {(i, j) for i in range(T) for j in range(i + 1)}

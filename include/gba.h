@@ -274,6 +274,40 @@ GBA_API int gba_schur_step(const gba_problem* problem, const double* x,
                    const double* near_y, double mu,
                    const gba_options* options, double* delta_x);
 
+/* ---- allocation-free cost ------------------------------------------------
+ * No counterpart in the reference: an entry point for callers that must not
+ * allocate device memory -- a plugin inside an application that owns every
+ * device allocation through its own pool, or code that runs where
+ * cudaMalloc is not allowed.  It evaluates the same sum as gba_cost (trivial
+ * or Huber loss, identity key weights) for a problem whose arrays the caller
+ * already holds in device memory, and writes the sum to d_cost (device).
+ * It allocates nothing: its temporaries live in a fixed static device array
+ * of libgba.so (about 1.6 MB, held on every GPU that loads the library until
+ * exit), so problems are limited to GBA_NOALLOC_MAX_IMAGES images (larger
+ * ones return GBA_ERR_INVALID).  Every call shares that array: calls whose
+ * work overlaps on the GPU race and must be serialized.  The first call on a
+ * device looks up the array's device address (once per device); make it
+ * before any stream capture.  `stream` is a cudaStream_t (NULL = default
+ * stream); the call only enqueues work. */
+#define GBA_NOALLOC_MAX_IMAGES 16384
+
+typedef struct gba_device_problem {
+  int32_t number_of_points;
+  int32_t number_of_images;
+  int32_t number_of_cameras;
+  int32_t number_of_keys;
+  const int32_t* key_image;    /* device [K] image id of each key           */
+  const int32_t* key_point;    /* device [K] point id of each key           */
+  const double* keys;          /* device [2K] observed keys                 */
+  const int32_t* image_camera; /* device [I] camera id of each image        */
+  const double* cameras;       /* device [10C] k1 k2 k3 d1 d2 f s cx cy a   */
+  const double* points;        /* device [3P]                               */
+  const double* images;        /* device [6I] angle-axis r, translation t   */
+} gba_device_problem;
+
+GBA_API int gba_cost_noalloc(const gba_device_problem* problem, int32_t loss,
+                             double huber_delta, double* d_cost, void* stream);
+
 /* ---- library ------------------------------------------------------------ */
 GBA_API const char* gba_status_string(int status);
 GBA_API const char* gba_version(void);

@@ -19,8 +19,9 @@ namespace gba {
 constexpr int kTile = 32;          // dense Cholesky tile (FP64)
 constexpr int kKeyChunk = 1024;    // keys per cost work chunk
 constexpr int kPointChunk = 128;   // points per point work chunk
-constexpr int kImageChunk = 8;     // images per image work chunk (warp each)
-constexpr int kPairItem = 256;     // pairs per Schur-assembly work item
+constexpr int kImageChunk = 8;     // images per image work chunk (backsub)
+constexpr int kImageItem = 512;    // keys per image-reduce work item (warp each)
+constexpr int kPairItem = 1024;    // pairs per Schur-assembly work item
 constexpr int kJRStride = 20;      // per key: Jp(6) Ji(12) rw(2)
 constexpr int kZStride = 20;       // per key: Z(18) + pad
 constexpr int kItemStride = 44;    // per work item: 36 block + 6 rhs + pad
@@ -89,6 +90,10 @@ struct DevPlan {
   const int* img_keys;       // keys of each image, by point
   const int* img_prob;
   const int* img_cam;        // global camera id
+  int n_img_items;
+  const int4* img_items;     // (image, q begin, q end, prob), <= kImageItem keys
+  const int* img_item_off;   // [I+1] items of each image
+  double* img_item_partial;  // [items * 28]
   const double* cam64;       // [C*10]  k1 k2 k3 d1 d2 f s cx cy a
   const float* cam32;        // [C*10]
   // parameters (double buffered by LMState::parity)
@@ -109,9 +114,9 @@ struct DevPlan {
   double* U;                 // [36I]
   double* gi;                // [6I]
   // reduced systems
-  double* S;                 // sum n^2 over problems
-  double* b;                 // [6I]  rhs -> forward solution -> delta (images)
-  double* Linv;              // [B * max_nt * kTile^2] inverses of diagonal tiles
+  void* S;                   // T: sum n^2 over problems (lower triangles)
+  void* b;                   // T: [6I] rhs -> forward solution -> delta (images)
+  void* Linv;                // T: [B * max_nt * kTile^2] inverses of diagonal tiles
   int* factor_flag;          // [B] 0 ok, 1 failed
   // Schur assembly
   const int2* pairs;         // (key_a, key_b) per pair, grouped by block

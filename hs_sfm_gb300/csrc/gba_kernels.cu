@@ -87,6 +87,13 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -175,7 +182,8 @@ __device__ __forceinline__ void project64(const double* R, const double* X, cons
   double y0 = R[0] * X[0] + R[1] * X[1] + R[2] * X[2] + R[9];
   double y1 = R[3] * X[0] + R[4] * X[1] + R[5] * X[2] + R[10];
   double y2 = R[6] * X[0] + R[7] * X[1] + R[8] * X[2] + R[11];
-  double n0 = y0 / y2, n1 = y1 / y2;
+  const double iz = 1.0 / y2;
+  double n0 = y0 * iz, n1 = y1 * iz;
   double r2 = n0 * n0 + n1 * n1;
   double coeff = cam[0] * r2 + cam[1] * (r2 * r2) + cam[2] * (r2 * r2 * r2);
   double dx = coeff * n0 + (2.0 * cam[3] * n0 * n1 + cam[4] * (r2 + 2.0 * n0 * n0));
@@ -373,7 +381,7 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
     double rho, w;
     loss_eval(d.loss, d.huber_delta, sq, rho, w);
     acc += rho;
-    const double sw = sqrt(w);
+    const double sw = (w == 1.0) ? 1.0 : sqrt(w);
     T out[4] = {T(e0 * sw), T(e1 * sw), T(sw), T(0)};
     store_vec<4>(rw + 4LL * k, out);
   }
@@ -467,22 +475,24 @@ __global__ void __launch_bounds__(kPointChunk) k_linearize(DevPlan d) {
 }
 
 // ---------------------------------------------------------------------------
-// image reduce: per image (warp), U_i and g_i with Kahan lane sums
+// image reduce: U_i = sum J_i^T J_i, g_i = sum J_i^T r.  Each image's keys
+// are split into work items of <= kImageItem keys (one warp each, Kahan lane
+// sums in T, warp sum in T); k_image_finalize adds an image's items in order
+// in FP64.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(32 * kImageChunk) k_image_reduce(DevPlan d) {
-  const Chunk ch = d.img_chunks[blockIdx.x];
-  const LMState& st = d.state[ch.prob];
+__global__ void __launch_bounds__(256) k_image_reduce(DevPlan d) {
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= d.n_img_items) return;
+  const int4 it = __ldg(d.img_items + wid);   // (image, q begin, q end, prob)
+  const LMState& st = d.state[it.w];
   if (!st.relin || !st.active) return;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int img = ch.begin + w;
-  if (img >= ch.end) return;
   const T* __restrict__ JR = tptr<T>(d.JR);
   T acc[27], cmp[27];
 #pragma unroll
   for (int e = 0; e < 27; ++e) { acc[e] = T(0); cmp[e] = T(0); }
-  const int qb = __ldg(d.img_key_off + img), qe = __ldg(d.img_key_off + img + 1);
-  for (int q = qb + lane; q < qe; q += 32) {
+  for (int q = it.y + lane; q < it.z; q += 32) {
     const int k = __ldg(d.img_keys + q);
     T rec[kJRStride];
     load_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
@@ -492,9 +502,9 @@ __global__ void __launch_bounds__(32 * kImageChunk) k_image_reduce(DevPlan d) {
     for (int a = 0; a < 6; ++a) {
 #pragma unroll
       for (int b = a; b < 6; ++b) {
-        T term = ji[a] * ji[b] + ji[6 + a] * ji[6 + b];
-        T y = term - cmp[e];
-        T t = acc[e] + y;
+        const T term = ji[a] * ji[b] + ji[6 + a] * ji[6 + b];
+        const T y = term - cmp[e];
+        const T t = acc[e] + y;
         cmp[e] = (t - acc[e]) - y;
         acc[e] = t;
         ++e;
@@ -502,35 +512,50 @@ __global__ void __launch_bounds__(32 * kImageChunk) k_image_reduce(DevPlan d) {
     }
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
-      T term = ji[a] * rec[18] + ji[6 + a] * rec[19];
-      T y = term - cmp[21 + a];
-      T t = acc[21 + a] + y;
+      const T term = ji[a] * rec[18] + ji[6 + a] * rec[19];
+      const T y = term - cmp[21 + a];
+      const T t = acc[21 + a] + y;
       cmp[21 + a] = (t - acc[21 + a]) - y;
       acc[21 + a] = t;
     }
   }
-  double tot[27];
+  double* out = d.img_item_partial + 28LL * wid;
 #pragma unroll
-  for (int e = 0; e < 27; ++e) tot[e] = warp_sum(double(acc[e]) - double(cmp[e]));
+  for (int e = 0; e < 27; ++e) {
+    const T v = warp_sum_t(T(acc[e] - cmp[e]));
+    if (lane == e) out[e] = double(v);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_image_finalize(DevPlan d) {
+  const int img = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (img >= d.I) return;
+  const int prob = d.img_prob[img];
+  const LMState& st = d.state[prob];
+  if (!st.relin || !st.active) return;
+  const int ib = d.img_item_off[img], ie = d.img_item_off[img + 1];
+  double v = 0.0;
+  if (lane < 27)
+    for (int t = ib; t < ie; ++t) v += d.img_item_partial[28LL * t + lane];
+  // lane e holds entry e of (upper U in row order, then g)
   double* U = d.U + 36LL * img;
-  int e = 0;
   double dmax = 0.0, gmax = 0.0;
-#pragma unroll
-  for (int a = 0; a < 6; ++a) {
-#pragma unroll
-    for (int b = a; b < 6; ++b) {
-      if (lane == (e & 31)) { U[6 * a + b] = tot[e]; U[6 * b + a] = tot[e]; }
-      if (a == b) dmax = fmax(dmax, tot[e]);
-      ++e;
-    }
+  if (lane < 21) {
+    int a = 0, e = lane;
+    while (e >= 6 - a) { e -= 6 - a; ++a; }
+    const int b = a + e;
+    U[6 * a + b] = v;
+    U[6 * b + a] = v;
+    if (a == b) dmax = v;
+  } else if (lane < 27) {
+    d.gi[6LL * img + (lane - 21)] = v;
+    gmax = fabs(v);
   }
-#pragma unroll
-  for (int a = 0; a < 6; ++a) {
-    if (lane == a) d.gi[6LL * img + a] = tot[21 + a];
-    gmax = fmax(gmax, fabs(tot[21 + a]));
-  }
+  dmax = warp_max(dmax);
+  gmax = warp_max(gmax);
   if (lane == 0) {
-    LMState* sp = d.state + ch.prob;
+    LMState* sp = d.state + prob;
     atomicMax(&sp->maxdiag_bits, dbits(dmax));
     atomicMax(&sp->ginf_bits, dbits(gmax));
   }
@@ -641,20 +666,23 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
         acc[6 * r + c] += za[r] * zb[c] + za[6 + r] * zb[6 + c] + za[12 + r] * zb[12 + c];
     }
   }
+  // warp reduction in the working precision; FP64 only for the stored sums
   double* out = d.item_partial + (long long)kItemStride * wid;
 #pragma unroll
   for (int e = 0; e < 36; ++e) {
-    double v = warp_sum(double(acc[e]));
-    if (lane == (e & 31)) out[e] = v;
+    const T v = warp_sum_t(acc[e]);
+    if (lane == (e & 31)) out[e] = double(v);
   }
 #pragma unroll
   for (int e = 0; e < 6; ++e) {
-    double v = warp_sum(double(racc[e]));
-    if (lane == ((36 + e) & 31)) out[36 + e] = v;
+    const T v = warp_sum_t(racc[e]);
+    if (lane == ((36 + e) & 31)) out[36 + e] = double(v);
   }
 }
 
-// Dense reduced system (lower triangle) and rhs, FP64.
+// Dense reduced system (lower triangle) and rhs in precision T; the block
+// sums over work items are taken in FP64.
+template <typename T>
 __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
   const int p = blockIdx.y;
   const ProbInfo pi = d.prob[p];
@@ -683,7 +711,7 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
   } else {
     s = -v;
   }
-  d.S[pi.s_off + (long long)row * n + col] = s;
+  tptr_mut<T>(d.S)[pi.s_off + (long long)row * n + col] = T(s);
   if (col == 0) {
     // rhs b_i[a] = g_i[a] - sum over the diagonal block's items
     const int dblk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)i * I + i);
@@ -692,229 +720,242 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
       const int ib = __ldg(d.blk_item_off + dblk), ie = __ldg(d.blk_item_off + dblk + 1);
       for (int t = ib; t < ie; ++t) rv += d.item_partial[(long long)kItemStride * t + 36 + a];
     }
-    d.b[6LL * gi_img + a] = d.gi[6LL * gi_img + a] - rv;
+    tptr_mut<T>(d.b)[6LL * gi_img + a] = T(d.gi[6LL * gi_img + a] - rv);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Tiled FP64 Cholesky (lower), forward solve folded in, backward solve.
+// Tiled Cholesky of the reduced system S (lower, precision T), one launch per
+// column step.  Launch k (k = -1 .. nt-2) subtracts column k's rank-32
+// contribution from every trailing tile and factors column c = k+1: every
+// CTA of column c recomputes the diagonal tile's factor and inverse itself
+// (a 32x32 factorization held in one warp's registers), so no separate panel
+// launch is needed; the CTA owning tile (c, c) publishes L_cc^-1 and the
+// forward-solve value y_c = L_cc^-1 b_c.  S keeps its diagonal tiles (the
+// factor lives in Linv), the off-diagonal tiles are overwritten by L.
+// The backward solve L^T delta = y then takes one launch per tile row.
 // ---------------------------------------------------------------------------
-struct TileView {
-  double* S;
-  int n;
-};
-
 __device__ __forceinline__ int tile_rows(int n, int t) { return min(kTile, n - kTile * t); }
 
-// Factor the diagonal tile k held in smem a[kTile][kTile+1] (m x m lower),
-// write L back, its inverse to Linv, the forward solution y_k = L^-1 b_k,
-// and for the last tile the first backward step delta = L^-T y.
-__device__ void diag_factor(DevPlan& d, int p, const ProbInfo& pi, int k,
-                            double (*a)[kTile + 1], double (*inv)[kTile + 1], int* fail) {
-  const int n = pi.n, m = tile_rows(n, k);
-  const int tid = threadIdx.x, nth = blockDim.x;
-  for (int j = 0; j < m; ++j) {
-    if (tid == 0) {
-      double dj = a[j][j];
-      if (!(dj > 0.0) || !isfinite(dj)) *fail = 1;
-      a[j][j] = sqrt(fmax(dj, 0.0));
-    }
-    __syncthreads();
-    if (*fail) break;
-    const double djj = a[j][j];
-    for (int i = j + 1 + tid; i < m; i += nth) a[i][j] /= djj;
-    __syncthreads();
-    const int rem = m - j - 1;
-    for (int e = tid; e < rem * rem; e += nth) {
-      int i = j + 1 + e / rem, l = j + 1 + e % rem;
-      if (l <= i) a[i][l] -= a[i][j] * a[l][j];
-    }
-    __syncthreads();
+template <typename T>
+using Tile = T[kTile][kTile + 1];
+
+// Rectangular tile (ti, tj) of S; entries past the matrix read 0.
+template <typename T>
+__device__ void load_rect(const T* S, int n, int ti, int tj, Tile<T>& t) {
+  const int mi = tile_rows(n, ti), mj = tile_rows(n, tj);
+  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+    const int r = e / kTile, c = e % kTile;
+    t[r][c] = (r < mi && c < mj) ? S[(long long)(kTile * ti + r) * n + kTile * tj + c] : T(0);
   }
-  if (*fail) {
+}
+
+// Diagonal tile (ti, ti): the stored lower triangle; the upper triangle reads
+// 0 and rows past the matrix are identity rows.
+template <typename T>
+__device__ void load_diag(const T* S, int n, int ti, Tile<T>& t) {
+  const int m = tile_rows(n, ti);
+  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+    const int r = e / kTile, c = e % kTile;
+    T v = T(0);
+    if (r < m) {
+      if (c <= r) v = S[(long long)(kTile * ti + r) * n + kTile * ti + c];
+    } else if (r == c) {
+      v = T(1);
+    }
+    t[r][c] = v;
+  }
+}
+
+// A -= X Y^T (32x32x32), 256 threads, 4 outputs each.
+template <typename T>
+__device__ __forceinline__ void tile_sub_xyt(Tile<T>& A, const Tile<T>& X, const Tile<T>& Y) {
+  const int r = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 4;
+  T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+#pragma unroll 8
+  for (int q = 0; q < kTile; ++q) {
+    const T x = X[r][q];
+    s0 += x * Y[c0][q];
+    s1 += x * Y[c0 + 1][q];
+    s2 += x * Y[c0 + 2][q];
+    s3 += x * Y[c0 + 3][q];
+  }
+  A[r][c0] -= s0;
+  A[r][c0 + 1] -= s1;
+  A[r][c0 + 2] -= s2;
+  A[r][c0 + 3] -= s3;
+}
+
+// Factor the SPD tile D (lower triangle used; identity-padded) in one warp,
+// lane i holding row i, and write L^-1 to Dinv.  Returns false when a pivot
+// was not positive.
+template <typename T>
+__device__ bool warp_potrf_inverse(const Tile<T>& D, Tile<T>& Dinv, int lane) {
+  constexpr unsigned FULL = 0xffffffffu;
+  T a[kTile];
+#pragma unroll
+  for (int q = 0; q < kTile; ++q) a[q] = D[lane][q];
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < kTile; ++j) {
+    const T djj = __shfl_sync(FULL, a[j], j);
+    ok = ok && (djj > T(0));
+    const T ljj = sqrt(djj);
+    const T rinv = T(1) / ljj;
+    const T lij = (lane > j) ? a[j] * rinv : ((lane == j) ? ljj : T(0));
+    a[j] = lij;
+#pragma unroll
+    for (int l = j + 1; l < kTile; ++l) {
+      const T llj = __shfl_sync(FULL, lij, l);
+      a[l] -= lij * llj;
+    }
+  }
+  // forward substitution L X = I, one row of X per lane, rows in order
+  T x[kTile];
+#pragma unroll
+  for (int c = 0; c < kTile; ++c) x[c] = (c == lane) ? T(1) : T(0);
+#pragma unroll
+  for (int q = 0; q < kTile; ++q) {
+    const T rq = T(1) / __shfl_sync(FULL, a[q], q);
+    if (lane == q) {
+#pragma unroll
+      for (int c = 0; c <= q; ++c) x[c] *= rq;
+    }
+    const T liq = a[q];
+#pragma unroll
+    for (int c = 0; c <= q; ++c) {
+      const T xqc = __shfl_sync(FULL, x[c], q);
+      if (lane > q) x[c] -= liq * xqc;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < kTile; ++c) Dinv[lane][c] = (c <= lane) ? x[c] : T(0);
+  return ok;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
+  __shared__ Tile<T> A, Li, Lj, D, Dinv;
+  __shared__ T yk[kTile], tv[kTile];
+  const int p = blockIdx.y;
+  const LMState& st = d.state[p];
+  if (!st.active || d.factor_flag[p]) return;
+  const ProbInfo pi = d.prob[p];
+  const int c = k + 1;
+  const int Tn = pi.nt - c;           // tile rows c .. nt-1
+  if (Tn <= 0) return;
+  int i, j;
+  if (k < 0) {                        // first launch: column 0 only
+    if ((int)blockIdx.x >= Tn) return;
+    i = blockIdx.x;
+    j = 0;
+  } else {
+    const int lin = blockIdx.x;
+    if (lin >= Tn * (Tn + 1) / 2) return;
+    int ti = int((sqrt(8.0 * lin + 1.0) - 1.0) * 0.5);
+    while ((ti + 1) * (ti + 2) / 2 <= lin) ++ti;
+    while (ti * (ti + 1) / 2 > lin) --ti;
+    i = c + ti;
+    j = c + (lin - ti * (ti + 1) / 2);
+  }
+  const int n = pi.n;
+  T* S = tptr_mut<T>(d.S) + pi.s_off;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // own tile and, for k >= 0, the column-k factors
+  if (i == j) load_diag<T>(S, n, i, A); else load_rect<T>(S, n, i, j, A);
+  if (k >= 0) {
+    load_rect<T>(S, n, i, k, Li);
+    load_rect<T>(S, n, j, k, Lj);
+    if (tid < kTile) yk[tid] = b[kTile * k + tid];   // y_k (tile k is full)
+  }
+  if (j == c && i != c) load_diag<T>(S, n, c, D);
+  __syncthreads();
+  if (k >= 0) {
+    tile_sub_xyt<T>(A, Li, Lj);
+    if (j == c && i != c) tile_sub_xyt<T>(D, Lj, Lj);
+  }
+  if (j == c && tid < kTile) {
+    // b_i after column k: b_i - L_ik y_k
+    const int mi = tile_rows(n, i);
+    T t = tid < mi ? b[kTile * i + tid] : T(0);
+    if (k >= 0) {
+#pragma unroll 8
+      for (int q = 0; q < kTile; ++q) t -= Li[tid][q] * yk[q];
+    }
+    tv[tid] = t;
+  }
+  __syncthreads();
+  if (j != c) {                       // trailing tile: write back
+    const int mi = tile_rows(n, i), mj = tile_rows(n, j);
+    for (int e = tid; e < kTile * kTile; e += blockDim.x) {
+      const int r = e / kTile, q = e % kTile;
+      if (r < mi && q < mj && (i != j || q <= r)) S[(long long)(kTile * i + r) * n + kTile * j + q] = A[r][q];
+    }
+    return;
+  }
+  // column c: factor the diagonal tile (own tile when i == c)
+  __shared__ int ok_s;
+  if (warp == 0) {
+    const bool ok = warp_potrf_inverse<T>(i == c ? A : D, Dinv, lane);
+    if (lane == 0) ok_s = ok ? 1 : 0;
+  }
+  __syncthreads();
+  if (!ok_s) {
     if (tid == 0) d.factor_flag[p] = 1;
     return;
   }
-  double* S = d.S + pi.s_off;
-  const int r0 = kTile * k;
-  for (int e = tid; e < m * m; e += nth) {
-    int i = e / m, l = e % m;
-    if (l <= i) S[(long long)(r0 + i) * n + r0 + l] = a[i][l];
-  }
-  // inverse of the lower-triangular tile, one column per thread
-  for (int c = tid; c < kTile; c += nth) {
-    for (int r = 0; r < kTile; ++r) inv[r][c] = 0.0;
-    if (c < m) {
-      for (int r = c; r < m; ++r) {
-        double s = (r == c) ? 1.0 : 0.0;
-        for (int q = c; q < r; ++q) s -= a[r][q] * inv[q][c];
-        inv[r][c] = s / a[r][r];
-      }
-    }
-  }
-  __syncthreads();
-  double* Li = d.Linv + ((long long)p * d.max_nt + k) * kTile * kTile;
-  for (int e = tid; e < kTile * kTile; e += nth) Li[e] = inv[e / kTile][e % kTile];
-  // forward solve y_k = L_kk^-1 b_k (b_k already has the panel updates)
-  __shared__ double yk[kTile];
-  double* bk = d.b + 6LL * pi.image_begin + r0;
-  if (tid < m) {
-    double s = 0.0;
-    for (int q = 0; q <= tid; ++q) s += inv[tid][q] * bk[q];
-    yk[tid] = s;
-  }
-  __syncthreads();
-  if (k == pi.nt - 1) {
-    // first backward step: delta_k = L_kk^-T y_k
-    if (tid < m) {
-      double s = 0.0;
-      for (int q = tid; q < m; ++q) s += inv[q][tid] * yk[q];
-      bk[tid] = s;
-    }
-  } else if (tid < m) {
-    bk[tid] = yk[tid];
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ void load_tile_sym(const double* S, int n, int r0, int m,
-                                              double (*a)[kTile + 1]) {
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    int i = e / kTile, l = e % kTile;
-    double v = 0.0;
-    if (i < m && l < m) {
-      int gi = r0 + i, gl = r0 + l;
-      v = (l <= i) ? S[(long long)gi * n + gl] : S[(long long)gl * n + gi];
-    }
-    a[i][l] = v;
-  }
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(256) k_chol_diag0(DevPlan d) {
-  __shared__ double a[kTile][kTile + 1];
-  __shared__ double inv[kTile][kTile + 1];
-  __shared__ int fail;
-  const int p = blockIdx.x;
-  const LMState& st = d.state[p];
-  if (!st.active || d.factor_flag[p]) return;
-  const ProbInfo pi = d.prob[p];
-  if (pi.nt <= 0) return;
-  if (threadIdx.x == 0) fail = 0;
-  load_tile_sym(d.S + pi.s_off, pi.n, 0, tile_rows(pi.n, 0), a);
-  diag_factor(d, p, pi, 0, a, inv, &fail);
-}
-
-// L_ik = A_ik L_kk^-T for tiles i > k, and b_i -= L_ik y_k.
-__global__ void __launch_bounds__(256) k_chol_panel(DevPlan d, int k) {
-  __shared__ double A[kTile][kTile + 1];
-  __shared__ double Li[kTile][kTile + 1];
-  __shared__ double L[kTile][kTile + 1];
-  __shared__ double yk[kTile];
-  const int p = blockIdx.y;
-  const LMState& st = d.state[p];
-  if (!st.active || d.factor_flag[p]) return;
-  const ProbInfo pi = d.prob[p];
-  const int i = k + 1 + blockIdx.x;
-  if (i >= pi.nt) return;
-  const int n = pi.n, mi = tile_rows(n, i), m = tile_rows(n, k);
-  const double* S = d.S + pi.s_off;
-  const double* Lg = d.Linv + ((long long)p * d.max_nt + k) * kTile * kTile;
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    int r = e / kTile, c = e % kTile;
-    A[r][c] = (r < mi && c < m) ? S[(long long)(kTile * i + r) * n + kTile * k + c] : 0.0;
-    Li[r][c] = Lg[e];
-  }
-  double* b = d.b + 6LL * pi.image_begin;
-  if (threadIdx.x < kTile) yk[threadIdx.x] = threadIdx.x < m ? b[kTile * k + threadIdx.x] : 0.0;
-  __syncthreads();
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    int r = e / kTile, c = e % kTile;
-    double s = 0.0;
-    for (int q = 0; q <= c; ++q) s += A[r][q] * Li[c][q];
-    L[r][c] = s;
-  }
-  __syncthreads();
-  double* Sw = d.S + pi.s_off;
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    int r = e / kTile, c = e % kTile;
-    if (r < mi && c < m) Sw[(long long)(kTile * i + r) * n + kTile * k + c] = L[r][c];
-  }
-  if (threadIdx.x < mi) {
-    double s = 0.0;
-    for (int c = 0; c < m; ++c) s += L[threadIdx.x][c] * yk[c];
-    b[kTile * i + threadIdx.x] -= s;
-  }
-}
-
-// Trailing update A_ij -= L_ik L_jk^T for k < j <= i; the CTA owning tile
-// (k+1, k+1) then factors it.
-__global__ void __launch_bounds__(256) k_chol_update(DevPlan d, int k) {
-  __shared__ double Lik[kTile][kTile + 1];
-  __shared__ double Ljk[kTile][kTile + 1];
-  __shared__ double inv[kTile][kTile + 1];
-  __shared__ int fail;
-  const int p = blockIdx.y;
-  const LMState& st = d.state[p];
-  if (!st.active || d.factor_flag[p]) return;
-  const ProbInfo pi = d.prob[p];
-  const int T = pi.nt - k - 1;   // trailing tiles of this problem (may be <= 0)
-  const int lin = blockIdx.x;
-  if (T <= 0 || lin >= T * (T + 1) / 2) return;
-  // decode lin -> (ti, tj), tj <= ti
-  int ti = int((sqrt(8.0 * lin + 1.0) - 1.0) * 0.5);
-  while ((ti + 1) * (ti + 2) / 2 <= lin) ++ti;
-  while (ti * (ti + 1) / 2 > lin) --ti;
-  const int tj = lin - ti * (ti + 1) / 2;
-  const int i = k + 1 + ti, j = k + 1 + tj;
-  const int n = pi.n, mi = tile_rows(n, i), mj = tile_rows(n, j), m = tile_rows(n, k);
-  double* S = d.S + pi.s_off;
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    int r = e / kTile, c = e % kTile;
-    Lik[r][c] = (r < mi && c < m) ? S[(long long)(kTile * i + r) * n + kTile * k + c] : 0.0;
-    Ljk[r][c] = (r < mj && c < m) ? S[(long long)(kTile * j + r) * n + kTile * k + c] : 0.0;
-  }
-  __syncthreads();
-  const bool diag = (i == j);
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    int r = e / kTile, c = e % kTile;
-    if (r < mi && c < mj && (!diag || c <= r)) {
-      double s = 0.0;
+  const int mi = tile_rows(n, i);
+  if (i == c) {
+    T* Lg = tptr_mut<T>(d.Linv) + ((long long)p * d.max_nt + c) * kTile * kTile;
+    for (int e = tid; e < kTile * kTile; e += blockDim.x) Lg[e] = Dinv[e / kTile][e % kTile];
+    if (tid < kTile) {
+      T y = T(0);
 #pragma unroll 8
-      for (int q = 0; q < kTile; ++q) s += Lik[r][q] * Ljk[c][q];
-      long long off = (long long)(kTile * i + r) * n + kTile * j + c;
-      double v = S[off] - s;
-      S[off] = v;
-      if (diag && i == k + 1) inv[r][c] = v;  // stash for the fused factorization
+      for (int q = 0; q < kTile; ++q) y += Dinv[tid][q] * tv[q];
+      yk[tid] = y;
     }
-  }
-  if (diag && i == k + 1) {
     __syncthreads();
-    // mirror the lower part into a full symmetric tile
-    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-      int r = e / kTile, c = e % kTile;
-      if (r < mi && c < mi) {
-        if (c <= r) Lik[r][c] = inv[r][c];
+    if (tid < mi) {
+      if (c == pi.nt - 1) {           // last tile: first backward step
+        T dl = T(0);
+        for (int q = tid; q < kTile; ++q) dl += Dinv[q][tid] * yk[q];
+        b[kTile * c + tid] = dl;
       } else {
-        Lik[r][c] = 0.0;
+        b[kTile * c + tid] = yk[tid];
       }
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-      int r = e / kTile, c = e % kTile;
-      if (r < mi && c < mi && c > r) Lik[r][c] = Lik[c][r];
+    return;
+  }
+  // i > c: L_ic = A_ic L_cc^-T, and the column-k part of the forward solve
+  if (tid < mi) b[kTile * i + tid] = tv[tid];
+  {
+    const int r = tid >> 3, c0 = (tid & 7) * 4;
+    T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+#pragma unroll 8
+    for (int q = 0; q < kTile; ++q) {
+      const T x = A[r][q];
+      s0 += x * Dinv[c0][q];
+      s1 += x * Dinv[c0 + 1][q];
+      s2 += x * Dinv[c0 + 2][q];
+      s3 += x * Dinv[c0 + 3][q];
     }
-    if (threadIdx.x == 0) fail = 0;
-    __syncthreads();
-    diag_factor(d, p, pi, k + 1, Lik, inv, &fail);
+    if (r < mi) {
+      T* row = S + (long long)(kTile * i + r) * n + kTile * c;
+      row[c0] = s0;
+      row[c0 + 1] = s1;
+      row[c0 + 2] = s2;
+      row[c0 + 3] = s3;
+    }
   }
 }
 
 // Backward solve step k (k >= 1): y_j -= L_kj^T delta_k for j < k; the CTA
 // for j = k-1 then computes delta_{k-1} = L_{k-1,k-1}^-T y_{k-1}.
-__global__ void __launch_bounds__(128) k_chol_backward(DevPlan d, int k) {
-  __shared__ double dk[kTile];
-  __shared__ double yj[kTile];
+template <typename T>
+__global__ void __launch_bounds__(256) k_chol_backward(DevPlan d, int k) {
+  __shared__ Tile<T> L;
+  __shared__ T dk[kTile], yj[kTile];
   const int p = blockIdx.y;
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p]) return;
@@ -923,25 +964,27 @@ __global__ void __launch_bounds__(128) k_chol_backward(DevPlan d, int k) {
   const int j = blockIdx.x;
   if (j >= k) return;
   const int n = pi.n, m = tile_rows(n, k);
-  const double* S = d.S + pi.s_off;
-  double* b = d.b + 6LL * pi.image_begin;
-  if (threadIdx.x < kTile) dk[threadIdx.x] = threadIdx.x < m ? b[kTile * k + threadIdx.x] : 0.0;
+  const T* S = tptr<T>(d.S) + pi.s_off;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
+  load_rect<T>(S, n, k, j, L);
+  if (threadIdx.x < kTile) dk[threadIdx.x] = threadIdx.x < m ? b[kTile * k + threadIdx.x] : T(0);
   __syncthreads();
   if (threadIdx.x < kTile) {
     const int c = threadIdx.x;
-    double s = 0.0;
-    for (int r = 0; r < m; ++r) s += S[(long long)(kTile * k + r) * n + kTile * j + c] * dk[r];
-    double y = b[kTile * j + c] - s;
+    T s = T(0);
+#pragma unroll 8
+    for (int r = 0; r < kTile; ++r) s += L[r][c] * dk[r];
+    const T y = b[kTile * j + c] - s;
     yj[c] = y;
     if (j != k - 1) b[kTile * j + c] = y;
   }
   if (j == k - 1) {
     __syncthreads();
-    const double* Li = d.Linv + ((long long)p * d.max_nt + j) * kTile * kTile;
+    const T* Lv = tptr<T>(d.Linv) + ((long long)p * d.max_nt + j) * kTile * kTile;
     if (threadIdx.x < kTile) {
       const int c = threadIdx.x;
-      double s = 0.0;
-      for (int q = c; q < kTile; ++q) s += Li[q * kTile + c] * yj[q];
+      T s = T(0);
+      for (int q = c; q < kTile; ++q) s += Lv[q * kTile + c] * yj[q];
       b[kTile * j + c] = s;
     }
   }
@@ -969,10 +1012,10 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       for (int k = kb; k < ke; ++k) {
         T z[kZStride];
         load_vec<kZStride>(Z + (long long)kZStride * k, z);
-        const double* di = d.b + 6LL * __ldg(d.key_img + k);
+        const T* di = tptr<T>(d.b) + 6LL * __ldg(d.key_img + k);
         T dl[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) dl[c] = T(di[c]);
+        for (int c = 0; c < 6; ++c) dl[c] = di[c];
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
           t0 -= z[c] * dl[c];
@@ -1011,7 +1054,7 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
     double dn2 = 0.0, xn2 = 0.0, gd = 0.0;
     const long long e0 = 6LL * ch.begin, e1 = 6LL * ch.end;
     for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      double dv = d.b[e], xv = d.x_img[par][e];
+      double dv = double(tptr<T>(d.b)[e]), xv = d.x_img[par][e];
       d.x_img[1 - par][e] = xv - dv;
       dn2 += dv * dv;
       xn2 += xv * xv;
@@ -1182,6 +1225,23 @@ __global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out) {
 }
 
 template <typename T>
+int run_cholesky(const DevPlan& d, cudaStream_t s) {
+  int n = 0;
+  k_chol_step<T><<<dim3(unsigned(d.max_nt), unsigned(d.B)), 256, 0, s>>>(d, -1);
+  ++n;
+  for (int k = 0; k + 1 < d.max_nt; ++k) {
+    const int Tn = d.max_nt - k - 1;
+    k_chol_step<T><<<dim3(unsigned(Tn * (Tn + 1) / 2), unsigned(d.B)), 256, 0, s>>>(d, k);
+    ++n;
+  }
+  for (int k = d.max_nt - 1; k >= 1; --k) {
+    k_chol_backward<T><<<dim3(unsigned(k), unsigned(d.B)), 256, 0, s>>>(d, k);
+    ++n;
+  }
+  return n;
+}
+
+template <typename T>
 void run_image_prep(const DevPlan& d, int which, cudaStream_t s) {
   if (d.I > 0) k_image_prep<T><<<(d.I + 127) / 128, 128, 0, s>>>(d, which);
 }
@@ -1236,9 +1296,10 @@ int launch_linearize(const DevPlan& d, cudaStream_t s) {
 }
 
 int launch_image_reduce(const DevPlan& d, cudaStream_t s) {
-  if (d.n_img_chunks <= 0) return 0;
-  GBA_DISPATCH(d, (k_image_reduce<T><<<d.n_img_chunks, 32 * kImageChunk, 0, s>>>(d)));
-  return 1;
+  if (d.n_img_items <= 0) return 0;
+  GBA_DISPATCH(d, (k_image_reduce<T><<<(d.n_img_items + 7) / 8, 256, 0, s>>>(d)));
+  k_image_finalize<<<(d.I + 7) / 8, 256, 0, s>>>(d);
+  return 2;
 }
 
 int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s) {
@@ -1261,7 +1322,7 @@ int launch_assemble_items(const DevPlan& d, cudaStream_t s) {
 int launch_assemble_S(const DevPlan& d, cudaStream_t s) {
   if (d.max_n <= 0) return 0;
   dim3 grid(unsigned((1LL * d.max_n * d.max_n + 255) / 256), unsigned(d.B));
-  k_assemble_S<<<grid, 256, 0, s>>>(d);
+  GBA_DISPATCH(d, (k_assemble_S<T><<<grid, 256, 0, s>>>(d)));
   return 1;
 }
 
@@ -1272,21 +1333,7 @@ int launch_assemble(const DevPlan& d, cudaStream_t s) {
 int launch_cholesky(const DevPlan& d, cudaStream_t s) {
   if (d.max_nt <= 0) return 0;
   int n = 0;
-  k_chol_diag0<<<d.B, 256, 0, s>>>(d);
-  ++n;
-  for (int k = 0; k + 1 < d.max_nt; ++k) {
-    dim3 gp(unsigned(d.max_nt - 1 - k), unsigned(d.B));
-    k_chol_panel<<<gp, 256, 0, s>>>(d, k);
-    const int T = d.max_nt - k - 1;
-    dim3 gu(unsigned(T * (T + 1) / 2), unsigned(d.B));
-    k_chol_update<<<gu, 256, 0, s>>>(d, k);
-    n += 2;
-  }
-  for (int k = d.max_nt - 1; k >= 1; --k) {
-    dim3 gb(unsigned(k), unsigned(d.B));
-    k_chol_backward<<<gb, 128, 0, s>>>(d, k);
-    ++n;
-  }
+  GBA_DISPATCH(d, n = run_cholesky<T>(d, s));
   return n;
 }
 

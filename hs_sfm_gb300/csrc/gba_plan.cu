@@ -220,6 +220,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   std::vector<int> blk_map;
   std::vector<long long> blk_map_off(nprob, 0);
   std::vector<Chunk> key_chunks, pt_chunks, img_chunks;
+  std::vector<int4> img_items;
+  std::vector<int> img_item_off(1, 0);
   std::vector<int> prob_key_chunk_off(1, 0), prob_pt_chunk_off(1, 0), prob_img_chunk_off(1, 0);
   prob.resize(nprob);
   key_sorted_to_orig.resize(nprob);
@@ -315,6 +317,12 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         img_keys[kb + cur[li]++] = int(kb + t);
       }
       for (int i = 0; i <= ni; ++i) img_key_off[ib + i] = int(kb + ic[i]);
+      for (int i = 0; i < ni; ++i) {
+        const int q0 = img_key_off[ib + i], q1 = img_key_off[ib + i + 1];
+        for (int qq = q0; qq < q1; qq += kImageItem)
+          img_items.push_back(make_int4(int(ib + i), qq, std::min(q1, qq + kImageItem), q));
+        img_item_off.push_back(int(img_items.size()));
+      }
     }
     // reduced-system blocks: (i <= j) with their key pairs, point order
     {
@@ -425,6 +433,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.img_keys = arena.upload(img_keys);
   D.img_prob = arena.upload(img_prob);
   D.img_cam = arena.upload(img_cam);
+  D.n_img_items = int(img_items.size());
+  D.img_items = arena.upload(img_items);
+  D.img_item_off = arena.upload(img_item_off);
+  D.img_item_partial = arena.alloc<double>(28 * std::max<size_t>(img_items.size(), 1));
   D.cam64 = arena.upload(cam64);
   D.cam32 = arena.upload(cam32);
   for (int t = 0; t < 2; ++t) {
@@ -442,9 +454,9 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.PS = arena.alloc<char>(12 * P * tsz);
   D.U = arena.alloc<double>(36 * I);
   D.gi = arena.alloc<double>(6 * I);
-  D.S = arena.alloc<double>(size_t(std::max<long long>(s_off, 1)));
-  D.b = arena.alloc<double>(6 * I);
-  D.Linv = arena.alloc<double>(size_t(nprob) * std::max(max_nt, 1) * kTile * kTile);
+  D.S = arena.alloc<char>(size_t(std::max<long long>(s_off, 1)) * tsz);
+  D.b = arena.alloc<char>(size_t(std::max<int64_t>(6 * I, 1)) * tsz);
+  D.Linv = arena.alloc<char>(size_t(nprob) * std::max(max_nt, 1) * kTile * kTile * tsz);
   D.factor_flag = arena.alloc<int>(nprob);
   D.pairs = arena.upload(pairs);
   D.items = arena.upload(items);
@@ -1019,7 +1031,13 @@ int gba_schur_step(const gba_problem* problem, const double* x, const double* ne
     std::vector<double> x0p(3 * pi.num_points), x1p(3 * pi.num_points), di(6 * pi.num_images);
     GBA_CUDA(cudaMemcpy(x0p.data(), P.d.x_pt[0], sizeof(double) * x0p.size(), cudaMemcpyDeviceToHost));
     GBA_CUDA(cudaMemcpy(x1p.data(), P.d.x_pt[1], sizeof(double) * x1p.size(), cudaMemcpyDeviceToHost));
-    GBA_CUDA(cudaMemcpy(di.data(), P.d.b, sizeof(double) * di.size(), cudaMemcpyDeviceToHost));
+    if (P.d.precision == GBA_PRECISION_MIXED) {
+      std::vector<float> df(di.size());
+      GBA_CUDA(cudaMemcpy(df.data(), P.d.b, sizeof(float) * df.size(), cudaMemcpyDeviceToHost));
+      std::copy(df.begin(), df.end(), di.begin());
+    } else {
+      GBA_CUDA(cudaMemcpy(di.data(), P.d.b, sizeof(double) * di.size(), cudaMemcpyDeviceToHost));
+    }
     for (size_t i = 0; i < x0p.size(); ++i) delta_x[i] = x0p[i] - x1p[i];
     std::copy(di.begin(), di.end(), delta_x + x0p.size());
     return GBA_OK;

@@ -1,8 +1,8 @@
 """CPU model of the dense-Cholesky launches of libgba.so: for batches of
 problems of uneven size, every S / b / Linv element a kernel touches must
 lie inside that problem's own region.  The model restates each kernel's
-grid and early-exit guards (hs_sfm_gb300/csrc/gba_kernels.cu: k_chol_diag0,
-k_chol_panel, k_chol_update with its fused diagonal factorization,
+grid and early-exit guards (hs_sfm_gb300/csrc/gba_kernels.cu: k_chol_step for
+k = -1 .. nt-2 with its redundant per-column diagonal factorization,
 k_chol_backward, k_assemble_S)."""
 import math
 
@@ -61,40 +61,39 @@ class Batch:
         self.check_linv(p, k)
         self.check_b(p, TILE * k, m)
 
+    def step_tile(self, p, k, i, j):
+        n, c = self.n[p], k + 1
+        mi, mj = rows(n, i), rows(n, j)
+        assert c <= j <= i < self.nt[p]
+        self.check_S(p, TILE * i, mi, TILE * j, mj)            # own tile
+        if k >= 0:
+            assert k <= self.nt[p] - 2                         # tile k is full
+            self.check_S(p, TILE * i, mi, TILE * k, rows(n, k))
+            self.check_S(p, TILE * j, mj, TILE * k, rows(n, k))
+            self.check_b(p, TILE * k, TILE)                    # y_k
+        if j == c:
+            self.check_S(p, TILE * c, rows(n, c), TILE * c, rows(n, c))  # diagonal tile
+            self.check_b(p, TILE * i, mi)
+            if i == c:
+                self.check_linv(p, c)
+
     def run(self):
         touched = 0
-        for p in range(self.B):                      # k_chol_diag0
-            if self.nt[p] <= 0:
-                continue
-            self.diag(p, 0)
-        for k in range(self.max_nt - 1):
-            for bx in range(self.max_nt - 1 - k):    # k_chol_panel
-                for p in range(self.B):
-                    i = k + 1 + bx
-                    if i >= self.nt[p]:
-                        continue
-                    mi, m = rows(self.n[p], i), rows(self.n[p], k)
-                    self.check_S(p, TILE * i, mi, TILE * k, m)
-                    self.check_linv(p, k)
-                    self.check_b(p, TILE * k, m)
-                    self.check_b(p, TILE * i, mi)
-                    touched += 1
-            Tg = self.max_nt - k - 1                 # k_chol_update
+        for bx in range(self.max_nt):                 # k_chol_step, k = -1
+            for p in range(self.B):
+                if bx >= self.nt[p]:
+                    continue
+                self.step_tile(p, -1, bx, 0)
+                touched += 1
+        for k in range(self.max_nt - 1):              # k_chol_step, k >= 0
+            Tg = self.max_nt - k - 1
             for lin in range(Tg * (Tg + 1) // 2):
                 for p in range(self.B):
-                    T = self.nt[p] - k - 1
-                    if T <= 0 or lin >= T * (T + 1) // 2:
+                    Tn = self.nt[p] - (k + 1)
+                    if Tn <= 0 or lin >= Tn * (Tn + 1) // 2:
                         continue
                     ti, tj = decode(lin)
-                    i, j = k + 1 + ti, k + 1 + tj
-                    assert j <= i < self.nt[p]
-                    n = self.n[p]
-                    mi, mj, m = rows(n, i), rows(n, j), rows(n, k)
-                    self.check_S(p, TILE * i, mi, TILE * k, m)
-                    self.check_S(p, TILE * j, mj, TILE * k, m)
-                    self.check_S(p, TILE * i, mi, TILE * j, mj)
-                    if i == j == k + 1:
-                        self.diag(p, k + 1)
+                    self.step_tile(p, k, k + 1 + ti, k + 1 + tj)
                     touched += 1
         for k in range(self.max_nt - 1, 0, -1):     # k_chol_backward
             for j in range(k):

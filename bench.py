@@ -164,7 +164,8 @@ class ClockSampler:
 def stage_bytes(K, P, I, pairs, items, tsz):
     """Per launch, for the stages of one LM iteration."""
     return {
-        "linearize": K * (4 + 4 * tsz + 20 * tsz + 4) + P * (24 + 4 + 12 * tsz) + I * 42 * 8,
+        "linearize": K * (4 + 4 * tsz + 20 * tsz) + P * (24 + 4 + 12 * tsz),
+        "image_reduce": K * (4 + 14 * tsz) + I * 42 * 8,
         "point_schur": K * (20 * tsz + 18 * tsz) + P * (12 * tsz + 12 * tsz + 4),
         "assemble": K * 18 * tsz + pairs * 8 + items * (16 + 42 * 8) + P * 3 * tsz,
         "backsub": K * (18 * tsz + 4) + P * (12 * tsz + 24 + 24 + 4) + I * 6 * 8 * 3,

@@ -43,9 +43,9 @@ LOSS_HUBER = 1
 LINEAR_DENSE_CHOLESKY = 0
 LINEAR_PCG = 1
 
-NUM_STAGES = 8
+NUM_STAGES = 12
 STAGE_NAMES = ["linearize", "point_schur", "assemble", "factor", "backsub", "cost",
-               "control", "other"]
+               "control", "assemble_dense", "solve", "image_reduce", "image_prep", "reserved"]
 
 
 class PointConstraint(C.Structure):

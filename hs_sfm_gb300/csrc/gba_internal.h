@@ -155,6 +155,8 @@ int launch_assemble(const DevPlan& d, cudaStream_t s);
 int launch_assemble_items(const DevPlan& d, cudaStream_t s);
 int launch_assemble_S(const DevPlan& d, cudaStream_t s);
 int launch_cholesky(const DevPlan& d, cudaStream_t s);
+int launch_cholesky_factor(const DevPlan& d, cudaStream_t s);
+int launch_cholesky_solve(const DevPlan& d, cudaStream_t s);
 int launch_backsub(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_step(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_accept(const DevPlan& d, cudaStream_t s);

@@ -740,32 +740,47 @@ __device__ __forceinline__ int tile_rows(int n, int t) { return min(kTile, n - k
 template <typename T>
 using Tile = T[kTile][kTile + 1];
 
-// Rectangular tile (ti, tj) of S; entries past the matrix read 0.
-template <typename T>
-__device__ void load_rect(const T* S, int n, int ti, int tj, Tile<T>& t) {
-  const int mi = tile_rows(n, ti), mj = tile_rows(n, tj);
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    const int r = e / kTile, c = e % kTile;
-    t[r][c] = (r < mi && c < mj) ? S[(long long)(kTile * ti + r) * n + kTile * tj + c] : T(0);
-  }
-}
+// Tile loads for 256-thread CTAs: each thread fetches its 4 elements of a
+// tile into registers first (all loads in flight together), then stores
+// them to shared memory.  Rectangular tiles read 0 past the matrix; a
+// diagonal tile keeps its stored lower triangle, reads 0 above it and has
+// identity rows past the matrix.
+constexpr int kCholThreads = 256;
+constexpr int kPerThread = kTile * kTile / kCholThreads;
 
-// Diagonal tile (ti, ti): the stored lower triangle; the upper triangle reads
-// 0 and rows past the matrix are identity rows.
 template <typename T>
-__device__ void load_diag(const T* S, int n, int ti, Tile<T>& t) {
-  const int m = tile_rows(n, ti);
-  for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-    const int r = e / kTile, c = e % kTile;
-    T v = T(0);
-    if (r < m) {
-      if (c <= r) v = S[(long long)(kTile * ti + r) * n + kTile * ti + c];
-    } else if (r == c) {
-      v = T(1);
+struct TileFetch {
+  T v[kPerThread];
+  __device__ __forceinline__ void rect(const T* S, int n, int ti, int tj) {
+    const int mi = tile_rows(n, ti), mj = tile_rows(n, tj);
+#pragma unroll
+    for (int u = 0; u < kPerThread; ++u) {
+      const int e = threadIdx.x + u * kCholThreads, r = e / kTile, c = e % kTile;
+      v[u] = (r < mi && c < mj) ? S[(long long)(kTile * ti + r) * n + kTile * tj + c] : T(0);
     }
-    t[r][c] = v;
   }
-}
+  __device__ __forceinline__ void diag(const T* S, int n, int ti) {
+    const int m = tile_rows(n, ti);
+#pragma unroll
+    for (int u = 0; u < kPerThread; ++u) {
+      const int e = threadIdx.x + u * kCholThreads, r = e / kTile, c = e % kTile;
+      T x = T(0);
+      if (r < m) {
+        if (c <= r) x = S[(long long)(kTile * ti + r) * n + kTile * ti + c];
+      } else if (r == c) {
+        x = T(1);
+      }
+      v[u] = x;
+    }
+  }
+  __device__ __forceinline__ void store(Tile<T>& t) const {
+#pragma unroll
+    for (int u = 0; u < kPerThread; ++u) {
+      const int e = threadIdx.x + u * kCholThreads;
+      t[e / kTile][e % kTile] = v[u];
+    }
+  }
+};
 
 // A -= X Y^T (32x32x32), 256 threads, 4 outputs each.
 template <typename T>
@@ -786,11 +801,15 @@ __device__ __forceinline__ void tile_sub_xyt(Tile<T>& A, const Tile<T>& X, const
   A[r][c0 + 3] -= s3;
 }
 
-// Factor the SPD tile D (lower triangle used; identity-padded) in one warp,
-// lane i holding row i, and write L^-1 to Dinv.  Returns false when a pivot
-// was not positive.
+// Factor the SPD tile D (lower triangle used; identity-padded) in one warp and
+// write L^-1 to Dinv; D is overwritten by L.  Lane i keeps row i of the
+// tile in registers; each factored column is broadcast through shared memory
+// (col, double-buffered) and the reciprocal pivots are kept in rinv.  The
+// inverse is formed one column per lane by forward substitution against L in
+// shared memory, with the stored reciprocals (no divisions).  Returns false
+// when a pivot was not positive.
 template <typename T>
-__device__ bool warp_potrf_inverse(const Tile<T>& D, Tile<T>& Dinv, int lane) {
+__device__ bool warp_potrf_inverse(Tile<T>& D, Tile<T>& Dinv, T* col, T* rinv, int lane) {
   constexpr unsigned FULL = 0xffffffffu;
   T a[kTile];
 #pragma unroll
@@ -800,43 +819,46 @@ __device__ bool warp_potrf_inverse(const Tile<T>& D, Tile<T>& Dinv, int lane) {
   for (int j = 0; j < kTile; ++j) {
     const T djj = __shfl_sync(FULL, a[j], j);
     ok = ok && (djj > T(0));
-    const T ljj = sqrt(djj);
-    const T rinv = T(1) / ljj;
-    const T lij = (lane > j) ? a[j] * rinv : ((lane == j) ? ljj : T(0));
+    const T r = rsqrt(djj);
+    const T ljj = djj * r;
+    if (lane == j) rinv[j] = r;
+    const T lij = (lane > j) ? a[j] * r : ((lane == j) ? ljj : T(0));
     a[j] = lij;
+    T* cb = col + (j & 1) * kTile;
+    cb[lane] = lij;
+    __syncwarp();
 #pragma unroll
-    for (int l = j + 1; l < kTile; ++l) {
-      const T llj = __shfl_sync(FULL, lij, l);
-      a[l] -= lij * llj;
-    }
+    for (int l = j + 1; l < kTile; ++l) a[l] -= lij * cb[l];
   }
-  // forward substitution L X = I, one row of X per lane, rows in order
+#pragma unroll
+  for (int c = 0; c < kTile; ++c) D[lane][c] = (c <= lane) ? a[c] : T(0);
+  __syncwarp();
   T x[kTile];
 #pragma unroll
-  for (int c = 0; c < kTile; ++c) x[c] = (c == lane) ? T(1) : T(0);
+  for (int r = 0; r < kTile; ++r) x[r] = (r == lane) ? T(1) : T(0);
 #pragma unroll
   for (int q = 0; q < kTile; ++q) {
-    const T rq = T(1) / __shfl_sync(FULL, a[q], q);
-    if (lane == q) {
+    x[q] *= rinv[q];
 #pragma unroll
-      for (int c = 0; c <= q; ++c) x[c] *= rq;
-    }
-    const T liq = a[q];
-#pragma unroll
-    for (int c = 0; c <= q; ++c) {
-      const T xqc = __shfl_sync(FULL, x[c], q);
-      if (lane > q) x[c] -= liq * xqc;
-    }
+    for (int r = q + 1; r < kTile; ++r) x[r] -= D[r][q] * x[q];
   }
 #pragma unroll
-  for (int c = 0; c < kTile; ++c) Dinv[lane][c] = (c <= lane) ? x[c] : T(0);
+  for (int r = 0; r < kTile; ++r) Dinv[r][lane] = x[r];
   return ok;
 }
+
+// Programmatic dependent launch: the Cholesky kernels are launched so that
+// their CTAs may start while the previous kernel drains; griddepcontrol.wait
+// blocks until the previous grid has completed and its writes are visible.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
   __shared__ Tile<T> A, Li, Lj, D, Dinv;
   __shared__ T yk[kTile], tv[kTile];
+  pdl_wait();
+  pdl_trigger();
   const int p = blockIdx.y;
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p]) return;
@@ -852,7 +874,7 @@ __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
   } else {
     const int lin = blockIdx.x;
     if (lin >= Tn * (Tn + 1) / 2) return;
-    int ti = int((sqrt(8.0 * lin + 1.0) - 1.0) * 0.5);
+    int ti = int((sqrtf(8.0f * float(lin) + 1.0f) - 1.0f) * 0.5f);
     while ((ti + 1) * (ti + 2) / 2 <= lin) ++ti;
     while (ti * (ti + 1) / 2 > lin) --ti;
     i = c + ti;
@@ -862,14 +884,25 @@ __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
   T* S = tptr_mut<T>(d.S) + pi.s_off;
   T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // own tile and, for k >= 0, the column-k factors
-  if (i == j) load_diag<T>(S, n, i, A); else load_rect<T>(S, n, i, j, A);
+  // own tile and, for k >= 0, the column-k factors: all loads issued first
+  TileFetch<T> fa, fi, fj, fd;
+  if (i == j) fa.diag(S, n, i); else fa.rect(S, n, i, j);
   if (k >= 0) {
-    load_rect<T>(S, n, i, k, Li);
-    load_rect<T>(S, n, j, k, Lj);
-    if (tid < kTile) yk[tid] = b[kTile * k + tid];   // y_k (tile k is full)
+    fi.rect(S, n, i, k);
+    fj.rect(S, n, j, k);
   }
-  if (j == c && i != c) load_diag<T>(S, n, c, D);
+  const bool need_d = (j == c && i != c);
+  if (need_d) fd.diag(S, n, c);
+  T ykv = T(0), bv = T(0);
+  if (k >= 0 && tid < kTile) ykv = b[kTile * k + tid];   // y_k (tile k is full)
+  if (j == c && tid < kTile && tid < tile_rows(n, i)) bv = b[kTile * i + tid];
+  fa.store(A);
+  if (k >= 0) {
+    fi.store(Li);
+    fj.store(Lj);
+    if (tid < kTile) yk[tid] = ykv;
+  }
+  if (need_d) fd.store(D);
   __syncthreads();
   if (k >= 0) {
     tile_sub_xyt<T>(A, Li, Lj);
@@ -877,8 +910,7 @@ __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
   }
   if (j == c && tid < kTile) {
     // b_i after column k: b_i - L_ik y_k
-    const int mi = tile_rows(n, i);
-    T t = tid < mi ? b[kTile * i + tid] : T(0);
+    T t = bv;
     if (k >= 0) {
 #pragma unroll 8
       for (int q = 0; q < kTile; ++q) t -= Li[tid][q] * yk[q];
@@ -896,8 +928,9 @@ __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
   }
   // column c: factor the diagonal tile (own tile when i == c)
   __shared__ int ok_s;
+  __shared__ T colbuf[2 * kTile], rinv[kTile];
   if (warp == 0) {
-    const bool ok = warp_potrf_inverse<T>(i == c ? A : D, Dinv, lane);
+    const bool ok = warp_potrf_inverse<T>(i == c ? A : D, Dinv, colbuf, rinv, lane);
     if (lane == 0) ok_s = ok ? 1 : 0;
   }
   __syncthreads();
@@ -956,6 +989,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_chol_backward(DevPlan d, int k) {
   __shared__ Tile<T> L;
   __shared__ T dk[kTile], yj[kTile];
+  pdl_wait();
+  pdl_trigger();
   const int p = blockIdx.y;
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p]) return;
@@ -966,15 +1001,22 @@ __global__ void __launch_bounds__(256) k_chol_backward(DevPlan d, int k) {
   const int n = pi.n, m = tile_rows(n, k);
   const T* S = tptr<T>(d.S) + pi.s_off;
   T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
-  load_rect<T>(S, n, k, j, L);
-  if (threadIdx.x < kTile) dk[threadIdx.x] = threadIdx.x < m ? b[kTile * k + threadIdx.x] : T(0);
+  TileFetch<T> fl;
+  fl.rect(S, n, k, j);
+  T dv = T(0), yv = T(0);
+  if (threadIdx.x < kTile) {
+    dv = threadIdx.x < m ? b[kTile * k + threadIdx.x] : T(0);
+    yv = b[kTile * j + threadIdx.x];
+  }
+  fl.store(L);
+  if (threadIdx.x < kTile) dk[threadIdx.x] = dv;
   __syncthreads();
   if (threadIdx.x < kTile) {
     const int c = threadIdx.x;
     T s = T(0);
 #pragma unroll 8
     for (int r = 0; r < kTile; ++r) s += L[r][c] * dk[r];
-    const T y = b[kTile * j + c] - s;
+    const T y = yv - s;
     yj[c] = y;
     if (j != k - 1) b[kTile * j + c] = y;
   }
@@ -1224,18 +1266,39 @@ __global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out) {
   for (int j = 0; j < 12; ++j) ji_out[12LL * k + j] = double(ji[j]);
 }
 
+template <typename Kernel>
+void launch_pdl(Kernel kernel, dim3 grid, dim3 block, cudaStream_t s, const DevPlan& d, int k) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, d, k);
+}
+
 template <typename T>
-int run_cholesky(const DevPlan& d, cudaStream_t s) {
+int run_cholesky_factor(const DevPlan& d, cudaStream_t s) {
   int n = 0;
-  k_chol_step<T><<<dim3(unsigned(d.max_nt), unsigned(d.B)), 256, 0, s>>>(d, -1);
+  launch_pdl(k_chol_step<T>, dim3(unsigned(d.max_nt), unsigned(d.B)), dim3(256), s, d, -1);
   ++n;
   for (int k = 0; k + 1 < d.max_nt; ++k) {
     const int Tn = d.max_nt - k - 1;
-    k_chol_step<T><<<dim3(unsigned(Tn * (Tn + 1) / 2), unsigned(d.B)), 256, 0, s>>>(d, k);
+    launch_pdl(k_chol_step<T>, dim3(unsigned(Tn * (Tn + 1) / 2), unsigned(d.B)), dim3(256), s, d, k);
     ++n;
   }
+  return n;
+}
+
+template <typename T>
+int run_cholesky_solve(const DevPlan& d, cudaStream_t s) {
+  int n = 0;
   for (int k = d.max_nt - 1; k >= 1; --k) {
-    k_chol_backward<T><<<dim3(unsigned(k), unsigned(d.B)), 256, 0, s>>>(d, k);
+    launch_pdl(k_chol_backward<T>, dim3(unsigned(k), unsigned(d.B)), dim3(256), s, d, k);
     ++n;
   }
   return n;
@@ -1330,11 +1393,22 @@ int launch_assemble(const DevPlan& d, cudaStream_t s) {
   return launch_assemble_items(d, s) + launch_assemble_S(d, s);
 }
 
-int launch_cholesky(const DevPlan& d, cudaStream_t s) {
+int launch_cholesky_factor(const DevPlan& d, cudaStream_t s) {
   if (d.max_nt <= 0) return 0;
   int n = 0;
-  GBA_DISPATCH(d, n = run_cholesky<T>(d, s));
+  GBA_DISPATCH(d, n = run_cholesky_factor<T>(d, s));
   return n;
+}
+
+int launch_cholesky_solve(const DevPlan& d, cudaStream_t s) {
+  if (d.max_nt <= 0) return 0;
+  int n = 0;
+  GBA_DISPATCH(d, n = run_cholesky_solve<T>(d, s));
+  return n;
+}
+
+int launch_cholesky(const DevPlan& d, cudaStream_t s) {
+  return launch_cholesky_factor(d, s) + launch_cholesky_solve(d, s);
 }
 
 int launch_backsub(const DevPlan& d, cudaStream_t s) {

@@ -500,14 +500,19 @@ void Plan::enqueue(bool profile) {
   };
   mark(-1);
   n += launch_init(d, s);
+  mark(GBA_STAGE_CONTROL);
   n += launch_image_prep(d, 0, s);
+  mark(GBA_STAGE_IMAGE_PREP);
   n += launch_cost(d, 0, s);
-  n += launch_ctrl_initial_cost(d, s);
   mark(GBA_STAGE_COST);
+  n += launch_ctrl_initial_cost(d, s);
+  mark(GBA_STAGE_CONTROL);
   n += launch_linearize(d, s);
-  n += launch_image_reduce(d, s);
-  n += launch_ctrl_after_linearize(d, s);
   mark(GBA_STAGE_LINEARIZE);
+  n += launch_image_reduce(d, s);
+  mark(GBA_STAGE_IMAGE_REDUCE);
+  n += launch_ctrl_after_linearize(d, s);
+  mark(GBA_STAGE_CONTROL);
   for (int it = 0; it < opt.max_iterations; ++it) {
     n += launch_point_schur(d, s);
     mark(GBA_STAGE_POINT_SCHUR);
@@ -515,21 +520,26 @@ void Plan::enqueue(bool profile) {
     mark(GBA_STAGE_ASSEMBLE);
     n += launch_assemble_S(d, s);
     mark(GBA_STAGE_OTHER);
-    n += launch_cholesky(d, s);
+    n += launch_cholesky_factor(d, s);
     mark(GBA_STAGE_FACTOR);
+    n += launch_cholesky_solve(d, s);
+    mark(GBA_STAGE_SOLVE);
     n += launch_backsub(d, s);
     mark(GBA_STAGE_BACKSUB);
     n += launch_ctrl_step(d, s);
     mark(GBA_STAGE_CONTROL);
     n += launch_image_prep(d, 1, s);
+    mark(GBA_STAGE_IMAGE_PREP);
     n += launch_cost(d, 1, s);
     mark(GBA_STAGE_COST);
     n += launch_ctrl_accept(d, s);
     mark(GBA_STAGE_CONTROL);
     n += launch_linearize(d, s);
-    n += launch_image_reduce(d, s);
-    n += launch_ctrl_after_linearize(d, s);
     mark(GBA_STAGE_LINEARIZE);
+    n += launch_image_reduce(d, s);
+    mark(GBA_STAGE_IMAGE_REDUCE);
+    n += launch_ctrl_after_linearize(d, s);
+    mark(GBA_STAGE_CONTROL);
   }
   GBA_CUDA(cudaGetLastError());
   launches_last_run = n;
@@ -538,7 +548,7 @@ void Plan::enqueue(bool profile) {
 int Plan::run() {
   const bool profile = opt.profile != 0;
   if (profile) {
-    const size_t need = 8 + size_t(opt.max_iterations) * 12;
+    const size_t need = 16 + size_t(opt.max_iterations) * 20;
     while (prof_events.size() < need) {
       cudaEvent_t e;
       GBA_CUDA(cudaEventCreate(&e));

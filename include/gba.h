@@ -172,16 +172,20 @@ GBA_API void gba_default_options(gba_options* options);
 #define GBA_STOP_SMALL_STEP     2
 #define GBA_STOP_ERROR          3
 
-#define GBA_NUM_STAGES 8
+#define GBA_NUM_STAGES 12
 /* stage indices of gba_report.stage_ms */
-#define GBA_STAGE_LINEARIZE   0
-#define GBA_STAGE_POINT_SCHUR 1
-#define GBA_STAGE_ASSEMBLE    2
-#define GBA_STAGE_FACTOR      3
-#define GBA_STAGE_BACKSUB     4
-#define GBA_STAGE_COST        5
-#define GBA_STAGE_CONTROL     6
-#define GBA_STAGE_OTHER       7
+#define GBA_STAGE_LINEARIZE    0   /* per-point Jacobians, V_p, g_p          */
+#define GBA_STAGE_POINT_SCHUR  1   /* C_p, Z, h_p                            */
+#define GBA_STAGE_ASSEMBLE     2   /* reduced-system block sums              */
+#define GBA_STAGE_FACTOR       3   /* Cholesky column steps + forward solve  */
+#define GBA_STAGE_BACKSUB      4   /* point back-substitution and update     */
+#define GBA_STAGE_COST         5   /* candidate cost                         */
+#define GBA_STAGE_CONTROL      6   /* LM decisions                           */
+#define GBA_STAGE_OTHER        7   /* dense reduced system from block sums   */
+#define GBA_STAGE_SOLVE        8   /* backward triangular solve              */
+#define GBA_STAGE_IMAGE_REDUCE 9   /* U_i, g_i                               */
+#define GBA_STAGE_IMAGE_PREP  10   /* image rotations                        */
+#define GBA_STAGE_RESERVED    11
 
 typedef struct gba_report {
   int32_t status;             /* GBA_OK or an error code                    */

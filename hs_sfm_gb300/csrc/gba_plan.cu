@@ -852,9 +852,13 @@ int gba_plan_last_run_launches(gba_plan* p, int64_t* n) {
 
 int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, int32_t n,
                     const gba_options* options, double* const* x_inout, gba_report* reports) {
-  if (!x_inout) return GBA_ERR_INVALID;
+  if (!x_inout || !options) return GBA_ERR_INVALID;
+  // A one-shot solve runs its launch sequence once: capturing it into a
+  // CUDA graph would cost more than it saves, so it is launched directly.
+  gba_options once = *options;
+  once.use_cuda_graph = 0;
   gba_plan* plan = nullptr;
-  int err = gba_plan_create(problems, near_ys, n, options, &plan);
+  int err = gba_plan_create(problems, near_ys, n, &once, &plan);
   if (err) return err;
   for (int q = 0; q < n && !err; ++q) err = gba_plan_set_initial_x(plan, q, x_inout[q]);
   if (!err) err = gba_plan_run(plan);

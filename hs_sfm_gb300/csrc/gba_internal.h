@@ -102,6 +102,10 @@ struct DevPlan {
   const double* x0_pt;
   const double* x0_img;
   double* img_rot[2];        // [12I] R (9) + t (3), FP64
+  float2* img_rot_ff[2];     // [12I] double-float mirror (mixed path) or null
+  float2* x_ff[2];           // [3P] double-float mirror of x_pt (mixed path) or null
+  const float2* key_obs_ff;  // [2K] double-float keys (mixed path) or null
+  const float2* cam_ff;      // [10C] double-float cameras, [9] = f * a (mixed path)
   void* img_lin[2];          // [12I] T: r(3) t(3) ct s c a1 a2 pad
   // per key
   void* RW[2];               // [4K] T: rw0 rw1 sqrt(w) pad  (whitened, weighted residual)

@@ -145,6 +145,60 @@ __device__ __forceinline__ void loss_eval(int loss, double delta, double s, doub
   }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic: a value is the unevaluated sum hi + lo of two
+// floats (about 48 significant bits).  Error-free transformations: Knuth's
+// two-sum, Dekker's fast two-sum, and the FMA-based exact product; the
+// reciprocal is one Newton step from the float reciprocal.  Used by the
+// mixed path to evaluate projections at FP64-class accuracy on the FP32
+// pipes (the FP64 pipe of this part issues at 1/57 of the FP32 rate).
+// ---------------------------------------------------------------------------
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ ff ff_add(ff x, ff y) {
+  const ff s = ff_two_sum(x.hi, y.hi);
+  return ff_fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+__device__ __forceinline__ ff ff_add_f(ff x, float y) {
+  const ff s = ff_two_sum(x.hi, y);
+  return ff_fast_two_sum(s.hi, s.lo + x.lo);
+}
+__device__ __forceinline__ ff ff_neg(ff x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ ff ff_mul(ff x, ff y) {
+  const float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, e);
+  e = fmaf(x.lo, y.hi, e);
+  return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ ff ff_mul_f(ff x, float y) {
+  const float p = x.hi * y;
+  float e = fmaf(x.hi, y, -p);
+  e = fmaf(x.lo, y, e);
+  return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
+__device__ __forceinline__ ff ff_rcp(ff y) {
+  const float r = 1.0f / y.hi;
+  const ff e = ff_add_f(ff_neg(ff_mul_f(y, r)), 1.0f);   // 1 - y r
+  return ff_add_f(ff_mul_f(e, r), r);                    // r + r (1 - y r)
+}
+__host__ __device__ __forceinline__ float2 ff_split(double d) {
+  const float hi = float(d);
+  return make_float2(hi, float(d - double(hi)));
+}
+__device__ __forceinline__ ff ff_ld(float2 v) { return {v.x, v.y}; }
+
 // Rodrigues coefficients of an angle-axis vector.  Near theta = 0 the
 // reference formulas divide by zero (analytical_jacobian_matrix_calculator.hpp
 // :359-380); series of sin and cos are used below theta = 1e-2.
@@ -305,8 +359,12 @@ __global__ void k_init(DevPlan d) {
 __global__ void k_copy_x0(DevPlan d) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   long long np = 3LL * d.P, ni = 6LL * d.I;
-  if (i < np) d.x_pt[0][i] = d.x0_pt[i];
-  else if (i < np + ni) d.x_img[0][i - np] = d.x0_img[i - np];
+  if (i < np) {
+    d.x_pt[0][i] = d.x0_pt[i];
+    if (d.x_ff[0]) d.x_ff[0][i] = ff_split(d.x0_pt[i]);
+  } else if (i < np + ni) {
+    d.x_img[0][i - np] = d.x0_img[i - np];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -336,6 +394,11 @@ __global__ void k_image_prep(DevPlan d, int which) {
     R[6] = -st_ * k1 + omc * k2 * k0; R[7] = st_ * k0 + omc * k2 * k1; R[8] = ct + omc * k2 * k2;
   }
   R[9] = x[3]; R[10] = x[4]; R[11] = x[5];
+  if (d.img_rot_ff[par]) {
+    float2* Rf = d.img_rot_ff[par] + 12LL * i;
+#pragma unroll
+    for (int j = 0; j < 12; ++j) Rf[j] = ff_split(R[j]);
+  }
   T* IL = tptr_mut<T>(d.img_lin[par]) + 12LL * i;
   IL[0] = T(r0); IL[1] = T(r1); IL[2] = T(r2);
   IL[3] = T(x[3]); IL[4] = T(x[4]); IL[5] = T(x[5]);
@@ -386,6 +449,82 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
     store_vec<4>(rw + 4LL * k, out);
   }
   double tot = block_sum(acc, red);
+  if (threadIdx.x == 0) d.key_chunk_sum[blockIdx.x] = tot;
+}
+
+// Mixed-path cost: the projection in double-float from the double-float
+// mirrors of x, R|t, the keys and the cameras; per-thread sums in
+// double-float, block sums in FP64.
+__global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
+  __shared__ double red[32];
+  const Chunk ch = d.key_chunks[blockIdx.x];
+  const LMState& st = d.state[ch.prob];
+  if (which == 0 ? !st.active : !st.evaluate) return;
+  const int par = which ? 1 - st.parity : st.parity;
+  const float2* __restrict__ xp = d.x_ff[par];
+  const float2* __restrict__ rot = d.img_rot_ff[par];
+  float* __restrict__ rw = static_cast<float*>(d.RW[par]);
+  ff acc = {0.0f, 0.0f};
+  for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
+    const int img = __ldg(d.key_img + k), pt = __ldg(d.key_pt + k);
+    const float2* R = rot + 12LL * img;
+    const ff X0 = ff_ld(xp[3LL * pt]), X1 = ff_ld(xp[3LL * pt + 1]), X2 = ff_ld(xp[3LL * pt + 2]);
+    ff y[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      ff a = ff_ld(R[9 + m]);
+      a = ff_fma(ff_ld(R[3 * m]), X0, a);
+      a = ff_fma(ff_ld(R[3 * m + 1]), X1, a);
+      y[m] = ff_fma(ff_ld(R[3 * m + 2]), X2, a);
+    }
+    const ff iz = ff_rcp(y[2]);
+    ff n0 = ff_mul(y[0], iz), n1 = ff_mul(y[1], iz);
+    const float2* cam = d.cam_ff + 10 * __ldg(d.img_cam + img);
+    const ff k1 = ff_ld(cam[0]), k2 = ff_ld(cam[1]), k3 = ff_ld(cam[2]);
+    const ff d1 = ff_ld(cam[3]), d2 = ff_ld(cam[4]);
+    const ff r2 = ff_add(ff_mul(n0, n0), ff_mul(n1, n1));
+    ff dx = {0.0f, 0.0f}, dy = {0.0f, 0.0f};
+    if (k1.hi != 0.0f || k2.hi != 0.0f || k3.hi != 0.0f) {
+      const ff coeff = ff_mul(r2, ff_fma(r2, ff_fma(r2, k3, k2), k1));
+      dx = ff_mul(coeff, n0);
+      dy = ff_mul(coeff, n1);
+    }
+    if (d1.hi != 0.0f || d2.hi != 0.0f) {
+      const ff xy2 = ff_mul_f(ff_mul(n0, n1), 2.0f);
+      dx = ff_add(dx, ff_add(ff_mul(d1, xy2), ff_mul(d2, ff_add(r2, ff_mul_f(ff_mul(n0, n0), 2.0f)))));
+      dy = ff_add(dy, ff_add(ff_mul(d2, xy2), ff_mul(d1, ff_add(r2, ff_mul_f(ff_mul(n1, n1), 2.0f)))));
+    }
+    n0 = ff_add(n0, dx);
+    n1 = ff_add(n1, dy);
+    const ff f = ff_ld(cam[5]), sk = ff_ld(cam[6]), cx = ff_ld(cam[7]), cy = ff_ld(cam[8]);
+    const ff fa = ff_ld(cam[9]);   // f * a, stored pre-multiplied
+    const ff u = ff_add(ff_fma(f, n0, ff_mul(sk, n1)), cx);
+    const ff v = ff_fma(fa, n1, cy);
+    const float2 ob0 = d.key_obs_ff[2LL * k], ob1 = d.key_obs_ff[2LL * k + 1];
+    ff e0f = ff_add(u, ff_neg(ff_ld(ob0))), e1f = ff_add(v, ff_neg(ff_ld(ob1)));   // r = f(x) - y
+    if (d.key_wl) {   // whitened residual L^T r
+      const ff l00 = ff_ld(ff_split(__ldg(d.key_wl + 3LL * k)));
+      const ff l10 = ff_ld(ff_split(__ldg(d.key_wl + 3LL * k + 1)));
+      const ff l11 = ff_ld(ff_split(__ldg(d.key_wl + 3LL * k + 2)));
+      const ff w0 = ff_fma(l00, e0f, ff_mul(l10, e1f));
+      e1f = ff_mul(l11, e1f);
+      e0f = w0;
+    }
+    const ff sqf = ff_fma(e0f, e0f, ff_mul(e1f, e1f));
+    const float e0 = e0f.hi + e0f.lo, e1 = e1f.hi + e1f.lo;
+    float sw = 1.0f;
+    const float hd = float(d.huber_delta);
+    if (d.loss == GBA_LOSS_HUBER && sqf.hi > hd * hd) {
+      const float r = sqrtf(sqf.hi);
+      acc = ff_add_f(acc, 2.0f * hd * r - hd * hd);
+      sw = sqrtf(hd / r);
+    } else {
+      acc = ff_add(acc, sqf);
+    }
+    float out[4] = {e0 * sw, e1 * sw, sw, 0.0f};
+    store_vec<4>(rw + 4LL * k, out);
+  }
+  const double tot = block_sum(double(acc.hi) + double(acc.lo), red);
   if (threadIdx.x == 0) d.key_chunk_sum[blockIdx.x] = tot;
 }
 
@@ -847,18 +986,10 @@ __device__ bool warp_potrf_inverse(Tile<T>& D, Tile<T>& Dinv, T* col, T* rinv, i
   return ok;
 }
 
-// Programmatic dependent launch: the Cholesky kernels are launched so that
-// their CTAs may start while the previous kernel drains; griddepcontrol.wait
-// blocks until the previous grid has completed and its writes are visible.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" :::); }
-
 template <typename T>
 __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
   __shared__ Tile<T> A, Li, Lj, D, Dinv;
   __shared__ T yk[kTile], tv[kTile];
-  pdl_wait();
-  pdl_trigger();
   const int p = blockIdx.y;
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p]) return;
@@ -989,8 +1120,6 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_chol_backward(DevPlan d, int k) {
   __shared__ Tile<T> L;
   __shared__ T dk[kTile], yj[kTile];
-  pdl_wait();
-  pdl_trigger();
   const int p = blockIdx.y;
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p]) return;
@@ -1073,9 +1202,11 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       load_vec<12>(tptr<T>(d.PV) + 12LL * pt, pv);
       const double* x = d.x_pt[par] + 3LL * pt;
       double* xn = d.x_pt[1 - par] + 3LL * pt;
+      float2* xf = d.x_ff[1 - par] ? d.x_ff[1 - par] + 3LL * pt : nullptr;
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         xn[a] = x[a] - dp[a];
+        if (xf) xf[a] = ff_split(xn[a]);
         dn2 += dp[a] * dp[a];
         xn2 += x[a] * x[a];
         gd += double(pv[6 + a]) * dp[a];
@@ -1266,29 +1397,14 @@ __global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out) {
   for (int j = 0; j < 12; ++j) ji_out[12LL * k + j] = double(ji[j]);
 }
 
-template <typename Kernel>
-void launch_pdl(Kernel kernel, dim3 grid, dim3 block, cudaStream_t s, const DevPlan& d, int k) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, d, k);
-}
-
 template <typename T>
 int run_cholesky_factor(const DevPlan& d, cudaStream_t s) {
   int n = 0;
-  launch_pdl(k_chol_step<T>, dim3(unsigned(d.max_nt), unsigned(d.B)), dim3(256), s, d, -1);
+  k_chol_step<T><<<dim3(unsigned(d.max_nt), unsigned(d.B)), 256, 0, s>>>(d, -1);
   ++n;
   for (int k = 0; k + 1 < d.max_nt; ++k) {
     const int Tn = d.max_nt - k - 1;
-    launch_pdl(k_chol_step<T>, dim3(unsigned(Tn * (Tn + 1) / 2), unsigned(d.B)), dim3(256), s, d, k);
+    k_chol_step<T><<<dim3(unsigned(Tn * (Tn + 1) / 2), unsigned(d.B)), 256, 0, s>>>(d, k);
     ++n;
   }
   return n;
@@ -1298,7 +1414,7 @@ template <typename T>
 int run_cholesky_solve(const DevPlan& d, cudaStream_t s) {
   int n = 0;
   for (int k = d.max_nt - 1; k >= 1; --k) {
-    launch_pdl(k_chol_backward<T>, dim3(unsigned(k), unsigned(d.B)), dim3(256), s, d, k);
+    k_chol_backward<T><<<dim3(unsigned(k), unsigned(d.B)), 256, 0, s>>>(d, k);
     ++n;
   }
   return n;
@@ -1343,7 +1459,10 @@ int launch_image_prep(const DevPlan& d, int which, cudaStream_t s) {
 
 int launch_cost(const DevPlan& d, int which, cudaStream_t s) {
   if (d.n_key_chunks <= 0) return 0;
-  GBA_DISPATCH(d, (k_cost<T><<<d.n_key_chunks, 256, 0, s>>>(d, which)));
+  if (d.precision == GBA_PRECISION_MIXED)
+    k_cost_ff<<<d.n_key_chunks, 256, 0, s>>>(d, which);
+  else
+    k_cost<double><<<d.n_key_chunks, 256, 0, s>>>(d, which);
   return 1;
 }
 

@@ -439,7 +439,26 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.img_item_partial = arena.alloc<double>(28 * std::max<size_t>(img_items.size(), 1));
   D.cam64 = arena.upload(cam64);
   D.cam32 = arena.upload(cam32);
+  if (mixed) {
+    std::vector<float2> obs_ff(2 * K), cam_ff(10 * std::max<int64_t>(C, 1));
+    auto split = [](double v) {
+      float hi = float(v);
+      return make_float2(hi, float(v - double(hi)));
+    };
+    for (int64_t k = 0; k < K; ++k) {
+      obs_ff[2 * k] = split(key_obs[k].x);
+      obs_ff[2 * k + 1] = split(key_obs[k].y);
+    }
+    for (int64_t c = 0; c < C; ++c) {
+      for (int j = 0; j < 9; ++j) cam_ff[10 * c + j] = split(cam64[10 * c + j]);
+      cam_ff[10 * c + 9] = split(cam64[10 * c + 5] * cam64[10 * c + 9]);   // f * a
+    }
+    D.key_obs_ff = arena.upload(obs_ff);
+    D.cam_ff = arena.upload(cam_ff);
+  }
   for (int t = 0; t < 2; ++t) {
+    D.img_rot_ff[t] = mixed ? arena.alloc<float2>(12 * I) : nullptr;
+    D.x_ff[t] = mixed ? arena.alloc<float2>(3 * P) : nullptr;
     D.x_pt[t] = arena.alloc<double>(3 * P);
     D.x_img[t] = arena.alloc<double>(6 * I);
     D.img_rot[t] = arena.alloc<double>(12 * I);
@@ -494,7 +513,12 @@ void Plan::enqueue(bool profile) {
   size_t ev_i = 0;
   auto mark = [&](int stage) {
     if (!profile) return;
-    GBA_CUDA(cudaEventRecordWithFlags(prof_events[ev_i], s, cudaEventRecordExternal));
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    GBA_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusActive)   // an event-record node in the graph
+      GBA_CUDA(cudaEventRecordWithFlags(prof_events[ev_i], s, cudaEventRecordExternal));
+    else
+      GBA_CUDA(cudaEventRecord(prof_events[ev_i], s));
     prof_stage[ev_i] = stage;
     ++ev_i;
   };
@@ -557,6 +581,7 @@ int Plan::run() {
     if (!graph_exec) prof_stage.assign(prof_events.size(), -2);
   }
   GBA_CUDA(cudaSetDevice(device));
+  cudaGetLastError();   // a stale error from other code on this thread is not ours
   GBA_CUDA(cudaEventRecord(ev0, stream));
   if (opt.use_cuda_graph) {
     if (!graph_exec) {

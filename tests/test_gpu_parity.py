@@ -84,15 +84,22 @@ def test_jacobian_near_zero_rotation(gba):
 
 
 @pytest.mark.parametrize("loss", [abi.LOSS_TRIVIAL, abi.LOSS_HUBER])
-def test_cost(gba, loss):
+@pytest.mark.parametrize("weights", [False, True])
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_cost(gba, loss, weights, precision):
+    """FP64 path: FP64 projection, 1e-12.  Mixed path: double-float
+    projection, whitening and squares (about 48 bits), FP64 block sums: 1e-12
+    for inliers; Huber terms of outliers are formed in FP32 (1e-9)."""
     s = shuffled(distorted_ring())
-    rng = np.random.default_rng(2)
-    A = rng.normal(0, 0.3, size=(s.number_of_keys, 2, 2))
-    s.key_covariance_inverse = np.linalg.inv(np.einsum('kij,klj->kil', A, A) + np.eye(2))
-    opt = abi.make_options(loss=loss, huber_delta=1.0)
+    if weights:
+        rng = np.random.default_rng(2)
+        A = rng.normal(0, 0.3, size=(s.number_of_keys, 2, 2))
+        s.key_covariance_inverse = np.linalg.inv(np.einsum('kij,klj->kil', A, A) + np.eye(2))
+    opt = abi.make_options(loss=loss, huber_delta=1.0, precision=precision)
     c_gpu = gba.cost(s, s.x0, options=opt)
     c_ref = oracle.cost(s, s.x0, s.near_y, loss=loss, huber_delta=1.0)
-    assert abs(c_gpu - c_ref) <= 1e-12 * c_ref
+    tol = 1e-12 if (precision == abi.PRECISION_FP64 or loss == abi.LOSS_TRIVIAL) else 1e-9
+    assert abs(c_gpu - c_ref) <= tol * c_ref, (c_gpu, c_ref)
 
 
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])

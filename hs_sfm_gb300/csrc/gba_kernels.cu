@@ -53,11 +53,17 @@ __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
 // 16-byte aligned address with vector loads.
 template <int N>
 __device__ __forceinline__ void load_vec(const float* __restrict__ p, float* out) {
-  static_assert(N % 4 == 0, "float vectors of 4");
+  static_assert(N % 4 == 0 || N == 2, "float vectors of 4 (or one float2)");
+  if constexpr (N == 2) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    out[0] = v.x;
+    out[1] = v.y;
+  } else {
 #pragma unroll
-  for (int i = 0; i < N / 4; ++i) {
-    float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
-    out[4 * i] = v.x; out[4 * i + 1] = v.y; out[4 * i + 2] = v.z; out[4 * i + 3] = v.w;
+    for (int i = 0; i < N / 4; ++i) {
+      float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
+      out[4 * i] = v.x; out[4 * i + 1] = v.y; out[4 * i + 2] = v.z; out[4 * i + 3] = v.w;
+    }
   }
 }
 template <int N>
@@ -529,83 +535,103 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
 }
 
 // ---------------------------------------------------------------------------
-// linearize: per point (thread), its keys' Jacobians, V_p, g_p
+// linearize, one thread per key (coalesced JR records): the analytical
+// Jacobian of the key, whitened by the key weight and the IRLS weight.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(kPointChunk) k_linearize(DevPlan d) {
+__global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
+  const Chunk ch = d.key_chunks[blockIdx.x];
+  const LMState& st = d.state[ch.prob];
+  if (!st.relin || !st.active) return;
+  const int par = st.parity;
+  const double* __restrict__ xp = d.x_pt[par];
+  const T* __restrict__ IL = tptr<T>(d.img_lin[par]);
+  const T* __restrict__ rwb = tptr<T>(d.RW[par]);
+  T* __restrict__ JR = tptr_mut<T>(d.JR);
+  for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
+    const int img = __ldg(d.key_img + k), pt = __ldg(d.key_pt + k);
+    T X[3];
+    if (sizeof(T) == sizeof(float) && d.x_ff[par]) {   // mixed: high part of the mirror
+      const float2* xf = d.x_ff[par] + 3LL * pt;
+      X[0] = T(xf[0].x); X[1] = T(xf[1].x); X[2] = T(xf[2].x);
+    } else {
+      X[0] = T(xp[3LL * pt]); X[1] = T(xp[3LL * pt + 1]); X[2] = T(xp[3LL * pt + 2]);
+    }
+    T il[12];
+    load_vec<12>(IL + 12LL * img, il);
+    T cam[10];
+    load_cam<T>(d, __ldg(d.img_cam + img), cam);
+    T jp[6], ji[12];
+    key_jacobian<T>(X, il, cam, jp, ji);
+    T rw[4];
+    load_vec<4>(rwb + 4LL * k, rw);
+    const T sw = rw[2];
+    if (d.key_wl) {
+      const T l00 = T(__ldg(d.key_wl + 3LL * k)), l10 = T(__ldg(d.key_wl + 3LL * k + 1)),
+              l11 = T(__ldg(d.key_wl + 3LL * k + 2));
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const T a = jp[m], b = jp[3 + m];
+        jp[m] = (l00 * a + l10 * b) * sw;
+        jp[3 + m] = l11 * b * sw;
+      }
+#pragma unroll
+      for (int m = 0; m < 6; ++m) {
+        const T a = ji[m], b = ji[6 + m];
+        ji[m] = (l00 * a + l10 * b) * sw;
+        ji[6 + m] = l11 * b * sw;
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < 6; ++m) jp[m] *= sw;
+#pragma unroll
+      for (int m = 0; m < 12; ++m) ji[m] *= sw;
+    }
+    T rec[kJRStride];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) rec[m] = jp[m];
+#pragma unroll
+    for (int m = 0; m < 12; ++m) rec[6 + m] = ji[m];
+    rec[18] = rw[0];
+    rec[19] = rw[1];
+    store_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
+  }
+}
+
+// Per point: V_p = sum J_p^T J_p, g_p = sum J_p^T r from its keys' records.
+template <typename T>
+__global__ void __launch_bounds__(kPointChunk) k_point_reduce(DevPlan d) {
   __shared__ double red[32];
   const Chunk ch = d.pt_chunks[blockIdx.x];
   const LMState& st = d.state[ch.prob];
   if (!st.relin || !st.active) return;
-  const int par = st.parity;
   const int pt = ch.begin + threadIdx.x;
   double vmax = 0.0, gmax = 0.0;
   if (pt < ch.end) {
-    const double* xp = d.x_pt[par] + 3LL * pt;
-    const T X[3] = {T(xp[0]), T(xp[1]), T(xp[2])};
-    const T* __restrict__ IL = tptr<T>(d.img_lin[par]);
-    const T* __restrict__ rwb = tptr<T>(d.RW[par]);
-    T* __restrict__ JR = tptr_mut<T>(d.JR);
+    const T* __restrict__ JR = tptr<T>(d.JR);
     T V[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0};
     const int kb = __ldg(d.pt_key_off + pt), ke = __ldg(d.pt_key_off + pt + 1);
     for (int k = kb; k < ke; ++k) {
-      const int img = __ldg(d.key_img + k);
-      T il[12];
-      load_vec<12>(IL + 12LL * img, il);
-      T cam[10];
-      load_cam<T>(d, __ldg(d.img_cam + img), cam);
-      T jp[6], ji[12];
-      key_jacobian<T>(X, il, cam, jp, ji);
-      T rw[4];
-      load_vec<4>(rwb + 4LL * k, rw);
-      const T sw = rw[2];
-      if (d.key_wl) {
-        const T l00 = T(__ldg(d.key_wl + 3LL * k)), l10 = T(__ldg(d.key_wl + 3LL * k + 1)),
-                l11 = T(__ldg(d.key_wl + 3LL * k + 2));
-#pragma unroll
-        for (int m = 0; m < 3; ++m) {
-          T a = jp[m], b = jp[3 + m];
-          jp[m] = (l00 * a + l10 * b) * sw;
-          jp[3 + m] = l11 * b * sw;
-        }
-#pragma unroll
-        for (int m = 0; m < 6; ++m) {
-          T a = ji[m], b = ji[6 + m];
-          ji[m] = (l00 * a + l10 * b) * sw;
-          ji[6 + m] = l11 * b * sw;
-        }
-      } else {
-#pragma unroll
-        for (int m = 0; m < 6; ++m) jp[m] *= sw;
-#pragma unroll
-        for (int m = 0; m < 12; ++m) ji[m] *= sw;
-      }
-      T rec[kJRStride];
-#pragma unroll
-      for (int m = 0; m < 6; ++m) rec[m] = jp[m];
-#pragma unroll
-      for (int m = 0; m < 12; ++m) rec[6 + m] = ji[m];
-      rec[18] = rw[0];
-      rec[19] = rw[1];
-      store_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
-      // V += Jp^T Jp (upper: 00 01 02 11 12 22), g += Jp^T r
+      T jp[8], rr[2];
+      load_vec<8>(JR + (long long)kJRStride * k, jp);
+      load_vec<2>(JR + (long long)kJRStride * k + 18, rr);
       V[0] += jp[0] * jp[0] + jp[3] * jp[3];
       V[1] += jp[0] * jp[1] + jp[3] * jp[4];
       V[2] += jp[0] * jp[2] + jp[3] * jp[5];
       V[3] += jp[1] * jp[1] + jp[4] * jp[4];
       V[4] += jp[1] * jp[2] + jp[4] * jp[5];
       V[5] += jp[2] * jp[2] + jp[5] * jp[5];
-      g[0] += jp[0] * rw[0] + jp[3] * rw[1];
-      g[1] += jp[1] * rw[0] + jp[4] * rw[1];
-      g[2] += jp[2] * rw[0] + jp[5] * rw[1];
+      g[0] += jp[0] * rr[0] + jp[3] * rr[1];
+      g[1] += jp[1] * rr[0] + jp[4] * rr[1];
+      g[2] += jp[2] * rr[0] + jp[5] * rr[1];
     }
     T pv[12] = {V[0], V[1], V[2], V[3], V[4], V[5], g[0], g[1], g[2], T(0), T(0), T(0)};
     store_vec<12>(tptr_mut<T>(d.PV) + 12LL * pt, pv);
     vmax = fmax(fmax(double(V[0]), double(V[3])), double(V[5]));
     gmax = fmax(fmax(fabs(double(g[0])), fabs(double(g[1]))), fabs(double(g[2])));
   }
-  double bv = block_max(vmax, red);
-  double bg = block_max(gmax, red);
+  const double bv = block_max(vmax, red);
+  const double bg = block_max(gmax, red);
   if (threadIdx.x == 0) {
     LMState* sp = d.state + ch.prob;
     atomicMax(&sp->maxdiag_bits, dbits(bv));
@@ -701,10 +727,10 @@ __global__ void __launch_bounds__(256) k_image_finalize(DevPlan d) {
 }
 
 // ---------------------------------------------------------------------------
-// point Schur: C C^T = V + mu I, Z = C^-1 J_p^T J_i per key, h = C^-1 g
+// point factor: C C^T = V_p + mu I, C^-1 and h_p = C^-1 g_p per point
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(kPointChunk) k_point_schur(DevPlan d) {
+__global__ void __launch_bounds__(kPointChunk) k_point_factor(DevPlan d) {
   const Chunk ch = d.pt_chunks[blockIdx.x];
   const LMState& st = d.state[ch.prob];
   if (!st.active) return;
@@ -713,21 +739,20 @@ __global__ void __launch_bounds__(kPointChunk) k_point_schur(DevPlan d) {
   const T mu = T(st.mu);
   T pv[12];
   load_vec<12>(tptr<T>(d.PV) + 12LL * pt, pv);
-  // Cholesky of the damped 3x3 block (upper-stored V: 00 01 02 11 12 22)
-  T a00 = pv[0] + mu, a01 = pv[1], a02 = pv[2], a11 = pv[3] + mu, a12 = pv[4], a22 = pv[5] + mu;
+  const T a00 = pv[0] + mu, a01 = pv[1], a02 = pv[2], a11 = pv[3] + mu, a12 = pv[4], a22 = pv[5] + mu;
   bool ok = a00 > T(0);
-  T c00 = sqrt(a00);
-  T i00 = T(1) / c00;
-  T c10 = a01 * i00, c20 = a02 * i00;
-  T s11 = a11 - c10 * c10;
+  const T c00 = sqrt(a00);
+  const T i00 = T(1) / c00;
+  const T c10 = a01 * i00, c20 = a02 * i00;
+  const T s11 = a11 - c10 * c10;
   ok = ok && s11 > T(0);
-  T c11 = sqrt(s11);
-  T i11 = T(1) / c11;
-  T c21 = (a12 - c20 * c10) * i11;
-  T s22 = a22 - c20 * c20 - c21 * c21;
+  const T c11 = sqrt(s11);
+  const T i11 = T(1) / c11;
+  const T c21 = (a12 - c20 * c10) * i11;
+  const T s22 = a22 - c20 * c20 - c21 * c21;
   ok = ok && s22 > T(0);
-  T c22 = sqrt(s22);
-  T i22 = T(1) / c22;
+  const T c22 = sqrt(s22);
+  const T i22 = T(1) / c22;
   if (!ok) {
     atomicExch(d.factor_flag + ch.prob, 1);
     return;
@@ -740,21 +765,30 @@ __global__ void __launch_bounds__(kPointChunk) k_point_schur(DevPlan d) {
   T ps[12] = {i00, m10, i11, m20, m21, i22,
               i00 * g0, m10 * g0 + i11 * g1, m20 * g0 + m21 * g1 + i22 * g2, T(0), T(0), T(0)};
   store_vec<12>(tptr_mut<T>(d.PS) + 12LL * pt, ps);
+}
+
+// Z_a = C_p^-1 J_p^T J_i per key (coalesced records).
+template <typename T>
+__global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
+  const Chunk ch = d.key_chunks[blockIdx.x];
+  const LMState& st = d.state[ch.prob];
+  if (!st.active) return;
   const T* __restrict__ JR = tptr<T>(d.JR);
+  const T* __restrict__ PS = tptr<T>(d.PS);
   T* __restrict__ Z = tptr_mut<T>(d.Z);
-  const int kb = __ldg(d.pt_key_off + pt), ke = __ldg(d.pt_key_off + pt + 1);
-  for (int k = kb; k < ke; ++k) {
-    T rec[kJRStride];
+  for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
+    T rec[kJRStride], ps[8];
     load_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
+    load_vec<8>(PS + 12LL * __ldg(d.key_pt + k), ps);
+    const T i00 = ps[0], m10 = ps[1], i11 = ps[2], m20 = ps[3], m21 = ps[4], i22 = ps[5];
     const T* jp = rec;
     const T* ji = rec + 6;
     T z[kZStride];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-      // W[m][c] = jp[m] ji[c] + jp[3+m] ji[6+c]
-      T w0 = jp[0] * ji[c] + jp[3] * ji[6 + c];
-      T w1 = jp[1] * ji[c] + jp[4] * ji[6 + c];
-      T w2 = jp[2] * ji[c] + jp[5] * ji[6 + c];
+      const T w0 = jp[0] * ji[c] + jp[3] * ji[6 + c];
+      const T w1 = jp[1] * ji[c] + jp[4] * ji[6 + c];
+      const T w2 = jp[2] * ji[c] + jp[5] * ji[6 + c];
       z[c] = i00 * w0;
       z[6 + c] = m10 * w0 + i11 * w1;
       z[12 + c] = m20 * w0 + m21 * w1 + i22 * w2;
@@ -784,8 +818,13 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
   for (int e = 0; e < 36; ++e) acc[e] = T(0);
 #pragma unroll
   for (int e = 0; e < 6; ++e) racc[e] = T(0);
-  for (int q = it.y + lane; q < it.z; q += 32) {
-    const int2 pr = __ldg(d.pairs + q);
+  // the next pair's key indices are fetched one iteration ahead, so each
+  // iteration waits on a single round trip (the Z records)
+  int q = it.y + lane;
+  int2 pr = q < it.z ? __ldg(d.pairs + q) : make_int2(0, 0);
+  for (; q < it.z; q += 32) {
+    const int qn = q + 32;
+    const int2 prn = qn < it.z ? __ldg(d.pairs + qn) : pr;
     T za[kZStride], zb[kZStride];
     load_vec<kZStride>(Z + (long long)kZStride * pr.x, za);
     if (diag) {
@@ -804,19 +843,26 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
       for (int c = 0; c < 6; ++c)
         acc[6 * r + c] += za[r] * zb[c] + za[6 + r] * zb[6 + c] + za[12 + r] * zb[12 + c];
     }
+    pr = prn;
   }
-  // warp reduction in the working precision; FP64 only for the stored sums
+  // warp reduction in the working precision; each lane then converts only
+  // the sums it stores (entries lane and lane + 32 of the 42)
   double* out = d.item_partial + (long long)kItemStride * wid;
+  T mine0 = T(0), mine1 = T(0);
 #pragma unroll
   for (int e = 0; e < 36; ++e) {
     const T v = warp_sum_t(acc[e]);
-    if (lane == (e & 31)) out[e] = double(v);
+    if (lane == e) mine0 = v;
+    if (lane + 32 == e) mine1 = v;
   }
 #pragma unroll
   for (int e = 0; e < 6; ++e) {
     const T v = warp_sum_t(racc[e]);
-    if (lane == ((36 + e) & 31)) out[36 + e] = double(v);
+    if (lane == 36 + e) mine0 = v;
+    if (lane + 32 == 36 + e) mine1 = v;
   }
+  out[lane] = double(mine0);
+  if (lane < 10) out[32 + lane] = double(mine1);
 }
 
 // Dense reduced system (lower triangle) and rhs in precision T; the block
@@ -1472,9 +1518,16 @@ int launch_ctrl_initial_cost(const DevPlan& d, cudaStream_t s) {
 }
 
 int launch_linearize(const DevPlan& d, cudaStream_t s) {
-  if (d.n_pt_chunks <= 0) return 0;
-  GBA_DISPATCH(d, (k_linearize<T><<<d.n_pt_chunks, kPointChunk, 0, s>>>(d)));
-  return 1;
+  int n = 0;
+  if (d.n_key_chunks > 0) {
+    GBA_DISPATCH(d, (k_linearize_keys<T><<<d.n_key_chunks, 256, 0, s>>>(d)));
+    ++n;
+  }
+  if (d.n_pt_chunks > 0) {
+    GBA_DISPATCH(d, (k_point_reduce<T><<<d.n_pt_chunks, kPointChunk, 0, s>>>(d)));
+    ++n;
+  }
+  return n;
 }
 
 int launch_image_reduce(const DevPlan& d, cudaStream_t s) {
@@ -1490,9 +1543,16 @@ int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s) {
 }
 
 int launch_point_schur(const DevPlan& d, cudaStream_t s) {
-  if (d.n_pt_chunks <= 0) return 0;
-  GBA_DISPATCH(d, (k_point_schur<T><<<d.n_pt_chunks, kPointChunk, 0, s>>>(d)));
-  return 1;
+  int n = 0;
+  if (d.n_pt_chunks > 0) {
+    GBA_DISPATCH(d, (k_point_factor<T><<<d.n_pt_chunks, kPointChunk, 0, s>>>(d)));
+    ++n;
+  }
+  if (d.n_key_chunks > 0) {
+    GBA_DISPATCH(d, (k_key_z<T><<<d.n_key_chunks, 256, 0, s>>>(d)));
+    ++n;
+  }
+  return n;
 }
 
 int launch_assemble_items(const DevPlan& d, cudaStream_t s) {

@@ -52,7 +52,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--points", type=int, default=100_000)
     ap.add_argument("--images", type=int, default=200)
-    ap.add_argument("--workload", default="grid", choices=["grid", "windows"])
+    ap.add_argument("--workload", default="grid", choices=["grid", "windows", "serving"])
+    ap.add_argument("--rates", default="50,200,800,2000",
+                    help="serving: Poisson arrival rates swept (req/s)")
+    ap.add_argument("--duration", type=float, default=10.0, help="serving: seconds per rate")
+    ap.add_argument("--pool", type=int, default=256, help="serving: distinct request scenes")
+    ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--max-in-flight", type=int, default=4)
     ap.add_argument("--windows", type=int, default=512)
     ap.add_argument("--per-problem-sample", type=int, default=512,
                     help="windows solved one by one on the FP64 path (all by default)")
@@ -447,6 +453,134 @@ def run_windows(args, ws, rank, local):
     return 0
 
 
+SERVE_ITERS = 10
+SERVE_WORKLOAD = ("Poisson stream of BA requests, log-normal sizes (median 20 cameras / 5k points, "
+                  "capped 300 / 200k), ring geometry with 5 keys per point, 10 LM iterations each")
+
+
+def _mg1(arrivals, service):
+    """FIFO single-server latencies of the one-request-at-a-time path for
+    the same arrivals, from each request's measured solve time."""
+    free, lat = 0.0, []
+    for a, s in zip(arrivals, service):
+        start = max(a, free)
+        free = start + s
+        lat.append(free - a)
+    return np.array(lat)
+
+
+def run_serving(args, ws, rank, local):
+    """Continuous batching (gba_server) under Poisson arrivals, one rate at a
+    time; beside it the one-request-at-a-time FP64 path (gba_solve) on the
+    same arrival sequence, its latencies computed from measured solve times."""
+    import ctypes as C
+    import torch
+    from hs_sfm_gb300 import abi, gba, synthetic
+    torch.cuda.set_device(local)
+    L = gba.lib()
+    I, P = synthetic.request_sizes(args.pool, seed=4 + 1000 * rank)
+    pool = [synthetic.ring_scene(num_images=int(i), num_points=int(p), obs_per_point=5,
+                                 seed=100_000 * (rank + 1) + j, name=f"request{j}")
+            for j, (i, p) in enumerate(zip(I, P))]
+    cps = [abi.CProblem(s) for s in pool]
+    ys = [np.ascontiguousarray(s.near_y, dtype=np.float64) for s in pool]
+    x0s = [np.ascontiguousarray(s.x0, dtype=np.float64) for s in pool]
+    # reference quality and service times of the per-problem FP64 path
+    opt64 = abi.make_options(max_iterations=SERVE_ITERS, eps1=0.0, eps2=0.0,
+                             precision=abi.PRECISION_FP64, device=local)
+    for s in pool[:4]:
+        gba.solve(s, opt64)
+    service, cost64 = [], []
+    for s in pool:
+        t0 = time.perf_counter()
+        _, r = gba.solve(s, opt64)
+        service.append(time.perf_counter() - t0)
+        cost64.append(r.final_cost)
+    service, cost64 = np.array(service), np.array(cost64)
+    cfg = gba.default_server_config(max_iterations=SERVE_ITERS, eps1=0.0, eps2=0.0,
+                                    precision=abi.PRECISION_MIXED, device=local)
+    cfg.max_batch, cfg.max_in_flight = args.max_batch, args.max_in_flight
+    rates = [float(r) for r in args.rates.split(",") if r]
+    sweep, worst_rel, launches = [], 0.0, 0
+    clocks = ClockSampler(local)
+    clocks.start()
+    for rate in rates:
+        rng = np.random.default_rng(int(rate) + 7 * rank)
+        n = max(1, int(rng.poisson(rate * args.duration)))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+        which = rng.integers(0, len(pool), n)
+        srv = gba.Server(cfg)
+        k0 = gba.kernel_launch_count()
+        tickets = [0] * n
+        t_start = time.perf_counter()
+
+        def submitter():
+            t = C.c_int64()
+            for q in range(n):
+                delay = t_start + arrivals[q] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                j = int(which[q])
+                st = L.gba_server_submit(srv.h, cps[j].ref, abi.dptr(ys[j]), abi.dptr(x0s[j]),
+                                         C.byref(t))
+                tickets[q] = t.value if st == abi.GBA_OK else -st
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        lat, qms, done_at, costs = [], [], [], {}
+        out = {j: np.zeros(cps[j].x_size) for j in range(len(pool))}
+        for q in range(n):
+            while tickets[q] == 0:
+                time.sleep(0.0005)
+            if tickets[q] < 0:
+                raise gba.GbaError(-tickets[q], "gba_server_submit")
+            j = int(which[q])
+            rep = abi.Report()
+            st = L.gba_server_wait(srv.h, tickets[q], -1.0, abi.dptr(out[j]), C.byref(rep))
+            if st != abi.GBA_OK:
+                raise gba.GbaError(st, "gba_server_wait")
+            lat.append(rep.latency_ms)
+            qms.append(rep.queue_ms)
+            done_at.append(arrivals[q] + rep.latency_ms / 1e3)
+            costs[j] = rep.final_cost
+        th.join()
+        st = srv.stats()
+        srv.close()
+        launches += gba.kernel_launch_count() - k0
+        wall = max(done_at) - arrivals[0]
+        rel = max(abs(costs[j] - cost64[j]) / cost64[j] for j in costs)
+        worst_rel = max(worst_rel, rel)
+        base = _mg1(arrivals, service[which]) * 1e3
+        sweep.append({
+            "rate": rate, "requests": n, "solves_per_s": n / wall,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "queue_p50_ms": float(np.percentile(qms, 50)),
+            "batches": st["batches_launched"], "mean_batch": n / max(1, st["batches_launched"]),
+            "per_problem_fp64": {"solves_per_s": n / max(base[-1] / 1e3 + arrivals[-1] - arrivals[0],
+                                                         1e-9),
+                                 "p50_ms": float(np.percentile(base, 50)),
+                                 "p99_ms": float(np.percentile(base, 99))},
+            "final_cost_max_rel_diff_vs_fp64": float(rel)})
+    clk = clocks.stop()
+    top = max(sweep, key=lambda r: r["solves_per_s"])
+    line = {
+        "metric": "served BA solves/s", "value": top["solves_per_s"], "unit": "solves/s",
+        "n_gpus": ws, "steps": len(rates), "warmup": 0,
+        "ms_per_step": 1e3 * args.duration, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded ring requests)",
+        "config": {"workload": SERVE_WORKLOAD, "pool": len(pool), "duration_s": args.duration,
+                   "max_batch": args.max_batch, "max_in_flight": args.max_in_flight,
+                   "iterations_per_solve": SERVE_ITERS},
+        "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep,
+        "final_cost_max_rel_diff_vs_fp64": worst_rel,
+        "e2e": {"value": top["solves_per_s"], "unit": "solves/s",
+                "note": "host buffers through gba_server_submit/wait"},
+        "gpu_launches": int(launches), "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -454,6 +588,8 @@ def main():
         return run_reference(args, ws, rank)
     if args.workload == "windows":
         return run_windows(args, ws, rank, local)
+    if args.workload == "serving":
+        return run_serving(args, ws, rank, local)
     return run_gba(args, ws, rank, local)
 
 

@@ -104,6 +104,7 @@ class Report(C.Structure):
         ("setup_ms", C.c_double), ("solve_ms", C.c_double),
         ("stage_ms", C.c_double * NUM_STAGES),
         ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+        ("queue_ms", C.c_double), ("latency_ms", C.c_double),
     ]
 
     def as_dict(self):
@@ -111,6 +112,20 @@ class Report(C.Structure):
              if name not in ("pad_", "stage_ms")}
         d["stage_ms"] = list(self.stage_ms)
         return d
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("solve", Options), ("memory_budget_bytes", C.c_int64), ("max_batch", C.c_int32),
+                ("max_in_flight", C.c_int32), ("reserved_", C.c_int32 * 6)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "submitted", "completed", "cancelled", "refused", "queued", "in_flight_requests",
+        "in_flight_batches", "batches_launched", "admitted_bytes", "budget_bytes")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PRECISION_FP64,

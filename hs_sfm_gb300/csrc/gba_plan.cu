@@ -68,15 +68,19 @@ void expand_camera(uint32_t mask, const double* c, double out[10]) {
 }
 
 // Device buffer registry.
+// Device buffer registry.  Allocations are stream-ordered on the plan's
+// stream (cudaMallocAsync / cudaFreeAsync from the device's default pool), so
+// creating or destroying a plan never synchronizes other plans' streams.
 struct DeviceArena {
   std::vector<void*> ptrs;
+  cudaStream_t stream = nullptr;
   size_t bytes = 0;
   long long uploaded = 0;
   template <typename T>
   T* alloc(size_t count) {
     if (count == 0) count = 1;
     void* p = nullptr;
-    GBA_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    GBA_CUDA(cudaMallocAsync(&p, count * sizeof(T), stream));
     ptrs.push_back(p);
     bytes += count * sizeof(T);
     return static_cast<T*>(p);
@@ -84,12 +88,13 @@ struct DeviceArena {
   template <typename T>
   T* upload(const std::vector<T>& h) {
     T* p = alloc<T>(h.size());
-    if (!h.empty()) GBA_CUDA(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    if (!h.empty())
+      GBA_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
     uploaded += (long long)(h.size() * sizeof(T));
     return p;
   }
   void release() {
-    for (void* p : ptrs) cudaFree(p);
+    for (void* p : ptrs) cudaFreeAsync(p, stream);
     ptrs.clear();
   }
 };
@@ -183,6 +188,16 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   device = opt.device;
   GBA_CUDA(cudaSetDevice(device));
   GBA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  arena.stream = stream;
+  {
+    // keep freed plan memory in the pool instead of returning it each time
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   GBA_CUDA(cudaEventCreate(&ev0));
   GBA_CUDA(cudaEventCreate(&ev1));
   const bool mixed = opt.precision == GBA_PRECISION_MIXED;
@@ -499,8 +514,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.pt_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(pt_chunks.size(), 1));
   D.img_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(img_chunks.size(), 1));
   D.launch_counter = nullptr;
-  GBA_CUDA(cudaMemset(D.state, 0, sizeof(LMState) * nprob));
-  GBA_CUDA(cudaDeviceSynchronize());
+  GBA_CUDA(cudaMemsetAsync(D.state, 0, sizeof(LMState) * nprob, stream));
+  GBA_CUDA(cudaStreamSynchronize(stream));
   setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return GBA_OK;
 }
@@ -780,11 +795,12 @@ int gba_plan_set_initial_x(gba_plan* p, int32_t q, const double* x0) {
   return guarded([&] {
     gba::Plan& P = p->impl;
     const gba::ProbInfo& pi = P.prob[q];
-    GBA_CUDA(cudaMemcpy(const_cast<double*>(P.d.x0_pt) + 3LL * pi.point_begin, x0,
-                        sizeof(double) * 3 * pi.num_points, cudaMemcpyHostToDevice));
-    GBA_CUDA(cudaMemcpy(const_cast<double*>(P.d.x0_img) + 6LL * pi.image_begin,
-                        x0 + 3LL * pi.num_points, sizeof(double) * 6 * pi.num_images,
-                        cudaMemcpyHostToDevice));
+    GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_pt) + 3LL * pi.point_begin, x0,
+                             sizeof(double) * 3 * pi.num_points, cudaMemcpyHostToDevice, P.stream));
+    GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_img) + 6LL * pi.image_begin,
+                             x0 + 3LL * pi.num_points, sizeof(double) * 6 * pi.num_images,
+                             cudaMemcpyHostToDevice, P.stream));
+    GBA_CUDA(cudaStreamSynchronize(P.stream));
     P.h2d_bytes += (long long)sizeof(double) * (3LL * pi.num_points + 6LL * pi.num_images);
     return GBA_OK;
   });
@@ -805,15 +821,17 @@ int gba_plan_get_x(gba_plan* p, int32_t q, double* x) {
   return guarded([&] {
     gba::Plan& P = p->impl;
     gba::LMState st;
+    GBA_CUDA(cudaStreamSynchronize(P.stream));
     GBA_CUDA(cudaMemcpy(&st, P.d.state + q, sizeof(st), cudaMemcpyDeviceToHost));
     const gba::ProbInfo& pi = P.prob[q];
     const int par = P.ran ? st.parity : 0;
     const double* xp = P.ran ? P.d.x_pt[par] : P.d.x0_pt;
     const double* xi = P.ran ? P.d.x_img[par] : P.d.x0_img;
-    GBA_CUDA(cudaMemcpy(x, xp + 3LL * pi.point_begin, sizeof(double) * 3 * pi.num_points,
-                        cudaMemcpyDeviceToHost));
-    GBA_CUDA(cudaMemcpy(x + 3LL * pi.num_points, xi + 6LL * pi.image_begin,
-                        sizeof(double) * 6 * pi.num_images, cudaMemcpyDeviceToHost));
+    GBA_CUDA(cudaMemcpyAsync(x, xp + 3LL * pi.point_begin, sizeof(double) * 3 * pi.num_points,
+                             cudaMemcpyDeviceToHost, P.stream));
+    GBA_CUDA(cudaMemcpyAsync(x + 3LL * pi.num_points, xi + 6LL * pi.image_begin,
+                             sizeof(double) * 6 * pi.num_images, cudaMemcpyDeviceToHost, P.stream));
+    GBA_CUDA(cudaStreamSynchronize(P.stream));
     P.d2h_bytes += (long long)sizeof(st) +
                    (long long)sizeof(double) * (3LL * pi.num_points + 6LL * pi.num_images);
     return GBA_OK;
@@ -825,6 +843,7 @@ int gba_plan_get_report(gba_plan* p, int32_t q, gba_report* r) {
   return guarded([&] {
     gba::Plan& P = p->impl;
     gba::LMState st;
+    GBA_CUDA(cudaStreamSynchronize(P.stream));
     GBA_CUDA(cudaMemcpy(&st, P.d.state + q, sizeof(st), cudaMemcpyDeviceToHost));
     std::memset(r, 0, sizeof(*r));
     r->status = st.status;
@@ -852,6 +871,19 @@ int gba_plan_get_report(gba_plan* p, int32_t q, gba_report* r) {
   });
 }
 
+int gba_plan_query(gba_plan* p) {
+  if (!p) return GBA_ERR_INVALID;
+  if (!p->impl.ran) return GBA_OK;
+  cudaError_t e = cudaEventQuery(p->impl.ev1);
+  if (e == cudaSuccess) return GBA_OK;
+  if (e == cudaErrorNotReady) {
+    cudaGetLastError();
+    return GBA_ERR_BUSY;
+  }
+  cudaGetLastError();
+  return GBA_ERR_CUDA;
+}
+
 int gba_plan_last_run_ms(gba_plan* p, double* ms) {
   if (!p || !ms) return GBA_ERR_INVALID;
   return guarded([&] {
@@ -872,6 +904,12 @@ int gba_plan_kernel_stats(gba_plan* p, int32_t stage, double* total_ms, int32_t*
 int gba_plan_last_run_launches(gba_plan* p, int64_t* n) {
   if (!p || !n) return GBA_ERR_INVALID;
   *n = p->impl.launches_last_run;
+  return GBA_OK;
+}
+
+int gba_plan_device_bytes(gba_plan* p, int64_t* bytes) {
+  if (!p || !bytes) return GBA_ERR_INVALID;
+  *bytes = int64_t(p->impl.arena.bytes);
   return GBA_OK;
 }
 

@@ -65,6 +65,20 @@ def lib():
     L.gba_jacobian.argtypes = [P, d, d, d, d, C.c_int32]
     L.gba_cost.argtypes = [P, d, d, O, d]
     L.gba_schur_step.argtypes = [P, d, d, C.c_double, O, d]
+    L.gba_plan_query.argtypes = [vp]
+    L.gba_plan_device_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
+    SC = C.POINTER(abi.ServerConfig)
+    L.gba_default_server_config.argtypes = [SC]
+    L.gba_default_server_config.restype = None
+    L.gba_server_create.argtypes = [SC, C.POINTER(vp)]
+    L.gba_server_destroy.argtypes = [vp]
+    L.gba_server_submit.argtypes = [vp, P, d, d, C.POINTER(C.c_int64)]
+    L.gba_server_poll.argtypes = [vp, C.c_int64, d, R]
+    L.gba_server_wait.argtypes = [vp, C.c_int64, C.c_double, d, R]
+    L.gba_server_cancel.argtypes = [vp, C.c_int64]
+    L.gba_server_get_stats.argtypes = [vp, C.POINTER(abi.ServerStats)]
+    L.gba_estimate_device_bytes.restype = C.c_int64
+    L.gba_estimate_device_bytes.argtypes = [P, C.c_int32]
     _lib = L
     return L
 
@@ -162,10 +176,106 @@ class Plan:
         _check(lib().gba_plan_last_run_launches(self.h, C.byref(v)), "launches")
         return v.value
 
+    def query(self):
+        """True when the last run has finished on the device (non-blocking)."""
+        st = lib().gba_plan_query(self.h)
+        if st == abi.GBA_ERR_BUSY:
+            return False
+        _check(st, "gba_plan_query")
+        return True
+
+    def device_bytes(self):
+        v = C.c_int64()
+        _check(lib().gba_plan_device_bytes(self.h, C.byref(v)), "device_bytes")
+        return v.value
+
     def close(self):
         if getattr(self, "h", None):
             lib().gba_plan_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def estimate_device_bytes(scene, precision=abi.PRECISION_FP64):
+    cp = abi.CProblem(scene)
+    return int(lib().gba_estimate_device_bytes(cp.ref, precision))
+
+
+def default_server_config(**solve_options):
+    cfg = abi.ServerConfig()
+    lib().gba_default_server_config(C.byref(cfg))
+    if solve_options:
+        cfg.solve = abi.make_options(**solve_options)
+    return cfg
+
+
+class Server:
+    """Continuous-batching request loop (gba_server_*).
+
+    submit() copies the request and returns a ticket; poll() / wait() return
+    (x, report) once it is solved, or None while it is queued or running."""
+
+    def __init__(self, config=None, **fields):
+        self.config = config if config is not None else default_server_config()
+        for k, v in fields.items():
+            setattr(self.config, k, v)
+        h = C.c_void_p()
+        _check(lib().gba_server_create(C.byref(self.config), C.byref(h)), "gba_server_create")
+        self.h = h
+        self._sizes = {}
+
+    def submit(self, scene, x0=None, near_y=None):
+        cp = abi.CProblem(scene)
+        y = _f64(scene.near_y if near_y is None else near_y)
+        x0 = _f64(scene.x0 if x0 is None else x0)
+        t = C.c_int64()
+        _check(lib().gba_server_submit(self.h, cp.ref, abi.dptr(y), abi.dptr(x0), C.byref(t)),
+               "gba_server_submit")
+        self._sizes[t.value] = cp.x_size
+        return t.value
+
+    def _result(self, st, ticket, out, rep):
+        if st == abi.GBA_ERR_BUSY:
+            return None
+        self._sizes.pop(ticket, None)
+        _check(st, "gba_server result")
+        return out, rep
+
+    def poll(self, ticket):
+        out = np.zeros(self._sizes.get(ticket, 0))
+        rep = abi.Report()
+        st = lib().gba_server_poll(self.h, ticket, abi.dptr(out), C.byref(rep))
+        return self._result(st, ticket, out, rep)
+
+    def wait(self, ticket, timeout_ms=-1.0):
+        out = np.zeros(self._sizes.get(ticket, 0))
+        rep = abi.Report()
+        st = lib().gba_server_wait(self.h, ticket, float(timeout_ms), abi.dptr(out), C.byref(rep))
+        return self._result(st, ticket, out, rep)
+
+    def cancel(self, ticket):
+        _check(lib().gba_server_cancel(self.h, ticket), "gba_server_cancel")
+
+    def stats(self):
+        s = abi.ServerStats()
+        _check(lib().gba_server_get_stats(self.h, C.byref(s)), "gba_server_get_stats")
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gba_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:

@@ -206,6 +206,8 @@ typedef struct gba_report {
   double stage_ms[GBA_NUM_STAGES];  /* with options.profile                 */
   int64_t h2d_bytes;          /* host->device bytes copied for this solve   */
   int64_t d2h_bytes;          /* device->host bytes copied for this solve   */
+  double queue_ms;            /* server: submit -> admitted                 */
+  double latency_ms;          /* server: submit -> result ready             */
 } gba_report;
 
 /* ---- one-shot solve: the drop-in for
@@ -232,6 +234,9 @@ GBA_API int gba_plan_set_initial_x(gba_plan* plan, int32_t problem, const double
 GBA_API int gba_plan_run(gba_plan* plan);
 /* Waits for the plan's stream; returns the first device status seen. */
 GBA_API int gba_plan_synchronize(gba_plan* plan);
+/* Non-blocking: GBA_OK when the last gba_plan_run has finished on the
+ * device, GBA_ERR_BUSY while it is still running. */
+GBA_API int gba_plan_query(gba_plan* plan);
 GBA_API int gba_plan_get_x(gba_plan* plan, int32_t problem, double* x_out);
 GBA_API int gba_plan_get_report(gba_plan* plan, int32_t problem, gba_report* report);
 /* Device time of the last gba_plan_run in milliseconds (CUDA events on the
@@ -242,6 +247,8 @@ GBA_API int gba_plan_kernel_stats(gba_plan* plan, int32_t stage, double* total_m
                           int32_t* launches);
 /* Counts of this library's kernel launches in the last run. */
 GBA_API int gba_plan_last_run_launches(gba_plan* plan, int64_t* launches);
+/* Device bytes the plan holds (every buffer of its arena). */
+GBA_API int gba_plan_device_bytes(gba_plan* plan, int64_t* bytes);
 
 /* ---- batched one-shot solve (independent problems, one plan) ----------- */
 GBA_API int gba_solve_batch(const gba_problem* problems, const double* const* near_ys,
@@ -277,6 +284,56 @@ GBA_API int gba_cost(const gba_problem* problem, const double* x,
 GBA_API int gba_schur_step(const gba_problem* problem, const double* x,
                    const double* near_y, double mu,
                    const gba_options* options, double* delta_x);
+
+/* ---- serving: continuous batching of independent solves ---------------
+ * A server owns a worker thread.  Submitted requests (deep-copied) wait in a
+ * FIFO queue; whenever device memory (the budget) and in-flight slots allow,
+ * the worker admits the queued requests that fit, packs them into one plan
+ * (a micro-batch) on its own CUDA stream and launches it while earlier
+ * micro-batches are still running, so requests that arrive while others are
+ * on the GPU overlap with them.  Finished micro-batches are harvested without
+ * blocking the device; their memory returns to the budget.  A request's
+ * result does not depend on what it was batched with (every reduction has a
+ * fixed order).  Requests larger than the whole budget are refused at submit
+ * (GBA_ERR_BUSY). */
+typedef struct gba_server gba_server;
+
+typedef struct gba_server_config {
+  gba_options solve;              /* options of every request's solve        */
+  int64_t memory_budget_bytes;    /* 0: 80% of the free device memory        */
+  int32_t max_batch;              /* requests packed into one micro-batch    */
+  int32_t max_in_flight;          /* micro-batches running concurrently      */
+  int32_t reserved_[6];
+} gba_server_config;
+
+typedef struct gba_server_stats {
+  int64_t submitted, completed, cancelled, refused;
+  int64_t queued, in_flight_requests, in_flight_batches, batches_launched;
+  int64_t admitted_bytes, budget_bytes;
+} gba_server_stats;
+
+GBA_API void gba_default_server_config(gba_server_config* config);
+GBA_API int gba_server_create(const gba_server_config* config, gba_server** server);
+GBA_API int gba_server_destroy(gba_server* server);
+/* Copies the problem, near_y [y_size] and x0 [x_size]; returns a ticket. */
+GBA_API int gba_server_submit(gba_server* server, const gba_problem* problem,
+                              const double* near_y, const double* x0, int64_t* ticket);
+/* Non-blocking.  GBA_OK: the result is ready -- x_out [x_size] and report
+ * are filled and the ticket is released; GBA_ERR_BUSY: still queued or
+ * running; GBA_ERR_INVALID: unknown ticket; other codes: the solve failed
+ * (the ticket is released). */
+GBA_API int gba_server_poll(gba_server* server, int64_t ticket, double* x_out,
+                            gba_report* report);
+/* As poll, waiting up to timeout_ms (negative: without limit). */
+GBA_API int gba_server_wait(gba_server* server, int64_t ticket, double timeout_ms,
+                            double* x_out, gba_report* report);
+/* A queued request is dropped; a running one finishes but its result is
+ * discarded.  Later polls return GBA_ERR_CANCELLED. */
+GBA_API int gba_server_cancel(gba_server* server, int64_t ticket);
+GBA_API int gba_server_get_stats(gba_server* server, gba_server_stats* stats);
+/* Device bytes a plan for this problem would hold (host-side estimate used
+ * for admission). */
+GBA_API int64_t gba_estimate_device_bytes(const gba_problem* problem, int32_t precision);
 
 /* ---- allocation-free cost ------------------------------------------------
  * No counterpart in the reference: an entry point for callers that must not

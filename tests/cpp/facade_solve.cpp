@@ -1,0 +1,62 @@
+// Drives the header-only facade (include/gba/camera_shared.hpp) the way the
+// reference's callers drive CameraSharedLevenbergMarquardtOptimizor
+// (test_camera_shared_relative_pair.cpp:976-984): build the vector function,
+// the inverse covariance and the optimizer, call it, read x back.
+//
+// usage: facade_solve <problem.bin> <x_out.bin> [--bad-size]
+// problem.bin: int64 P I C K mask iters; int64 feature_maps[2K];
+//              int64 image_camera_map[I]; double cameras[cC];
+//              double near_y[2K]; double x0[3P + 6I]
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "gba/camera_shared.hpp"
+
+int main(int argc, char** argv) {
+  if (argc < 3) return 2;
+  FILE* f = std::fopen(argv[1], "rb");
+  if (!f) return 2;
+  int64_t hdr[6];
+  if (std::fread(hdr, sizeof(int64_t), 6, f) != 6) return 2;
+  const int64_t P = hdr[0], I = hdr[1], C = hdr[2], K = hdr[3], mask = hdr[4], iters = hdr[5];
+  typedef gba::CameraSharedVectorFunction<double> VF;
+  VF vf;
+  vf.set_number_of_points(P);
+  vf.set_number_of_images(I);
+  vf.set_number_of_cameras(C);
+  vf.set_number_of_keys(K);
+  vf.intrinsic_computations_mask() = gba::IntrinsicComputationsMask((unsigned long)mask);
+  VF::FeatureMapContainer fm(static_cast<size_t>(K));
+  std::vector<int64_t> raw(2 * K);
+  if (std::fread(raw.data(), sizeof(int64_t), raw.size(), f) != raw.size()) return 2;
+  for (int64_t k = 0; k < K; ++k) fm[k] = VF::FeatureMap(raw[2 * k], raw[2 * k + 1]);
+  vf.set_feature_maps(fm);
+  VF::ImageCameraMap icm(static_cast<size_t>(I));
+  if (std::fread(icm.data(), sizeof(int64_t), icm.size(), f) != icm.size()) return 2;
+  vf.set_image_camera_map(icm);
+  std::vector<double> cams(size_t(C * vf.GetIntrinsicParamsSizePerCamera()));
+  if (std::fread(cams.data(), sizeof(double), cams.size(), f) != cams.size()) return 2;
+  if (vf.set_fix_cameras(cams) != 0) return 3;
+  gba::VectorX<double> y(2 * K);
+  if (std::fread(y.data(), sizeof(double), size_t(y.size()), f) != size_t(y.size())) return 2;
+  gba::VectorX<double> x0(3 * P + 6 * I);
+  if (std::fread(x0.data(), sizeof(double), size_t(x0.size()), f) != size_t(x0.size())) return 2;
+  std::fclose(f);
+  if (argc > 3 && std::strcmp(argv[3], "--bad-size") == 0) x0.resize(x0.size() - 1);
+
+  gba::CameraSharedYCovarianceInverse<double> cov;
+  cov.SetKeysUniformStdDev(1.0, size_t(K));
+  // (max_itr_num, tau, eps1, eps2) as the reference's relative-pair test
+  gba::CameraSharedLevenbergMarquardtOptimizor<VF> optimizor(x0, size_t(iters), 1e-3, 0.0, 0.0);
+  gba::VectorX<double> x;
+  const int err = optimizor(vf, y, cov, x);
+  std::printf("err %d status %d iterations %d final_cost %.17g\n", err, optimizor.last_status(),
+              optimizor.last_report().iterations, optimizor.last_report().final_cost);
+  if (err != 0) return 1;
+  FILE* g = std::fopen(argv[2], "wb");
+  std::fwrite(x.data(), sizeof(double), size_t(x.size()), g);
+  std::fclose(g);
+  return 0;
+}

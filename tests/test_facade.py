@@ -1,0 +1,40 @@
+"""The header-only C++ facade (include/gba/camera_shared.hpp): builds and
+links against libgba.so, keeps the reference's Err for a size mismatch
+(camera_shared_levenberg_marquardt_optimizor.hpp:48-51), and on a GPU
+reaches the oracle's final cost."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from hs_sfm_gb300 import abi, synthetic
+
+from facade_util import build_facade, write_problem
+
+
+def test_facade_builds_and_rejects_bad_initial_x(tmp_path):
+    exe = build_facade(str(tmp_path))
+    s = synthetic.ring_scene(num_images=5, num_points=60, obs_per_point=3, seed=4)
+    prob = tmp_path / "p.bin"
+    write_problem(prob, s, 5)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin"), "--bad-size"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1
+    assert r.stdout.startswith("err -1 status -2")
+
+
+@pytest.mark.gpu
+def test_facade_solve_matches_oracle(tmp_path):
+    import oracle
+    exe = build_facade(str(tmp_path))
+    s = synthetic.config(0)
+    prob = tmp_path / "p.bin"
+    write_problem(prob, s, 20)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    x = np.fromfile(tmp_path / "x.bin", dtype=np.float64)
+    err, x_ref, rref = oracle.lm_solve(s, options=abi.make_options(max_iterations=20, eps1=0.0,
+                                                                    eps2=0.0))
+    c = oracle.cost(s, x, s.near_y)
+    assert abs(c - rref.final_cost) <= 1e-6 * rref.final_cost

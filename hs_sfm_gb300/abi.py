@@ -90,7 +90,7 @@ class Options(C.Structure):
         ("huber_delta", C.c_double), ("linear_solver", C.c_int32),
         ("pcg_max_iterations", C.c_int32), ("pcg_relative_tolerance", C.c_double),
         ("use_cuda_graph", C.c_int32), ("profile", C.c_int32), ("device", C.c_int32),
-        ("reserved_", C.c_int32 * 7),
+        ("shared_device", C.c_int32), ("reserved_", C.c_int32 * 6),
     ]
 
 
@@ -131,7 +131,7 @@ class ServerStats(C.Structure):
 def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PRECISION_FP64,
                  loss=LOSS_TRIVIAL, huber_delta=1.0, linear_solver=LINEAR_DENSE_CHOLESKY,
                  pcg_max_iterations=100, pcg_relative_tolerance=1e-6, use_cuda_graph=1,
-                 profile=0, device=0) -> Options:
+                 profile=0, device=0, shared_device=0) -> Options:
     """Defaults of the reference's relative-pair test
     (test_camera_shared_relative_pair.cpp:976-979)."""
     o = Options()
@@ -141,6 +141,7 @@ def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PR
     o.linear_solver = linear_solver
     o.pcg_max_iterations, o.pcg_relative_tolerance = pcg_max_iterations, pcg_relative_tolerance
     o.use_cuda_graph, o.profile, o.device = use_cuda_graph, profile, device
+    o.shared_device = shared_device
     return o
 
 

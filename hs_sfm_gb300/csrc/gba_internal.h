@@ -12,11 +12,14 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/gba.h"
 
 namespace gba {
 
-constexpr int kTile = 32;          // dense Cholesky tile (FP64)
+constexpr int kTile = 32;          // dense Cholesky tile
+constexpr int kDfTraceCap = 1024;   // traced tasks per CTA of the dataflow factorization
 constexpr int kKeyChunk = 1024;    // keys per cost work chunk
 constexpr int kPointChunk = 128;   // points per point work chunk
 constexpr int kImageChunk = 8;     // images per image work chunk (backsub)
@@ -121,7 +124,14 @@ struct DevPlan {
   void* S;                   // T: sum n^2 over problems (lower triangles)
   void* b;                   // T: [6I] rhs -> forward solution -> delta (images)
   void* Linv;                // T: [B * max_nt * kTile^2] inverses of diagonal tiles
-  int* factor_flag;          // [B] 0 ok, 1 failed
+  int* factor_flag;          // [B] 0 ok, 1 not positive definite, 2 a bounded wait ran out
+  // dataflow factorization (one problem; df_grid == 0: per-column launches)
+  int df_grid, df_max_own;
+  const int* df_own_off;     // [df_grid + 1] owned tiles of each CTA
+  const int2* df_own;        // (i, j) per owned tile, sorted by (j, i) within a CTA
+  unsigned* df_flags;        // [nt * nt] epoch at which tile (i, j) was published
+  unsigned* df_sync;         // [0] epoch of the last launch, [1] finished CTAs, [2] aborted epoch
+  unsigned long long* df_trace; // optional task timeline: [grid][kDfTraceCap][4], or null
   // Schur assembly
   const int2* pairs;         // (key_a, key_b) per pair, grouped by block
   const int4* items;         // (block, pair_begin, pair_end, prob)
@@ -145,6 +155,11 @@ struct DevPlan {
   unsigned long long* launch_counter; // device-side count (unused: host counts)
 };
 
+// A failed CUDA call on the host side of a plan (GBA_ERR_* status).
+struct CudaError {
+  int status;
+};
+
 // Host launchers (gba_kernels.cu).  `T` selects the working precision of
 // the Jacobian / Schur stages: float (mixed) or double (plain FP64).
 int launch_init(const DevPlan& d, cudaStream_t s);
@@ -161,6 +176,10 @@ int launch_assemble_S(const DevPlan& d, cudaStream_t s);
 int launch_cholesky(const DevPlan& d, cudaStream_t s);
 int launch_cholesky_factor(const DevPlan& d, cudaStream_t s);
 int launch_cholesky_solve(const DevPlan& d, cudaStream_t s);
+// Tile ownership of the dataflow factorization of an nt-tile system for this
+// device, or false when it does not fit in shared memory.
+bool dataflow_layout(int nt, bool mixed, int device, int* grid, int* max_own,
+                     std::vector<int>* own_off, std::vector<int2>* own);
 int launch_backsub(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_step(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_accept(const DevPlan& d, cudaStream_t s);

@@ -30,11 +30,17 @@
 //                    camera_shared_nllso_meta_levenberg_marquardt.hpp:33-106)
 #include "gba_internal.h"
 
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 
 namespace gba {
 namespace {
+
+namespace cg = cooperative_groups;
 
 // ---------------------------------------------------------------------------
 // helpers
@@ -922,8 +928,45 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int tile_rows(int n, int t) { return min(kTile, n - kTile * t); }
 
+// Calls f(std::integral_constant<int, i>) for i = B, B + S, ... < E.
+template <int B, int E, int S, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    static_for<B + S, E, S>(f);
+  }
+}
+
+// Shared-memory tiles: rows padded to a 16-byte multiple (36 floats, 34
+// doubles) so that 16-byte vector loads along a row are aligned and the
+// rows touched together fall in different banks.
 template <typename T>
-using Tile = T[kTile][kTile + 1];
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using V = float4;
+  static constexpr int N = 4;
+  __device__ __forceinline__ static void unpack(const V& v, float* o) {
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+  }
+  __device__ __forceinline__ static V pack(const float* o) { return make_float4(o[0], o[1], o[2], o[3]); }
+};
+template <>
+struct Vec16<double> {
+  using V = double2;
+  static constexpr int N = 2;
+  __device__ __forceinline__ static void unpack(const V& v, double* o) {
+    o[0] = v.x;
+    o[1] = v.y;
+  }
+  __device__ __forceinline__ static V pack(const double* o) { return make_double2(o[0], o[1]); }
+};
+
+template <typename T>
+using Tile = T[kTile][kTile + Vec16<T>::N];
 
 // Tile loads for 256-thread CTAs: each thread fetches its 4 elements of a
 // tile into registers first (all loads in flight together), then stores
@@ -967,74 +1010,101 @@ struct TileFetch {
   }
 };
 
+// s[u] = sum_q X[r][q] Y[c][q] for r = tid / 8 and the four columns
+// c = tid % 8 + 8u, q ascending (256 threads).  Rows are read with 16-byte
+// vector loads; the eight Y rows a warp reads at once lie in distinct banks.
+template <typename T>
+__device__ __forceinline__ void tile_xyt(const Tile<T>& X, const Tile<T>& Y, T s[4]) {
+  using V = Vec16<T>;
+  constexpr int N = V::N;
+  const int r = threadIdx.x >> 3, c0 = threadIdx.x & 7;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) s[u] = T(0);
+#pragma unroll
+  for (int q = 0; q < kTile; q += N) {
+    T x[N];
+    V::unpack(*reinterpret_cast<const typename V::V*>(&X[r][q]), x);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      T y[N];
+      V::unpack(*reinterpret_cast<const typename V::V*>(&Y[c0 + 8 * u][q]), y);
+#pragma unroll
+      for (int e = 0; e < N; ++e) s[u] = fma(x[e], y[e], s[u]);
+    }
+  }
+}
+
 // A -= X Y^T (32x32x32), 256 threads, 4 outputs each.
 template <typename T>
 __device__ __forceinline__ void tile_sub_xyt(Tile<T>& A, const Tile<T>& X, const Tile<T>& Y) {
-  const int r = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 4;
-  T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
-#pragma unroll 8
-  for (int q = 0; q < kTile; ++q) {
-    const T x = X[r][q];
-    s0 += x * Y[c0][q];
-    s1 += x * Y[c0 + 1][q];
-    s2 += x * Y[c0 + 2][q];
-    s3 += x * Y[c0 + 3][q];
-  }
-  A[r][c0] -= s0;
-  A[r][c0 + 1] -= s1;
-  A[r][c0 + 2] -= s2;
-  A[r][c0 + 3] -= s3;
+  T s[4];
+  tile_xyt<T>(X, Y, s);
+  const int r = threadIdx.x >> 3, c0 = threadIdx.x & 7;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) A[r][c0 + 8 * u] -= s[u];
 }
 
 // Factor the SPD tile D (lower triangle used; identity-padded) in one warp and
-// write L^-1 to Dinv; D is overwritten by L.  Lane i keeps row i of the
-// tile in registers; each factored column is broadcast through shared memory
-// (col, double-buffered) and the reciprocal pivots are kept in rinv.  The
-// inverse is formed one column per lane by forward substitution against L in
-// shared memory, with the stored reciprocals (no divisions).  Returns false
-// when a pivot was not positive.
+// write L^-1 to Dinv (D is left as it is).  Lane i keeps row i of the tile
+// in registers, and column i of L^-1 (forward substitution against L).
+// Columns are factored two at a time: every lane forms the 2x2 pivot block
+// from three shuffles (both reciprocal square roots issued together: the
+// second pivot is det / p0), then its own entries of both columns, which
+// are broadcast through shared memory (col: two buffers of two columns) for
+// the trailing update of the tile and of the inverse columns.  No
+// divisions.  Returns false when a pivot was not positive.
 template <typename T>
-__device__ bool warp_potrf_inverse(Tile<T>& D, Tile<T>& Dinv, T* col, T* rinv, int lane) {
+__device__ bool warp_potrf_inverse(const Tile<T>& D, Tile<T>& Dinv, T* col, int lane) {
+  using V = Vec16<T>;
+  constexpr int N = V::N;
   constexpr unsigned FULL = 0xffffffffu;
-  T a[kTile];
+  T a[kTile], x[kTile];
 #pragma unroll
-  for (int q = 0; q < kTile; ++q) a[q] = D[lane][q];
-  bool ok = true;
-#pragma unroll
-  for (int j = 0; j < kTile; ++j) {
-    const T djj = __shfl_sync(FULL, a[j], j);
-    ok = ok && (djj > T(0));
-    const T r = rsqrt(djj);
-    const T ljj = djj * r;
-    if (lane == j) rinv[j] = r;
-    const T lij = (lane > j) ? a[j] * r : ((lane == j) ? ljj : T(0));
-    a[j] = lij;
-    T* cb = col + (j & 1) * kTile;
-    cb[lane] = lij;
-    __syncwarp();
-#pragma unroll
-    for (int l = j + 1; l < kTile; ++l) a[l] -= lij * cb[l];
-  }
-#pragma unroll
-  for (int c = 0; c < kTile; ++c) D[lane][c] = (c <= lane) ? a[c] : T(0);
-  __syncwarp();
-  T x[kTile];
+  for (int q = 0; q < kTile; q += N) V::unpack(*reinterpret_cast<const typename V::V*>(&D[lane][q]), a + q);
 #pragma unroll
   for (int r = 0; r < kTile; ++r) x[r] = (r == lane) ? T(1) : T(0);
+  bool ok = true;
+  // j is a compile-time constant in every step, so a[] and x[] stay in registers
+  static_for<0, kTile, 2>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    const T p0 = __shfl_sync(FULL, a[j], j);
+    const T p1 = __shfl_sync(FULL, a[j], j + 1);
+    const T p2 = __shfl_sync(FULL, a[j + 1], j + 1);
+    const T det = fma(p0, p2, -(p1 * p1));
+    const T r0 = rsqrt(p0);
+    const T rd = rsqrt(det);
+    const T l00 = p0 * r0;             // sqrt(p0)
+    const T l10 = p1 * r0;
+    const T r1 = l00 * rd;             // 1 / sqrt(det / p0)
+    const T l11 = det * rd * r0;       // sqrt(det / p0)
+    ok = ok && (p0 > T(0)) && (det > T(0));
+    const T li0 = (lane > j) ? a[j] * r0 : ((lane == j) ? l00 : T(0));
+    const T li1 = (lane > j + 1) ? fma(-li0, l10, a[j + 1]) * r1 : ((lane == j + 1) ? l11 : T(0));
+    a[j] = li0;
+    a[j + 1] = li1;
+    T* cb = col + ((j >> 1) & 1) * 2 * kTile;
+    cb[lane] = li0;
+    cb[kTile + lane] = li1;
+    x[j] *= r0;
+    x[j + 1] = fma(-l10, x[j], x[j + 1]) * r1;
+    __syncwarp();
 #pragma unroll
-  for (int q = 0; q < kTile; ++q) {
-    x[q] *= rinv[q];
-#pragma unroll
-    for (int r = q + 1; r < kTile; ++r) x[r] -= D[r][q] * x[q];
-  }
+    for (int l = j + 2; l < kTile; ++l) {
+      const T c0 = cb[l], c1 = cb[kTile + l];
+      a[l] = fma(-li0, c0, a[l]);
+      a[l] = fma(-li1, c1, a[l]);
+      x[l] = fma(-c0, x[j], x[l]);
+      x[l] = fma(-c1, x[j + 1], x[l]);
+    }
+  });
 #pragma unroll
   for (int r = 0; r < kTile; ++r) Dinv[r][lane] = x[r];
   return ok;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
-  __shared__ Tile<T> A, Li, Lj, D, Dinv;
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_chol_step(DevPlan d, int k) {
+  __shared__ __align__(16) Tile<T> A, Li, Lj, D, Dinv;
   __shared__ T yk[kTile], tv[kTile];
   const int p = blockIdx.y;
   const LMState& st = d.state[p];
@@ -1105,9 +1175,9 @@ __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
   }
   // column c: factor the diagonal tile (own tile when i == c)
   __shared__ int ok_s;
-  __shared__ T colbuf[2 * kTile], rinv[kTile];
+  __shared__ T colbuf[4 * kTile];
   if (warp == 0) {
-    const bool ok = warp_potrf_inverse<T>(i == c ? A : D, Dinv, colbuf, rinv, lane);
+    const bool ok = warp_potrf_inverse<T>(i == c ? A : D, Dinv, colbuf, lane);
     if (lane == 0) ok_s = ok ? 1 : 0;
   }
   __syncthreads();
@@ -1126,85 +1196,511 @@ __global__ void __launch_bounds__(256) k_chol_step(DevPlan d, int k) {
       yk[tid] = y;
     }
     __syncthreads();
-    if (tid < mi) {
-      if (c == pi.nt - 1) {           // last tile: first backward step
-        T dl = T(0);
-        for (int q = tid; q < kTile; ++q) dl += Dinv[q][tid] * yk[q];
-        b[kTile * c + tid] = dl;
-      } else {
-        b[kTile * c + tid] = yk[tid];
-      }
-    }
+    if (tid < mi) b[kTile * c + tid] = yk[tid];
     return;
   }
   // i > c: L_ic = A_ic L_cc^-T, and the column-k part of the forward solve
   if (tid < mi) b[kTile * i + tid] = tv[tid];
   {
-    const int r = tid >> 3, c0 = (tid & 7) * 4;
-    T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
-#pragma unroll 8
-    for (int q = 0; q < kTile; ++q) {
-      const T x = A[r][q];
-      s0 += x * Dinv[c0][q];
-      s1 += x * Dinv[c0 + 1][q];
-      s2 += x * Dinv[c0 + 2][q];
-      s3 += x * Dinv[c0 + 3][q];
-    }
+    T sv[4];
+    tile_xyt<T>(A, Dinv, sv);
+    const int r = tid >> 3, c0 = tid & 7;
     if (r < mi) {
       T* row = S + (long long)(kTile * i + r) * n + kTile * c;
-      row[c0] = s0;
-      row[c0 + 1] = s1;
-      row[c0 + 2] = s2;
-      row[c0 + 3] = s3;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) row[c0 + 8 * u] = sv[u];
     }
   }
 }
 
-// Backward solve step k (k >= 1): y_j -= L_kj^T delta_k for j < k; the CTA
-// for j = k-1 then computes delta_{k-1} = L_{k-1,k-1}^-T y_{k-1}.
+// Dataflow factorization of one problem's reduced system in a single
+// cooperative launch.  Every CTA owns a fixed set of tiles of the lower
+// triangle and keeps them in shared memory for the whole factorization: the
+// diagonal tile (i, i) and the tile left of it, (i, i-1), belong to the CTA
+// of row i; the other tiles are spread by work (j + 1 tasks for tile (i, j))
+// over all CTAs.  A tile's tasks are its updates A_ij -= L_ik L_jk^T for
+// k = 0 .. j-1, in that order, then its factorization (i == j, with the
+// forward solve y_j = L_jj^-1 b_j) or its panel L_ij = A_ij L_jj^-T.  A
+// finished factor or panel is written to global memory (L into S, L_jj^-1
+// into Linv, y_j into b) and announced by storing the launch's epoch into
+// the tile's flag with release semantics; consumers poll flags with acquire
+// loads and read the data through L2.  Each CTA runs, among its tiles whose
+// next task has its inputs published, the one with the smallest (j, i), and
+// applies up to kDfBatch consecutive ready updates of that tile with all of
+// their loads in flight together.  Per element the arithmetic is exactly
+// that of k_chol_step (same tile routines, same order of updates), so both
+// schedules give the same bits.  Every wait is bounded: a CTA that sees
+// nothing ready for kDfSpinLimit polls records a timeout and leaves; a
+// failed pivot or a timeout raises the abort word, which every waiting CTA
+// checks.
+constexpr int kDfThreads = 256;
+constexpr long long kDfSpinLimit = 1LL << 22;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_chol_backward(DevPlan d, int k) {
-  __shared__ Tile<T> L;
-  __shared__ T dk[kTile], yj[kTile];
-  const int p = blockIdx.y;
-  const LMState& st = d.state[p];
-  if (!st.active || d.factor_flag[p]) return;
+__host__ __device__ constexpr int df_batch() { return 2; }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+// Tile loads through L2 (data another CTA published in this launch).
+template <typename T>
+__device__ __forceinline__ void fetch_rect_cg(TileFetch<T>& f, const T* S, int n, int ti, int tj) {
+  const int mi = tile_rows(n, ti), mj = tile_rows(n, tj);
+#pragma unroll
+  for (int u = 0; u < kPerThread; ++u) {
+    const int e = threadIdx.x + u * kCholThreads, r = e / kTile, c = e % kTile;
+    f.v[u] = (r < mi && c < mj) ? __ldcg(S + (long long)(kTile * ti + r) * n + kTile * tj + c) : T(0);
+  }
+}
+
+template <typename T>
+size_t df_smem_bytes(int max_own) {
+  return sizeof(Tile<T>) * size_t(max_own + 2 * df_batch<T>() + 1) +
+         sizeof(T) * size_t(max_own) * kTile + sizeof(int) * size_t(5 * max_own + 8);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
+  constexpr int NB = df_batch<T>();
+  enum { kIdle = 0, kUpdate = 1, kFinish = 2, kChain = 3, kExit = 4, kChain2 = 5 };
+  extern __shared__ __align__(16) unsigned char df_raw[];
+  __shared__ T yv[NB][kTile], colbuf[4 * kTile];
+  __shared__ int s_sel, s_cnt, s_mode, s_ok;
+  const int p = 0;
   const ProbInfo pi = d.prob[p];
-  if (k >= pi.nt) return;
-  const int j = blockIdx.x;
-  if (j >= k) return;
-  const int n = pi.n, m = tile_rows(n, k);
-  const T* S = tptr<T>(d.S) + pi.s_off;
+  const int n = pi.n, nt = pi.nt;
+  const int ob = d.df_own_off[blockIdx.x], nown = d.df_own_off[blockIdx.x + 1] - ob;
+  const int mo = d.df_max_own;
+  Tile<T>* A = reinterpret_cast<Tile<T>*>(df_raw);   // [mo] owned tiles
+  Tile<T>* W = A + mo;                                // [2 * NB] fetched L tiles
+  Tile<T>& Dinv = W[2 * NB];
+  T* bown = reinterpret_cast<T*>(W + 2 * NB + 1);     // [mo][kTile] rhs of owned diagonal tiles
+  int* ti_s = reinterpret_cast<int*>(bown + size_t(mo) * kTile);
+  int* tj_s = ti_s + mo;
+  int* kt_s = tj_s + mo;       // next update step of each owned tile (j: factor/panel; j+1: done)
+  int* rd_s = kt_s + mo;       // ready tasks found by the last poll
+  int* pr_s = rd_s + mo;       // tile (i, i-1): local index of (i, i); otherwise -1
+  T* S = tptr_mut<T>(d.S) + pi.s_off;
   T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
-  TileFetch<T> fl;
-  fl.rect(S, n, k, j);
-  T dv = T(0), yv = T(0);
-  if (threadIdx.x < kTile) {
-    dv = threadIdx.x < m ? b[kTile * k + threadIdx.x] : T(0);
-    yv = b[kTile * j + threadIdx.x];
-  }
-  fl.store(L);
-  if (threadIdx.x < kTile) dk[threadIdx.x] = dv;
-  __syncthreads();
-  if (threadIdx.x < kTile) {
-    const int c = threadIdx.x;
-    T s = T(0);
-#pragma unroll 8
-    for (int r = 0; r < kTile; ++r) s += L[r][c] * dk[r];
-    const T y = yv - s;
-    yj[c] = y;
-    if (j != k - 1) b[kTile * j + c] = y;
-  }
-  if (j == k - 1) {
+  T* Lg = tptr_mut<T>(d.Linv) + (long long)p * d.max_nt * kTile * kTile;
+  unsigned* flags = d.df_flags;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const unsigned epoch = *reinterpret_cast<volatile unsigned*>(d.df_sync) + 1u;
+
+  // factor the diagonal tile A[t] of row i in warp 0 and publish L_ii^-1 and
+  // y_i = L_ii^-1 b_i; false (after raising the abort word) on a bad pivot
+  auto finish_diag = [&](int t, int i) -> bool {
+    if (warp == 0) {
+      const bool ok = warp_potrf_inverse<T>(A[t], Dinv, colbuf, lane);
+      if (lane == 0) s_ok = ok ? 1 : 0;
+    }
     __syncthreads();
-    const T* Lv = tptr<T>(d.Linv) + ((long long)p * d.max_nt + j) * kTile * kTile;
-    if (threadIdx.x < kTile) {
-      const int c = threadIdx.x;
-      T s = T(0);
-      for (int q = c; q < kTile; ++q) s += Lv[q * kTile + c] * yj[q];
-      b[kTile * j + c] = s;
+    if (!s_ok) {
+      if (tid == 0) {
+        d.factor_flag[p] = 1;
+        __threadfence();
+        atomicExch(d.df_sync + 2, epoch);
+      }
+      return false;
+    }
+    T* Lo = Lg + (long long)i * kTile * kTile;
+    for (int e = tid; e < kTile * kTile; e += blockDim.x) Lo[e] = Dinv[e / kTile][e % kTile];
+    if (tid < kTile) {
+      T y = T(0);
+#pragma unroll 8
+      for (int q = 0; q < kTile; ++q) y += Dinv[tid][q] * bown[t * kTile + q];
+      if (tid < tile_rows(n, i)) b[kTile * i + tid] = y;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      st_release_u32(flags + (long long)i * nt + i, epoch);
+      kt_s[t] = i + 1;
+    }
+    return true;
+  };
+
+  const LMState& st = d.state[p];
+  const bool run = st.active && !d.factor_flag[p];
+  if (run) {
+    for (int t = tid; t < nown; t += blockDim.x) {
+      const int2 tl = d.df_own[ob + t];
+      ti_s[t] = tl.x;
+      tj_s[t] = tl.y;
+      kt_s[t] = 0;
+    }
+    __syncthreads();
+    for (int t = tid; t < nown; t += blockDim.x) {
+      int pr = -1;
+      if (tj_s[t] == ti_s[t] - 1)
+        for (int u = 0; u < nown; ++u)
+          if (ti_s[u] == ti_s[t] && tj_s[u] == ti_s[t]) pr = u;
+      pr_s[t] = pr;
+    }
+    for (int t = 0; t < nown; ++t) {      // owned tiles and rhs
+      TileFetch<T> f;
+      const int i = ti_s[t], j = tj_s[t];
+      if (i == j) f.diag(S, n, i); else f.rect(S, n, i, j);
+      f.store(A[t]);
+      if (i == j && tid < kTile) bown[t * kTile + tid] = tid < tile_rows(n, i) ? b[kTile * i + tid] : T(0);
     }
   }
+  __syncthreads();
+  int ndone = run ? 0 : nown;
+  long long idle = 0;
+  // optional timeline (thread 0): per task its wait start, selection, end
+  unsigned long long* tr = d.df_trace ? d.df_trace + size_t(blockIdx.x) * kDfTraceCap * 4 : nullptr;
+  unsigned long long tr_wait = 0, tr_sel = 0, tr_meta = 0;
+  int tr_n = 0;
+  bool tr_open = false;
+  if (tr && tid == 0) tr_wait = global_ns();
+  while (ndone < nown) {
+    if (tr && tid == 0 && tr_open) {
+      const unsigned long long now = global_ns();
+      if (tr_n < kDfTraceCap) {
+        unsigned long long* e = tr + 4 * tr_n;
+        e[0] = tr_meta;
+        e[1] = tr_wait;
+        e[2] = tr_sel;
+        e[3] = now;
+      }
+      ++tr_n;
+      tr_open = false;
+      tr_wait = now;
+    }
+    // poll: for each owned tile, how many of its next tasks have their inputs
+    for (int t = tid; t < nown; t += blockDim.x) {
+      const int i = ti_s[t], j = tj_s[t], k = kt_s[t];
+      int c = 0;
+      if (k < j) {
+        unsigned fi[NB], fj[NB];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+          fi[u] = (k + u < j) ? ld_acquire_u32(flags + (long long)i * nt + k + u) : 0u;
+          fj[u] = (k + u < j && i != j) ? ld_acquire_u32(flags + (long long)j * nt + k + u) : epoch;
+        }
+#pragma unroll
+        for (int u = 0; u < NB; ++u)
+          if (c == u && k + u < j && fi[u] == epoch && fj[u] == epoch) c = u + 1;
+      } else if (k == j) {
+        c = (i == j || ld_acquire_u32(flags + (long long)j * nt + j) == epoch) ? 1 : 0;
+      }
+      // a subdiagonal tile one update short of its panel: is L_jj^-1 out too?
+      int linv = 0;
+      if (pr_s[t] >= 0 && k == j - 1) linv = ld_acquire_u32(flags + (long long)j * nt + j) == epoch;
+      rd_s[t] = c | linv << 8;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int sel = -1, cnt = 0, mode = kIdle;
+      for (int t = 0; t < nown; ++t) {
+        if ((rd_s[t] & 0xff) > 0) {
+          sel = t;
+          cnt = rd_s[t] & 0xff;
+          const bool diag_at = pr_s[t] >= 0 && kt_s[pr_s[t]] == ti_s[t] - 1;
+          mode = kt_s[t] < tj_s[t] ? kUpdate : kFinish;
+          if (mode == kFinish && diag_at) mode = kChain;
+          // the last update of a subdiagonal tile, its panel and the next
+          // diagonal factor in one task when L_jj^-1 is already out
+          if (mode == kUpdate && diag_at && kt_s[t] == tj_s[t] - 1 && (rd_s[t] >> 8)) mode = kChain2;
+          break;
+        }
+      }
+      if (sel < 0) {
+        // the abort word is read every 16th idle round, the limit counted always
+        if ((++idle & 15) == 0 && ld_acquire_u32(d.df_sync + 2) == epoch) {
+          mode = kExit;
+        } else if (idle > kDfSpinLimit) {
+          d.factor_flag[p] = 2;                       // timed out
+          __threadfence();
+          atomicExch(d.df_sync + 2, epoch);
+          mode = kExit;
+        }
+      }
+      s_sel = sel;
+      s_cnt = cnt;
+      s_mode = mode;
+      if (tr && sel >= 0) {
+        tr_sel = global_ns();
+        tr_meta = (unsigned long long)mode << 56 | (unsigned long long)ti_s[sel] << 40 |
+                  (unsigned long long)tj_s[sel] << 24 | (unsigned long long)kt_s[sel] << 8 |
+                  (unsigned long long)cnt;
+        tr_open = true;
+      }
+    }
+    __syncthreads();
+    const int mode = s_mode, t = s_sel, cnt = s_cnt;
+    if (mode == kExit) break;
+    if (mode == kIdle) continue;
+    const int i = ti_s[t], j = tj_s[t], k0 = kt_s[t];
+    if (mode == kUpdate) {
+      // cnt consecutive updates from columns k0 .. k0+cnt-1
+      TileFetch<T> fi[NB], fj[NB];
+      T yr[NB];
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        if (u < cnt) {
+          fetch_rect_cg<T>(fi[u], S, n, i, k0 + u);
+          if (i != j) fetch_rect_cg<T>(fj[u], S, n, j, k0 + u);
+          if (i == j && tid < kTile) yr[u] = __ldcg(b + kTile * (k0 + u) + tid);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        if (u < cnt) {
+          fi[u].store(W[2 * u]);
+          if (i != j) fj[u].store(W[2 * u + 1]);
+          if (i == j && tid < kTile) yv[u][tid] = yr[u];
+        }
+      }
+      __syncthreads();
+      for (int u = 0; u < cnt; ++u) {
+        tile_sub_xyt<T>(A[t], W[2 * u], i == j ? W[2 * u] : W[2 * u + 1]);
+        if (i == j && tid < kTile) {
+          T tv = bown[t * kTile + tid];
+#pragma unroll 8
+          for (int q = 0; q < kTile; ++q) tv -= W[2 * u][tid][q] * yv[u][q];
+          bown[t * kTile + tid] = tv;
+        }
+      }
+      __syncthreads();
+      if (tid == 0) kt_s[t] = k0 + cnt;
+      __syncthreads();
+      continue;
+    }
+    if (i == j) {                          // factor a diagonal tile
+      if (!finish_diag(t, i)) break;
+      ++ndone;
+      __syncthreads();
+      continue;
+    }
+    // panel L_ij = A_ij L_jj^-T, kept in A[t] (kChain2: after the update
+    // from column j-1)
+    const bool chain = mode == kChain || mode == kChain2;
+    {
+      TileFetch<T> f, fi, fj;
+      const T* Li = Lg + (long long)j * kTile * kTile;
+#pragma unroll
+      for (int u = 0; u < kPerThread; ++u) f.v[u] = __ldcg(Li + threadIdx.x + u * kCholThreads);
+      if (mode == kChain2) {
+        fetch_rect_cg<T>(fi, S, n, i, j - 1);
+        fetch_rect_cg<T>(fj, S, n, j, j - 1);
+      }
+      T yj = T(0);
+      if (chain && tid < kTile) yj = __ldcg(b + kTile * j + tid);
+      f.store(Dinv);
+      if (mode == kChain2) {
+        fi.store(W[0]);
+        fj.store(W[1]);
+      }
+      if (chain && tid < kTile) yv[0][tid] = yj;
+    }
+    __syncthreads();
+    if (mode == kChain2) {
+      tile_sub_xyt<T>(A[t], W[0], W[1]);
+      __syncthreads();
+    }
+    {
+      T sv[4];
+      tile_xyt<T>(A[t], Dinv, sv);
+      __syncthreads();
+      const int r = tid >> 3, c0 = tid & 7;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) A[t][r][c0 + 8 * u] = sv[u];
+    }
+    __syncthreads();
+    {
+      const int mi = tile_rows(n, i);
+      const int r = tid >> 3, c0 = tid & 7;
+      if (r < mi) {
+        T* row = S + (long long)(kTile * i + r) * n + kTile * j;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) row[c0 + 8 * u] = A[t][r][c0 + 8 * u];
+      }
+    }
+    if (chain) {
+      // the diagonal tile of row i: its last update (from this panel), then
+      // its factorization; both are announced together
+      const int td = pr_s[t];
+      tile_sub_xyt<T>(A[td], A[t], A[t]);
+      if (tid < kTile) {
+        T tv = bown[td * kTile + tid];
+#pragma unroll 8
+        for (int q = 0; q < kTile; ++q) tv -= A[t][tid][q] * yv[0][q];
+        bown[td * kTile + tid] = tv;
+      }
+      __syncthreads();
+      if (!finish_diag(td, i)) break;
+      ++ndone;
+    } else {
+      __syncthreads();
+    }
+    if (tid == 0) {
+      st_release_u32(flags + (long long)i * nt + j, epoch);
+      kt_s[t] = j + 1;
+    }
+    ++ndone;
+    __syncthreads();
+  }
+  if (tr && tid == 0 && tr_open && tr_n < kDfTraceCap) {
+    unsigned long long* e = tr + 4 * tr_n;
+    e[0] = tr_meta;
+    e[1] = tr_wait;
+    e[2] = tr_sel;
+    e[3] = global_ns();
+  }
+  // the last CTA to finish opens the next epoch
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(d.df_sync + 1, 1u);
+    if (prev == gridDim.x - 1) {
+      d.df_sync[1] = 0u;
+      __threadfence();
+      atomicAdd(d.df_sync, 1u);
+    }
+  }
+}
+
+// Backward solve L^T delta = y in one launch per batch.  Problems with more
+// than kSolveSmallTiles tile rows get a cluster of kSolveRanks CTAs, the
+// others one CTA (R = 1).  Rank q owns the tile rows t = q (mod R) of y in
+// shared memory.  Step j (nt-1 down to 0): warp 7 of the owner of row j
+// forms delta_j = L_jj^-T y_j (y_j is final: its last update came from this
+// same CTA at step j+1) and stores it into every rank's shared memory; after
+// a cluster barrier every rank subtracts L_ji^T delta_j from its rows i < j,
+// warp w taking rows q + R*(w + 8u), reading row block j of L coalesced
+// along the row with the next step's loads already in flight.  The barrier
+// arrives relaxed (it must not wait for those loads); the delta stores are
+// ordered by a cluster-scope fence in the storing warp.
+constexpr int kSolveRanks = 8;
+constexpr int kSolveSmallTiles = 8;
+constexpr int kSolveOwnerWarp = 7;
+
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void fence_cluster() {
+  asm volatile("fence.acq_rel.cluster;\n" ::: "memory");
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void chol_solve_body(const DevPlan& d, int q) {
+  constexpr int kRows = R == 1 ? kSolveSmallTiles : (6 * 2048 / kTile + R - 1) / R;
+  __shared__ T ys[kRows][kTile];
+  __shared__ T xb[2][kTile];
+  const int p = blockIdx.y;
+  const LMState& st = d.state[p];
+  if (!st.active || d.factor_flag[p]) return;   // the same for every rank
+  const ProbInfo pi = d.prob[p];
+  const int nt = pi.nt, n = pi.n;
+  const T* S = tptr<T>(d.S) + pi.s_off;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
+  const T* Linv = tptr<T>(d.Linv) + (long long)p * d.max_nt * kTile * kTile;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nown = nt > q ? (nt - q + R - 1) / R : 0;
+  for (int e = tid; e < nown * kTile; e += blockDim.x) {
+    const int lt = e / kTile, r = e % kTile, t = q + R * lt;
+    ys[lt][r] = (kTile * t + r < n) ? b[kTile * t + r] : T(0);
+  }
+  // rows of step jj this warp handles first: i = q + R*warp
+  T cur[kTile];
+  auto fetch = [&](int jj) {
+    const int i = q + R * warp;
+    if (jj < 0 || i >= jj) return;
+    const int mj = tile_rows(n, jj);
+    const T* row = S + (long long)kTile * jj * n + kTile * i + lane;
+#pragma unroll
+    for (int r = 0; r < kTile; ++r) cur[r] = r < mj ? row[(long long)r * n] : T(0);
+  };
+  // column `lane` of L_jj^-1 for the next diagonal tile this rank owns
+  T lv[kTile];
+  int jown = nt - 1 - ((nt - 1 - q) % R + R) % R;
+  auto fetch_linv = [&](int jj) {
+    if (jj < 0 || warp != kSolveOwnerWarp) return;
+    const T* Lv = Linv + (long long)jj * kTile * kTile + lane;
+#pragma unroll
+    for (int r = 0; r < kTile; ++r) lv[r] = r >= lane ? Lv[r * kTile] : T(0);
+  };
+  fetch(nt - 1);
+  fetch_linv(jown);
+  if constexpr (R == 1) {
+    __syncthreads();
+  } else {   // every rank has started before its shared memory is written
+    __syncthreads();
+    cluster_arrive_relaxed();
+    cluster_wait();
+  }
+  for (int j = nt - 1; j >= 0; --j) {
+    const int par = j & 1;
+    T s = T(0);
+    const bool owner = (j == jown && warp == kSolveOwnerWarp);
+    if (owner) {
+      const T* y = ys[j / R];
+#pragma unroll
+      for (int r = 0; r < kTile; ++r) s += lv[r] * y[r];
+      if constexpr (R == 1) {
+        xb[par][lane] = s;
+      } else {
+        cg::cluster_group cluster = cg::this_cluster();
+        for (int rk = 0; rk < R; ++rk) *cluster.map_shared_rank(&xb[par][lane], rk) = s;
+        fence_cluster();
+      }
+    }
+    if constexpr (R == 1) {
+      __syncthreads();
+    } else {
+      cluster_arrive_relaxed();
+      cluster_wait();
+    }
+    if (owner) {
+      if (kTile * j + lane < n) b[kTile * j + lane] = s;
+      jown -= R;
+      fetch_linv(jown);
+    }
+    const int nact = j > q ? (j - q + R - 1) / R : 0;
+    if (warp < nact) {
+      T acc = T(0);
+#pragma unroll
+      for (int r = 0; r < kTile; ++r) acc += cur[r] * xb[par][r];
+      ys[warp][lane] -= acc;
+    }
+    for (int lt = warp + 8; lt < nact; lt += 8) {
+      const int i = q + R * lt;
+      const int mj = tile_rows(n, j);
+      const T* row = S + (long long)kTile * j * n + kTile * i + lane;
+      T acc = T(0);
+      for (int r = 0; r < mj; ++r) acc += row[(long long)r * n] * xb[par][r];
+      ys[lt][lane] -= acc;
+    }
+    fetch(j - 1);
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __cluster_dims__(kSolveRanks, 1, 1) __launch_bounds__(256)
+k_chol_solve(DevPlan d) {
+  chol_solve_body<T, kSolveRanks>(d, int(cg::this_cluster().block_rank()));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_chol_solve_small(DevPlan d) {
+  chol_solve_body<T, 1>(d, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1358,6 +1854,12 @@ __global__ void k_ctrl_step(DevPlan d) {
   if (lane != 0) return;
   st.iter += 1;
   st.evaluate = 0;
+  if (d.factor_flag[p] == 2) {        // a bounded wait of the factorization ran out
+    st.active = 0;
+    st.stop = GBA_STOP_ERROR;
+    st.status = GBA_ERR_TIMEOUT;
+    return;
+  }
   if (failed) {
     st.factor_fail += 1;
     st.rejected += 1;
@@ -1445,6 +1947,20 @@ __global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out) {
 
 template <typename T>
 int run_cholesky_factor(const DevPlan& d, cudaStream_t s) {
+  if (d.df_grid > 0) {
+    if (d.df_trace)
+      cudaMemsetAsync(d.df_trace, 0, sizeof(unsigned long long) * 4 * kDfTraceCap * size_t(d.df_grid), s);
+    DevPlan dd = d;
+    void* args[] = {&dd};
+    const cudaError_t e = cudaLaunchCooperativeKernel(
+        reinterpret_cast<const void*>(&k_chol_dataflow<T>), dim3(unsigned(d.df_grid)),
+        dim3(kDfThreads), args, df_smem_bytes<T>(d.df_max_own), s);
+    if (e != cudaSuccess) {
+      std::fprintf(stderr, "gba: k_chol_dataflow launch failed: %s\n", cudaGetErrorString(e));
+      throw CudaError{GBA_ERR_CUDA};
+    }
+    return 1;
+  }
   int n = 0;
   k_chol_step<T><<<dim3(unsigned(d.max_nt), unsigned(d.B)), 256, 0, s>>>(d, -1);
   ++n;
@@ -1458,12 +1974,11 @@ int run_cholesky_factor(const DevPlan& d, cudaStream_t s) {
 
 template <typename T>
 int run_cholesky_solve(const DevPlan& d, cudaStream_t s) {
-  int n = 0;
-  for (int k = d.max_nt - 1; k >= 1; --k) {
-    k_chol_backward<T><<<dim3(unsigned(k), unsigned(d.B)), 256, 0, s>>>(d, k);
-    ++n;
-  }
-  return n;
+  if (d.max_nt <= kSolveSmallTiles)
+    k_chol_solve_small<T><<<dim3(1u, unsigned(d.B)), 256, 0, s>>>(d);
+  else
+    k_chol_solve<T><<<dim3(unsigned(kSolveRanks), unsigned(d.B)), 256, 0, s>>>(d);
+  return 1;
 }
 
 template <typename T>
@@ -1584,6 +2099,80 @@ int launch_cholesky_solve(const DevPlan& d, cudaStream_t s) {
   int n = 0;
   GBA_DISPATCH(d, n = run_cholesky_solve<T>(d, s));
   return n;
+}
+
+template <typename T>
+bool dataflow_layout_t(int nt, int device, int* grid, int* max_own, std::vector<int>* own_off,
+                       std::vector<int2>* own) {
+  int sms = 0, coop = 0, optin = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (!coop || nt < 2) return false;
+  const long long ntiles = (long long)nt * (nt + 1) / 2;
+  const int G = int(std::min<long long>(sms, ntiles));
+  // row i's diagonal tile and its left neighbour go to CTA i mod G; the
+  // rest, heaviest first, to the CTA with the least work so far
+  std::vector<std::vector<int2>> lists(G);
+  std::vector<long long> load(G, 0);
+  for (int i = 0; i < nt; ++i) {
+    const int g = i % G;
+    lists[g].push_back(make_int2(i, i));
+    load[g] += i + 1;
+    if (i > 0) {
+      lists[g].push_back(make_int2(i, i - 1));
+      load[g] += i;
+    }
+  }
+  std::vector<int2> rest;
+  for (int j = 0; j < nt; ++j)
+    for (int i = j + 2; i < nt; ++i) rest.push_back(make_int2(i, j));
+  std::stable_sort(rest.begin(), rest.end(), [](const int2& a, const int2& b) { return a.y > b.y; });
+  for (const int2& t : rest) {
+    int g = 0;
+    for (int h = 1; h < G; ++h)
+      if (load[h] < load[g]) g = h;
+    lists[g].push_back(t);
+    load[g] += t.y + 1;
+  }
+  int mo = 0;
+  for (auto& l : lists) {
+    std::sort(l.begin(), l.end(), [](const int2& a, const int2& b) {
+      return a.y != b.y ? a.y < b.y : a.x < b.x;
+    });
+    mo = std::max(mo, int(l.size()));
+  }
+  const size_t smem = df_smem_bytes<T>(mo);
+  if (smem > size_t(optin) || mo > kDfThreads) return false;
+  if (cudaFuncSetAttribute(reinterpret_cast<const void*>(&k_chol_dataflow<T>),
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow<T>, kDfThreads, smem) !=
+          cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  own_off->assign(1, 0);
+  own->clear();
+  for (auto& l : lists) {
+    own->insert(own->end(), l.begin(), l.end());
+    own_off->push_back(int(own->size()));
+  }
+  *grid = G;
+  *max_own = mo;
+  return true;
+}
+
+bool dataflow_layout(int nt, bool mixed, int device, int* grid, int* max_own,
+                     std::vector<int>* own_off, std::vector<int2>* own) {
+  return mixed ? dataflow_layout_t<float>(nt, device, grid, max_own, own_off, own)
+               : dataflow_layout_t<double>(nt, device, grid, max_own, own_off, own);
 }
 
 int launch_cholesky(const DevPlan& d, cudaStream_t s) {

@@ -17,16 +17,13 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <cstdlib>
 #include <new>
 #include <numeric>
 #include <string>
 #include <vector>
 
 namespace gba {
-
-struct CudaError {
-  int status;
-};
 
 namespace {
 
@@ -128,6 +125,30 @@ struct Plan {
   double stage_ms[GBA_NUM_STAGES] = {};
   int stage_launches[GBA_NUM_STAGES] = {};
   double* d_rmse_scratch = nullptr;
+  std::string trace_path;
+
+  // Task timeline of the last dataflow factorization as CSV:
+  // cta,mode,i,j,k0,count,wait_ns,select_ns,end_ns (times from the first wait).
+  void write_trace() {
+    const size_t nent = size_t(d.df_grid) * kDfTraceCap;
+    std::vector<unsigned long long> h(nent * 4);
+    GBA_CUDA(cudaMemcpy(h.data(), d.df_trace, h.size() * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost));
+    unsigned long long t0 = ~0ull;
+    for (size_t e = 0; e < nent; ++e)
+      if (h[4 * e + 3]) t0 = std::min(t0, h[4 * e + 1]);
+    FILE* f = std::fopen(trace_path.c_str(), "w");
+    if (!f) return;
+    std::fprintf(f, "cta,mode,i,j,k0,count,wait_ns,select_ns,end_ns\n");
+    for (size_t e = 0; e < nent; ++e) {
+      const unsigned long long* r = &h[4 * e];
+      if (!r[3]) continue;
+      std::fprintf(f, "%zu,%llu,%llu,%llu,%llu,%llu,%llu,%llu,%llu\n", e / kDfTraceCap, r[0] >> 56,
+                   (r[0] >> 40) & 0xffff, (r[0] >> 24) & 0xffff, (r[0] >> 8) & 0xffff, r[0] & 0xff,
+                   r[1] - t0, r[2] - t0, r[3] - t0);
+    }
+    std::fclose(f);
+  }
 
   ~Plan() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -492,6 +513,28 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.b = arena.alloc<char>(size_t(std::max<int64_t>(6 * I, 1)) * tsz);
   D.Linv = arena.alloc<char>(size_t(nprob) * std::max(max_nt, 1) * kTile * kTile * tsz);
   D.factor_flag = arena.alloc<int>(nprob);
+  D.df_grid = 0;
+  D.df_trace = nullptr;
+  if (nprob == 1 && !opt.shared_device && max_nt >= 2) {
+    int grid = 0, mo = 0;
+    std::vector<int> own_off;
+    std::vector<int2> own;
+    if (dataflow_layout(max_nt, mixed, device, &grid, &mo, &own_off, &own)) {
+      D.df_grid = grid;
+      D.df_max_own = mo;
+      D.df_own_off = arena.upload(own_off);
+      D.df_own = arena.upload(own);
+      D.df_flags = arena.alloc<unsigned>(size_t(max_nt) * max_nt);
+      D.df_sync = arena.alloc<unsigned>(4);
+      GBA_CUDA(cudaMemsetAsync(D.df_flags, 0, sizeof(unsigned) * size_t(max_nt) * max_nt, stream));
+      GBA_CUDA(cudaMemsetAsync(D.df_sync, 0, sizeof(unsigned) * 4, stream));
+      const char* tp = std::getenv("GBA_FACTOR_TRACE");
+      if (tp && *tp) {   // diagnostics: task timeline of the factorization, written at sync
+        trace_path = tp;
+        D.df_trace = arena.alloc<unsigned long long>(size_t(grid) * kDfTraceCap * 4);
+      }
+    }
+  }
   D.pairs = arena.upload(pairs);
   D.items = arena.upload(items);
   D.blk_ij = arena.upload(blk_ij);
@@ -625,6 +668,7 @@ int Plan::run() {
 int Plan::sync() {
   GBA_CUDA(cudaStreamSynchronize(stream));
   GBA_CUDA(cudaGetLastError());
+  if (d.df_trace && !trace_path.empty()) write_trace();
   if (opt.profile) {
     std::fill(stage_ms, stage_ms + GBA_NUM_STAGES, 0.0);
     for (size_t i = 1; i < prof_stage.size(); ++i) {

@@ -180,6 +180,7 @@ struct gba_server {
           }
           gba_options o = cfg.solve;
           o.use_cuda_graph = 0;   // a micro-batch plan runs once
+          o.shared_device = 1;    // several micro-batches run at the same time
           int st = gba_plan_create(probs.data(), ys.data(), int32_t(probs.size()), &o, &b.plan);
           for (size_t q = 0; st == GBA_OK && q < b.reqs.size(); ++q)
             st = gba_plan_set_initial_x(b.plan, int32_t(q), b.reqs[q]->x0.data());

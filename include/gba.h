@@ -159,7 +159,11 @@ typedef struct gba_options {
   int32_t use_cuda_graph;     /* capture each LM iteration once, replay     */
   int32_t profile;            /* record per-stage CUDA events               */
   int32_t device;             /* CUDA device ordinal                        */
-  int32_t reserved_[7];
+  /* 1: other plans may run on the device at the same time (the server sets
+   * it); the grid-wide dataflow factorization, which wants every SM, is then
+   * not used. */
+  int32_t shared_device;
+  int32_t reserved_[6];
 } gba_options;
 
 /* Fills the defaults used by the reference's relative-pair test

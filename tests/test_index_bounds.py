@@ -3,7 +3,7 @@ problems of uneven size, every S / b / Linv element a kernel touches must
 lie inside that problem's own region.  The model restates each kernel's
 grid and early-exit guards (hs_sfm_gb300/csrc/gba_kernels.cu: k_chol_step for
 k = -1 .. nt-2 with its redundant per-column diagonal factorization,
-k_chol_backward, k_assemble_S)."""
+the cluster backward solve k_chol_solve, k_assemble_S)."""
 import math
 
 import numpy as np
@@ -77,6 +77,30 @@ class Batch:
             if i == c:
                 self.check_linv(p, c)
 
+    def solve(self, p, ranks=8, max_rows=(6 * 2048 // TILE + 7) // 8):
+        n, nt = self.n[p], self.nt[p]
+        for q in range(ranks):
+            nown = (nt - q + ranks - 1) // ranks if nt > q else 0
+            assert nown <= max_rows
+            for lt in range(nown):                    # ys load
+                t = q + ranks * lt
+                self.check_b(p, TILE * t, rows(n, t))
+            jown = nt - 1 - ((nt - 1 - q) % ranks)
+            owned = []
+            while jown >= 0:
+                owned.append(jown)
+                jown -= ranks
+            assert all(j % ranks == q for j in owned)
+            for j in owned:                           # delta_j and L_jj^-1
+                self.check_linv(p, j)
+                self.check_b(p, TILE * j, rows(n, j))
+            for j in range(nt - 1, -1, -1):
+                nact = (j - q + ranks - 1) // ranks if j > q else 0
+                for lt in range(nact):
+                    i = q + ranks * lt
+                    assert i < j and lt < nown
+                    self.check_S(p, TILE * j, rows(n, j), TILE * i, TILE)
+
     def run(self):
         touched = 0
         for bx in range(self.max_nt):                 # k_chol_step, k = -1
@@ -95,17 +119,8 @@ class Batch:
                     ti, tj = decode(lin)
                     self.step_tile(p, k, k + 1 + ti, k + 1 + tj)
                     touched += 1
-        for k in range(self.max_nt - 1, 0, -1):     # k_chol_backward
-            for j in range(k):
-                for p in range(self.B):
-                    if k >= self.nt[p]:
-                        continue
-                    n = self.n[p]
-                    m = rows(n, k)
-                    self.check_S(p, TILE * k, m, TILE * j, TILE)
-                    self.check_b(p, TILE * k, m)
-                    self.check_b(p, TILE * j, TILE)
-                    self.check_linv(p, j)
+        for p in range(self.B):                       # k_chol_solve, cluster per problem
+            self.solve(p)
         # k_assemble_S: thread (row, col) of the lower triangle
         for p in range(self.B):
             n, I = self.n[p], self.I[p]

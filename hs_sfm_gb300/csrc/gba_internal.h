@@ -20,6 +20,7 @@ namespace gba {
 
 constexpr int kTile = 32;          // dense Cholesky tile
 constexpr int kDfTraceCap = 1024;   // traced tasks per CTA of the dataflow factorization
+constexpr int kPcgSlots = 8;        // PCG partial sums per image chunk
 constexpr int kKeyChunk = 1024;    // keys per cost work chunk
 constexpr int kPointChunk = 128;   // points per point work chunk
 constexpr int kImageChunk = 8;     // images per image work chunk (backsub)
@@ -34,6 +35,8 @@ struct LMState {
   double mu, nu;
   double F, F_new;                 // current / candidate cost
   double dn2, xn2, gd;             // ||delta||^2, ||x||^2, g^T delta
+  double er;                       // e^T delta, e = g - (N + mu I) delta (inexact solves)
+  double raw;                      // sum of squared plain residuals at the current x
   unsigned long long ginf_bits;    // max |g| as ordered bits (non-negative)
   unsigned long long maxdiag_bits; // max diag(N) as ordered bits
   double initial_cost;
@@ -132,6 +135,21 @@ struct DevPlan {
   unsigned* df_flags;        // [nt * nt] epoch at which tile (i, j) was published
   unsigned* df_sync;         // [0] epoch of the last launch, [1] finished CTAs, [2] aborted epoch
   unsigned long long* df_trace; // optional task timeline: [grid][kDfTraceCap][4], or null
+  // block-Jacobi PCG on the block-sparse reduced system (linear_solver PCG)
+  int pcg;                   // 1: PCG instead of the dense factorization
+  int pcg_max_iterations;
+  double pcg_tol2;           // squared relative residual tolerance
+  const int2* blk_gij;       // [n_blocks] global (first, second) image of each block
+  const int* img_diag_blk;   // [I] block (i, i) of each image
+  const int* adj_off;        // [I + 1] blocks touching each image
+  const int2* adj;           // (block, other image << 1 | this image is the block's second)
+  void* Sblk;                // T: [n_blocks * 36], row = first image component
+  void* Minv;                // T: [I * 36] inverses of the diagonal blocks
+  void* pcg_r;               // T: [6I] residual
+  void* pcg_z;               // T: [6I] preconditioned residual
+  void* pcg_q;               // T: [6I] S p
+  void* pcg_p[2];            // T: [6I] search directions (by iteration parity)
+  double* pcg_part;          // [kPcgSlots * n_img_chunks]: p.q, r.z (x2), r.r (x2), b.b, x.r
   // Schur assembly
   const int2* pairs;         // (key_a, key_b) per pair, grouped by block
   const int4* items;         // (block, pair_begin, pair_end, prob)
@@ -149,7 +167,7 @@ struct DevPlan {
   const int* prob_key_chunk_off;  // [B+1]
   const int* prob_pt_chunk_off;   // [B+1]
   const int* prob_img_chunk_off;  // [B+1]
-  double* key_chunk_sum;          // [n_key_chunks] cost
+  double* key_chunk_sum;          // [2 * n_key_chunks] cost, sum of squared plain residuals
   double* pt_chunk_sum;           // [3 * n_pt_chunks] dn2, xn2, gd
   double* img_chunk_sum;          // [3 * n_img_chunks]
   unsigned long long* launch_counter; // device-side count (unused: host counts)
@@ -174,6 +192,9 @@ int launch_assemble(const DevPlan& d, cudaStream_t s);
 int launch_assemble_items(const DevPlan& d, cudaStream_t s);
 int launch_assemble_S(const DevPlan& d, cudaStream_t s);
 int launch_cholesky(const DevPlan& d, cudaStream_t s);
+int launch_assemble_blocks(const DevPlan& d, cudaStream_t s);
+int launch_pcg_setup(const DevPlan& d, cudaStream_t s);
+int launch_pcg_iterations(const DevPlan& d, cudaStream_t s);
 int launch_cholesky_factor(const DevPlan& d, cudaStream_t s);
 int launch_cholesky_solve(const DevPlan& d, cudaStream_t s);
 // Tile ownership of the dataflow factorization of an nt-tile system for this

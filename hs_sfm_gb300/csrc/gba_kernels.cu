@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
   const double* __restrict__ xp = d.x_pt[par];
   const double* __restrict__ rot = d.img_rot[par];
   T* __restrict__ rw = tptr_mut<T>(d.RW[par]);
-  double acc = 0.0;
+  double acc = 0.0, acc_raw = 0.0;
   for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
     const int img = __ldg(d.key_img + k), pt = __ldg(d.key_pt + k);
     double R[12];
@@ -445,6 +445,7 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
     project64(R, X, cam, u, v);
     const double2 ob = __ldg(d.key_obs + k);
     double e0 = u - ob.x, e1 = v - ob.y;   // r = f(x) - y
+    acc_raw += e0 * e0 + e1 * e1;
     if (d.key_wl) {
       const double l00 = __ldg(d.key_wl + 3LL * k), l10 = __ldg(d.key_wl + 3LL * k + 1),
                    l11 = __ldg(d.key_wl + 3LL * k + 2);
@@ -460,8 +461,12 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
     T out[4] = {T(e0 * sw), T(e1 * sw), T(sw), T(0)};
     store_vec<4>(rw + 4LL * k, out);
   }
-  double tot = block_sum(acc, red);
-  if (threadIdx.x == 0) d.key_chunk_sum[blockIdx.x] = tot;
+  const double tot = block_sum(acc, red);
+  const double tot_raw = block_sum(acc_raw, red);
+  if (threadIdx.x == 0) {
+    d.key_chunk_sum[2LL * blockIdx.x] = tot;
+    d.key_chunk_sum[2LL * blockIdx.x + 1] = tot_raw;
+  }
 }
 
 // Mixed-path cost: the projection in double-float from the double-float
@@ -477,6 +482,7 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
   const float2* __restrict__ rot = d.img_rot_ff[par];
   float* __restrict__ rw = static_cast<float*>(d.RW[par]);
   ff acc = {0.0f, 0.0f};
+  double acc_raw = 0.0;
   for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
     const int img = __ldg(d.key_img + k), pt = __ldg(d.key_pt + k);
     const float2* R = rot + 12LL * img;
@@ -514,6 +520,10 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
     const ff v = ff_fma(fa, n1, cy);
     const float2 ob0 = d.key_obs_ff[2LL * k], ob1 = d.key_obs_ff[2LL * k + 1];
     ff e0f = ff_add(u, ff_neg(ff_ld(ob0))), e1f = ff_add(v, ff_neg(ff_ld(ob1)));   // r = f(x) - y
+    {
+      const float r0 = e0f.hi + e0f.lo, r1 = e1f.hi + e1f.lo;
+      acc_raw += double(fmaf(r0, r0, r1 * r1));
+    }
     if (d.key_wl) {   // whitened residual L^T r
       const ff l00 = ff_ld(ff_split(__ldg(d.key_wl + 3LL * k)));
       const ff l10 = ff_ld(ff_split(__ldg(d.key_wl + 3LL * k + 1)));
@@ -537,7 +547,11 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
     store_vec<4>(rw + 4LL * k, out);
   }
   const double tot = block_sum(double(acc.hi) + double(acc.lo), red);
-  if (threadIdx.x == 0) d.key_chunk_sum[blockIdx.x] = tot;
+  const double tot_raw = block_sum(acc_raw, red);
+  if (threadIdx.x == 0) {
+    d.key_chunk_sum[2LL * blockIdx.x] = tot;
+    d.key_chunk_sum[2LL * blockIdx.x + 1] = tot_raw;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1704,6 +1718,289 @@ __global__ void __launch_bounds__(256) k_chol_solve_small(DevPlan d) {
 }
 
 // ---------------------------------------------------------------------------
+// Block-Jacobi PCG on the block-sparse reduced system (large scenes).  The
+// reduced system keeps one 6x6 block per co-visible image pair (first image
+// <= second): Sblk[blk][6x + y] is the row of component x of the first image
+// and the column of component y of the second.  The matrix-vector product
+// runs one warp per image over the blocks touching it (each block read from
+// both ends, no atomics); all sums have a fixed order, so a problem's
+// iterates are the same alone and in a batch.  The solution overwrites b.
+// Per problem and iteration: p.q, r.z, r.r and b.b are reduced from per-chunk
+// partials (chunks of kImageChunk images) by every CTA that needs them.
+// ---------------------------------------------------------------------------
+__device__ double block_sum_all(double v, double* smem) {
+  const double r = block_sum(v, smem);
+  if (threadIdx.x == 0) smem[32] = r;
+  __syncthreads();
+  return smem[32];
+}
+
+__device__ __forceinline__ double pcg_prob_sum(const DevPlan& d, int p, int slot, double* red) {
+  double v = 0.0;
+  for (int c = d.prob_img_chunk_off[p] + threadIdx.x; c < d.prob_img_chunk_off[p + 1]; c += blockDim.x)
+    v += d.pcg_part[(long long)kPcgSlots * c + slot];
+  return block_sum_all(v, red);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_assemble_blocks(DevPlan d) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= 36LL * d.n_blocks) return;
+  const int blk = int(e / 36), el = int(e % 36);
+  const int2 g = __ldg(d.blk_gij + blk);
+  const int p = __ldg(d.img_prob + g.x);
+  const LMState& st = d.state[p];
+  if (!st.active) return;
+  const int ib = __ldg(d.blk_item_off + blk), ie = __ldg(d.blk_item_off + blk + 1);
+  double v = 0.0;
+  for (int t = ib; t < ie; ++t) v += d.item_partial[(long long)kItemStride * t + el];
+  double sv = -v;
+  if (g.x == g.y) {
+    sv += d.U[36LL * g.x + el];
+    if (el % 7 == 0) sv += st.mu;
+  }
+  tptr_mut<T>(d.Sblk)[36LL * blk + el] = T(sv);
+  if (g.x == g.y && el < 6) {
+    double rv = 0.0;
+    for (int t = ib; t < ie; ++t) rv += d.item_partial[(long long)kItemStride * t + 36 + el];
+    tptr_mut<T>(d.b)[6LL * g.x + el] = T(d.gi[6LL * g.x + el] - rv);
+  }
+}
+
+// Inverse of each image's diagonal block (6x6 Cholesky, then L^-T L^-1).
+template <typename T>
+__global__ void __launch_bounds__(128) k_pcg_precond(DevPlan d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.I) return;
+  const int p = d.img_prob[i];
+  if (!d.state[p].active) return;
+  const T* A = tptr<T>(d.Sblk) + 36LL * d.img_diag_blk[i];
+  T L[6][6], X[6][6];
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    T sjj = A[7 * j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) sjj -= L[j][k] * L[j][k];
+    ok = ok && sjj > T(0);
+    const T ljj = sqrt(sjj > T(0) ? sjj : T(1));
+    const T rj = T(1) / ljj;
+    L[j][j] = ljj;
+#pragma unroll
+    for (int r = j + 1; r < 6; ++r) {
+      T sr = A[6 * r + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) sr -= L[r][k] * L[j][k];
+      L[r][j] = sr * rj;
+    }
+  }
+  // X = L^-1 (lower), column by column
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      if (r < c) {
+        X[r][c] = T(0);
+        continue;
+      }
+      T v = (r == c) ? T(1) : T(0);
+#pragma unroll
+      for (int k = c; k < r; ++k) v -= L[r][k] * X[k][c];
+      X[r][c] = v / L[r][r];
+    }
+  }
+  T* M = tptr_mut<T>(d.Minv) + 36LL * i;
+#pragma unroll
+  for (int x = 0; x < 6; ++x)
+#pragma unroll
+    for (int y = 0; y < 6; ++y) {
+      T v = T(0);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) v += X[k][x] * X[k][y];
+      M[6 * x + y] = v;
+    }
+  if (!ok) atomicExch(d.factor_flag + p, 1);
+}
+
+// z = Minv r for this warp's image: lanes 0..5 hold r and return z.
+template <typename T>
+__device__ __forceinline__ T pcg_precond_apply(const DevPlan& d, int img, T rv, int lane) {
+  const T* M = tptr<T>(d.Minv) + 36LL * img;
+  T z = T(0);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const T rk = __shfl_sync(0xffffffffu, rv, k);
+    if (lane < 6) z += M[6 * lane + k] * rk;
+  }
+  return z;
+}
+
+// x = 0 (in b), r = b, z = Minv r, p_0 = 0; partials r.z, r.r, b.b.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pcg_init(DevPlan d) {
+  __shared__ double red[33];
+  const Chunk ch = d.img_chunks[blockIdx.x];
+  const LMState& st = d.state[ch.prob];
+  if (!st.active || d.factor_flag[ch.prob]) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int img = ch.begin + warp;
+  double rz = 0.0, rr = 0.0;
+  if (img < ch.end) {
+    T* b = tptr_mut<T>(d.b);
+    const T rv = lane < 6 ? b[6LL * img + lane] : T(0);
+    const T z = pcg_precond_apply<T>(d, img, rv, lane);
+    if (lane < 6) {
+      b[6LL * img + lane] = T(0);
+      tptr_mut<T>(d.pcg_r)[6LL * img + lane] = rv;
+      tptr_mut<T>(d.pcg_z)[6LL * img + lane] = z;
+      tptr_mut<T>(d.pcg_p[0])[6LL * img + lane] = T(0);
+      rz = double(rv) * double(z);
+      rr = double(rv) * double(rv);
+    }
+  }
+  rz = block_sum(rz, red);
+  rr = block_sum(rr, red);
+  if (threadIdx.x == 0) {
+    double* part = d.pcg_part + (long long)kPcgSlots * blockIdx.x;
+    part[1] = rz;
+    part[3] = rr;
+    part[5] = rr;
+    part[6] = 0.0;
+  }
+}
+
+// Iteration it, part 1: beta from the last two r.z, p = z + beta p_old (own
+// images stored, neighbours' formed on the fly), q = S p, partial p.q.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pcg_spmv(DevPlan d, int it) {
+  __shared__ double red[33];
+  const Chunk ch = d.img_chunks[blockIdx.x];
+  const int p = ch.prob;
+  const LMState& st = d.state[p];
+  if (!st.active || d.factor_flag[p]) return;
+  const int par = it & 1;
+  const double rz = pcg_prob_sum(d, p, 1 + par, red);
+  const double rr = pcg_prob_sum(d, p, 3 + par, red);
+  const double bb = pcg_prob_sum(d, p, 5, red);
+  if (rr <= d.pcg_tol2 * bb) return;                  // converged (or b = 0)
+  const double rzp = it > 0 ? pcg_prob_sum(d, p, 1 + (par ^ 1), red) : 1.0;
+  const T beta = it > 0 ? T(rz / rzp) : T(0);
+  const T* z = tptr<T>(d.pcg_z);
+  const T* pold = tptr<T>(d.pcg_p[par]);
+  T* pnew = tptr_mut<T>(d.pcg_p[par ^ 1]);
+  const T* Sb = tptr<T>(d.Sblk);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int img = ch.begin + warp;
+  double dot = 0.0;
+  if (img < ch.end) {
+    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    const int a0 = __ldg(d.adj_off + img), a1 = __ldg(d.adj_off + img + 1);
+    for (int e = a0 + lane; e < a1; e += 32) {
+      const int2 en = __ldg(d.adj + e);
+      const int j = en.y >> 1;
+      T pj[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) pj[c] = z[6LL * j + c] + beta * pold[6LL * j + c];
+      const T* B = Sb + 36LL * en.x;
+      if (!(en.y & 1)) {
+#pragma unroll
+        for (int x = 0; x < 6; ++x)
+#pragma unroll
+          for (int y = 0; y < 6; ++y) acc[x] += B[6 * x + y] * pj[y];
+      } else {
+#pragma unroll
+        for (int x = 0; x < 6; ++x)
+#pragma unroll
+          for (int y = 0; y < 6; ++y) acc[y] += B[6 * x + y] * pj[x];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = warp_sum_t<T>(acc[c]);
+    if (lane < 6) {
+      T qv = acc[0];
+#pragma unroll
+      for (int c = 1; c < 6; ++c)
+        if (lane == c) qv = acc[c];
+      const T pv = z[6LL * img + lane] + beta * pold[6LL * img + lane];
+      pnew[6LL * img + lane] = pv;
+      tptr_mut<T>(d.pcg_q)[6LL * img + lane] = qv;
+      dot = double(pv) * double(qv);
+    }
+  }
+  dot = block_sum(dot, red);
+  if (threadIdx.x == 0) d.pcg_part[(long long)kPcgSlots * blockIdx.x] = dot;
+}
+
+// Iteration it, part 2: alpha = r.z / p.q, x += alpha p, r -= alpha q,
+// z = Minv r, partials of the next r.z and r.r.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
+  __shared__ double red[33];
+  const Chunk ch = d.img_chunks[blockIdx.x];
+  const int p = ch.prob;
+  LMState& st = d.state[p];
+  if (!st.active || d.factor_flag[p]) return;
+  const int par = it & 1;
+  const double rz = pcg_prob_sum(d, p, 1 + par, red);
+  const double rr = pcg_prob_sum(d, p, 3 + par, red);
+  const double bb = pcg_prob_sum(d, p, 5, red);
+  double* part = d.pcg_part + (long long)kPcgSlots * blockIdx.x;
+  if (rr <= d.pcg_tol2 * bb) {
+    // converged: carry this chunk's partials to the next parity so that
+    // every later iteration sees the same sums and returns as well
+    if (threadIdx.x == 0) {
+      part[1 + (par ^ 1)] = part[1 + par];
+      part[3 + (par ^ 1)] = part[3 + par];
+    }
+    return;
+  }
+  const double pq = pcg_prob_sum(d, p, 0, red);
+  if (!(pq > 0.0)) {
+    // breakdown (the residual is at the rounding floor): keep x and stop, by
+    // zeroing the next r.r, which the branch above then carries forward
+    if (threadIdx.x == 0) {
+      part[1 + (par ^ 1)] = part[1 + par];
+      part[3 + (par ^ 1)] = 0.0;
+    }
+    return;
+  }
+  const T alpha = T(rz / pq);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int img = ch.begin + warp;
+  double rzn = 0.0, rrn = 0.0, xr = 0.0;
+  if (img < ch.end) {
+    const long long o = 6LL * img + (lane < 6 ? lane : 0);
+    T rv = T(0);
+    if (lane < 6) {
+      T* x = tptr_mut<T>(d.b);
+      T* r = tptr_mut<T>(d.pcg_r);
+      const T pv = tptr<T>(d.pcg_p[par ^ 1])[o];
+      const T qv = tptr<T>(d.pcg_q)[o];
+      const T xv = x[o] + alpha * pv;
+      x[o] = xv;
+      rv = r[o] - alpha * qv;
+      r[o] = rv;
+      xr = double(xv) * double(rv);
+    }
+    const T z = pcg_precond_apply<T>(d, img, rv, lane);
+    if (lane < 6) {
+      tptr_mut<T>(d.pcg_z)[o] = z;
+      rzn = double(rv) * double(z);
+      rrn = double(rv) * double(rv);
+    }
+  }
+  rzn = block_sum(rzn, red);
+  rrn = block_sum(rrn, red);
+  xr = block_sum(xr, red);
+  if (threadIdx.x == 0) {
+    part[1 + (par ^ 1)] = rzn;
+    part[3 + (par ^ 1)] = rrn;
+    part[6] = xr;
+    if (blockIdx.x == d.prob_img_chunk_off[p]) st.pcg_iters += 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // back-substitution and update
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -1800,9 +2097,11 @@ __global__ void k_ctrl_initial_cost(DevPlan d) {
   if (p >= d.B) return;
   LMState& st = d.state[p];
   if (!st.active) return;
-  double F = prob_sum(d.key_chunk_sum, 1, 0, d.prob_key_chunk_off, p, lane);
+  double F = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, lane);
+  const double raw = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, lane);
   if (lane == 0) {
     st.F = F;
+    st.raw = raw;
     st.initial_cost = F;
     if (!isfinite(F)) {
       st.status = GBA_ERR_NAN;
@@ -1842,7 +2141,7 @@ __global__ void k_ctrl_step(DevPlan d) {
   LMState& st = d.state[p];
   if (!st.active) return;
   const bool failed = d.factor_flag[p] != 0;
-  double dn2 = 0, xn2 = 0, gd = 0;
+  double dn2 = 0, xn2 = 0, gd = 0, er = 0;
   if (!failed) {
     dn2 = prob_sum(d.pt_chunk_sum, 3, 0, d.prob_pt_chunk_off, p, lane) +
           prob_sum(d.img_chunk_sum, 3, 0, d.prob_img_chunk_off, p, lane);
@@ -1850,6 +2149,8 @@ __global__ void k_ctrl_step(DevPlan d) {
           prob_sum(d.img_chunk_sum, 3, 1, d.prob_img_chunk_off, p, lane);
     gd = prob_sum(d.pt_chunk_sum, 3, 2, d.prob_pt_chunk_off, p, lane) +
          prob_sum(d.img_chunk_sum, 3, 2, d.prob_img_chunk_off, p, lane);
+    // PCG leaves the image rows with residual r: the model decrease gains r^T delta_i
+    if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_img_chunk_off, p, lane);
   }
   if (lane != 0) return;
   st.iter += 1;
@@ -1869,6 +2170,7 @@ __global__ void k_ctrl_step(DevPlan d) {
     st.dn2 = dn2;
     st.xn2 = xn2;
     st.gd = gd;
+    st.er = er;
     if (sqrt(dn2) <= d.eps2 * (sqrt(xn2) + d.eps2)) {
       st.active = 0;
       st.stop = GBA_STOP_SMALL_STEP;
@@ -1884,15 +2186,19 @@ __global__ void k_ctrl_accept(DevPlan d) {
   if (p >= d.B) return;
   LMState& st = d.state[p];
   if (!st.evaluate) return;
-  const double Fn = prob_sum(d.key_chunk_sum, 1, 0, d.prob_key_chunk_off, p, lane);
+  const double Fn = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, lane);
+  const double raw_n = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, lane);
   if (lane != 0) return;
   st.evaluate = 0;
   st.F_new = Fn;
-  const double denom = st.mu * st.dn2 + st.gd;
+  // predicted decrease of the quadratic model, 2 g^T d - d^T N d, written
+  // with (N + mu I) d = g - e (e = 0 for the exact factorization)
+  const double denom = st.mu * st.dn2 + st.gd + st.er;
   const double rho = (st.F - Fn) / denom;
-  if (isfinite(Fn) && rho > 0.0) {
+  if (isfinite(Fn) && denom > 0.0 && rho > 0.0) {
     st.parity ^= 1;
     st.F = Fn;
+    st.raw = raw_n;
     st.relin = 1;
     const double t = 2.0 * rho - 1.0;
     st.mu *= fmax(1.0 / 3.0, 1.0 - t * t * t);
@@ -2173,6 +2479,29 @@ bool dataflow_layout(int nt, bool mixed, int device, int* grid, int* max_own,
                      std::vector<int>* own_off, std::vector<int2>* own) {
   return mixed ? dataflow_layout_t<float>(nt, device, grid, max_own, own_off, own)
                : dataflow_layout_t<double>(nt, device, grid, max_own, own_off, own);
+}
+
+int launch_assemble_blocks(const DevPlan& d, cudaStream_t s) {
+  if (d.n_blocks <= 0) return 0;
+  const long long n = 36LL * d.n_blocks;
+  GBA_DISPATCH(d, (k_assemble_blocks<T><<<unsigned((n + 255) / 256), 256, 0, s>>>(d)));
+  return 1;
+}
+
+int launch_pcg_setup(const DevPlan& d, cudaStream_t s) {
+  if (d.I <= 0) return 0;
+  GBA_DISPATCH(d, (k_pcg_precond<T><<<(d.I + 127) / 128, 128, 0, s>>>(d)));
+  GBA_DISPATCH(d, (k_pcg_init<T><<<d.n_img_chunks, 256, 0, s>>>(d)));
+  return 2;
+}
+
+int launch_pcg_iterations(const DevPlan& d, cudaStream_t s) {
+  if (d.I <= 0) return 0;
+  for (int it = 0; it < d.pcg_max_iterations; ++it) {
+    GBA_DISPATCH(d, (k_pcg_spmv<T><<<d.n_img_chunks, 256, 0, s>>>(d, it)));
+    GBA_DISPATCH(d, (k_pcg_update<T><<<d.n_img_chunks, 256, 0, s>>>(d, it)));
+  }
+  return 2 * d.pcg_max_iterations;
 }
 
 int launch_cholesky(const DevPlan& d, cudaStream_t s) {

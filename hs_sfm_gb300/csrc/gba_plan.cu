@@ -171,7 +171,7 @@ namespace {
 // Validates a problem for the device path.  The device path covers the
 // configuration of the benchmark workloads: points and images free, cameras
 // (shared intrinsics) fixed, no soft constraints.
-int validate(const gba_problem& p) {
+int validate(const gba_problem& p, bool pcg) {
   if (p.number_of_points < 0 || p.number_of_images < 0 || p.number_of_cameras < 0 ||
       p.number_of_keys < 0)
     return GBA_ERR_INVALID;
@@ -186,7 +186,7 @@ int validate(const gba_problem& p) {
   if (p.number_of_points > INT32_MAX / 4 || p.number_of_keys > INT32_MAX / 4)
     return GBA_ERR_INVALID;
   // the dense reduced system of one problem is at most 12288^2 doubles
-  if (p.number_of_images > 2048) return GBA_ERR_UNSUPPORTED;
+  if (!pcg && p.number_of_images > 2048) return GBA_ERR_UNSUPPORTED;
   for (int64_t i = 0; i < p.number_of_images; ++i) {
     int64_t c = p.image_camera_map[i];
     if (c < 0 || c >= p.number_of_cameras) return GBA_ERR_BAD_INDEX;
@@ -223,9 +223,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   GBA_CUDA(cudaEventCreate(&ev1));
   const bool mixed = opt.precision == GBA_PRECISION_MIXED;
   const size_t tsz = mixed ? sizeof(float) : sizeof(double);
+  const bool pcg = opt.linear_solver == GBA_LINEAR_PCG;
 
   for (int q = 0; q < nprob; ++q) {
-    int err = validate(problems[q]);
+    int err = validate(problems[q], pcg);
     if (err) return err;
     if (!near_ys || !near_ys[q]) return GBA_ERR_INVALID;
   }
@@ -280,7 +281,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     pi.n = 6 * ni;
     pi.nt = (pi.n + kTile - 1) / kTile;
     pi.s_off = s_off;
-    s_off += (long long)pi.n * pi.n;
+    if (!pcg) s_off += (long long)pi.n * pi.n;   // the dense system only for the factorization
     max_n = std::max(max_n, pi.n);
     max_nt = std::max(max_nt, pi.nt);
     x_size[q] = 3LL * np + 6LL * ni;
@@ -420,10 +421,12 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       pi.num_items = int(items.size()) - pi.item_begin;
       // dense map for the assembly of the lower triangle: map[j*ni + i], j <= i
       blk_map_off[q] = (long long)blk_map.size();
-      blk_map.resize(blk_map.size() + (size_t)ni * ni, -1);
-      for (int a = 0; a < ni; ++a)
-        for (int c = a; c < ni; ++c)
-          blk_map[blk_map_off[q] + (size_t)a * ni + c] = bid[(size_t)a * ni + c];
+      if (!pcg) {
+        blk_map.resize(blk_map.size() + (size_t)ni * ni, -1);
+        for (int a = 0; a < ni; ++a)
+          for (int c = a; c < ni; ++c)
+            blk_map[blk_map_off[q] + (size_t)a * ni + c] = bid[(size_t)a * ni + c];
+      }
     }
     // work chunks
     for (int s = 0; s < nk; s += kKeyChunk)
@@ -511,11 +514,55 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.gi = arena.alloc<double>(6 * I);
   D.S = arena.alloc<char>(size_t(std::max<long long>(s_off, 1)) * tsz);
   D.b = arena.alloc<char>(size_t(std::max<int64_t>(6 * I, 1)) * tsz);
-  D.Linv = arena.alloc<char>(size_t(nprob) * std::max(max_nt, 1) * kTile * kTile * tsz);
+  D.Linv = arena.alloc<char>(pcg ? 1 : size_t(nprob) * std::max(max_nt, 1) * kTile * kTile * tsz);
   D.factor_flag = arena.alloc<int>(nprob);
   D.df_grid = 0;
   D.df_trace = nullptr;
-  if (nprob == 1 && !opt.shared_device && max_nt >= 2) {
+  D.pcg = pcg ? 1 : 0;
+  D.pcg_max_iterations = opt.pcg_max_iterations;
+  D.pcg_tol2 = opt.pcg_relative_tolerance * opt.pcg_relative_tolerance;
+  if (pcg) {
+    // block-sparse reduced system: global image pair of each block, the
+    // diagonal block of each image, and every image's blocks by neighbour
+    const size_t nb = blk_ij.size();
+    std::vector<int2> blk_gij(nb);
+    std::vector<int> img_diag_blk(I, -1), adj_off(I + 1, 0);
+    for (int q = 0; q < nprob; ++q) {
+      const ProbInfo& pq = prob[q];
+      for (int t = pq.block_begin; t < pq.block_begin + pq.num_blocks; ++t)
+        blk_gij[t] = make_int2(pq.image_begin + blk_ij[t].x, pq.image_begin + blk_ij[t].y);
+    }
+    for (size_t t = 0; t < nb; ++t) {
+      adj_off[blk_gij[t].x + 1]++;
+      if (blk_gij[t].y != blk_gij[t].x) adj_off[blk_gij[t].y + 1]++;
+      else img_diag_blk[blk_gij[t].x] = int(t);
+    }
+    for (int64_t i = 0; i < I; ++i) adj_off[i + 1] += adj_off[i];
+    std::vector<int2> adj(adj_off[I]);
+    std::vector<int> fill(adj_off.begin(), adj_off.end() - 1);
+    for (size_t t = 0; t < nb; ++t) {
+      const int a = blk_gij[t].x, c = blk_gij[t].y;
+      adj[fill[a]++] = make_int2(int(t), c << 1);
+      if (c != a) adj[fill[c]++] = make_int2(int(t), a << 1 | 1);
+    }
+    for (int64_t i = 0; i < I; ++i)
+      std::sort(adj.begin() + adj_off[i], adj.begin() + adj_off[i + 1],
+                [](const int2& u, const int2& v) { return (u.y >> 1) < (v.y >> 1); });
+    D.blk_gij = arena.upload(blk_gij);
+    D.img_diag_blk = arena.upload(img_diag_blk);
+    D.adj_off = arena.upload(adj_off);
+    D.adj = arena.upload(adj);
+    D.Sblk = arena.alloc<char>(std::max<size_t>(nb, 1) * 36 * tsz);
+    D.Minv = arena.alloc<char>(size_t(std::max<int64_t>(I, 1)) * 36 * tsz);
+    const size_t v6 = size_t(std::max<int64_t>(6 * I, 1)) * tsz;
+    D.pcg_r = arena.alloc<char>(v6);
+    D.pcg_z = arena.alloc<char>(v6);
+    D.pcg_q = arena.alloc<char>(v6);
+    D.pcg_p[0] = arena.alloc<char>(v6);
+    D.pcg_p[1] = arena.alloc<char>(v6);
+    D.pcg_part = arena.alloc<double>(kPcgSlots * std::max<size_t>(img_chunks.size(), 1));
+  }
+  if (!pcg && nprob == 1 && !opt.shared_device && max_nt >= 2) {
     int grid = 0, mo = 0;
     std::vector<int> own_off;
     std::vector<int2> own;
@@ -553,7 +600,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.prob_key_chunk_off = arena.upload(prob_key_chunk_off);
   D.prob_pt_chunk_off = arena.upload(prob_pt_chunk_off);
   D.prob_img_chunk_off = arena.upload(prob_img_chunk_off);
-  D.key_chunk_sum = arena.alloc<double>(std::max<size_t>(key_chunks.size(), 1));
+  D.key_chunk_sum = arena.alloc<double>(2 * std::max<size_t>(key_chunks.size(), 1));
   D.pt_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(pt_chunks.size(), 1));
   D.img_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(img_chunks.size(), 1));
   D.launch_counter = nullptr;
@@ -600,12 +647,21 @@ void Plan::enqueue(bool profile) {
     mark(GBA_STAGE_POINT_SCHUR);
     n += launch_assemble_items(d, s);
     mark(GBA_STAGE_ASSEMBLE);
-    n += launch_assemble_S(d, s);
-    mark(GBA_STAGE_OTHER);
-    n += launch_cholesky_factor(d, s);
-    mark(GBA_STAGE_FACTOR);
-    n += launch_cholesky_solve(d, s);
-    mark(GBA_STAGE_SOLVE);
+    if (d.pcg) {
+      n += launch_assemble_blocks(d, s);
+      mark(GBA_STAGE_OTHER);
+      n += launch_pcg_setup(d, s);
+      mark(GBA_STAGE_FACTOR);
+      n += launch_pcg_iterations(d, s);
+      mark(GBA_STAGE_SOLVE);
+    } else {
+      n += launch_assemble_S(d, s);
+      mark(GBA_STAGE_OTHER);
+      n += launch_cholesky_factor(d, s);
+      mark(GBA_STAGE_FACTOR);
+      n += launch_cholesky_solve(d, s);
+      mark(GBA_STAGE_SOLVE);
+    }
     n += launch_backsub(d, s);
     mark(GBA_STAGE_BACKSUB);
     n += launch_ctrl_step(d, s);
@@ -808,7 +864,11 @@ int gba_plan_create(const gba_problem* problems, const double* const* near_ys, i
   if (!problems || !options || !out || n <= 0) return GBA_ERR_INVALID;
   *out = nullptr;
   if (int e = check_device()) return e;
-  if (options->linear_solver != GBA_LINEAR_DENSE_CHOLESKY) return GBA_ERR_UNSUPPORTED;
+  if (options->linear_solver != GBA_LINEAR_DENSE_CHOLESKY && options->linear_solver != GBA_LINEAR_PCG)
+    return GBA_ERR_INVALID;
+  if (options->linear_solver == GBA_LINEAR_PCG &&
+      (options->pcg_max_iterations < 1 || !(options->pcg_relative_tolerance >= 0.0)))
+    return GBA_ERR_INVALID;
   if (options->precision != GBA_PRECISION_FP64 && options->precision != GBA_PRECISION_MIXED)
     return GBA_ERR_INVALID;
   if (options->max_iterations < 0) return GBA_ERR_INVALID;
@@ -900,7 +960,7 @@ int gba_plan_get_report(gba_plan* p, int32_t q, gba_report* r) {
     r->initial_cost = st.initial_cost;
     r->final_cost = st.F;
     const int K = P.prob[q].num_keys;
-    r->final_rmse = K > 0 ? std::sqrt(std::max(st.F, 0.0) / K) : 0.0;
+    r->final_rmse = K > 0 ? std::sqrt(std::max(st.raw, 0.0) / K) : 0.0;   // plain residuals
     r->final_mu = st.mu;
     r->final_gradient_inf_norm = bits_to_double(st.ginf_bits);
     r->setup_ms = P.setup_ms;
@@ -1139,10 +1199,18 @@ int gba_schur_step(const gba_problem* problem, const double* x, const double* ne
     GBA_CUDA(cudaMemcpy(reinterpret_cast<char*>(P.d.state) + offsetof(gba::LMState, mu), &mu,
                         sizeof(double), cudaMemcpyHostToDevice));
     gba::launch_point_schur(P.d, s);
-    gba::launch_assemble(P.d, s);
-    gba::launch_cholesky(P.d, s);
+    long long nl = 0;
+    if (P.d.pcg) {
+      nl += gba::launch_assemble_items(P.d, s);
+      nl += gba::launch_assemble_blocks(P.d, s);
+      nl += gba::launch_pcg_setup(P.d, s);
+      nl += gba::launch_pcg_iterations(P.d, s);
+    } else {
+      nl += gba::launch_assemble(P.d, s);
+      nl += gba::launch_cholesky(P.d, s);
+    }
     gba::launch_backsub(P.d, s);
-    gba::g_launches += 12;
+    gba::g_launches += 9 + nl;
     GBA_CUDA(cudaStreamSynchronize(s));
     GBA_CUDA(cudaGetLastError());
     int flag = 0;

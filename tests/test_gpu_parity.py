@@ -160,6 +160,7 @@ def test_lm_distorted_with_key_weights(gba, precision):
     x, rep = gba.solve(s, _lm_opts(precision, 15))
     err, x_ref, rref = oracle.lm_solve(s, options=_lm_opts(abi.PRECISION_FP64, 15))
     assert abs(rep.final_cost - rref.final_cost) <= COST_RTOL * rref.final_cost
+    assert abs(rep.final_rmse - rref.final_rmse) <= RMSE_ATOL   # plain, unweighted residuals
 
 
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
@@ -176,6 +177,7 @@ def test_lm_huber_with_outliers(gba, precision):
     err, x_ref, rref = oracle.lm_solve(s, options=abi.make_options(
         max_iterations=20, eps1=0.0, eps2=0.0, loss=abi.LOSS_HUBER, huber_delta=1.0))
     assert abs(rep.final_cost - rref.final_cost) <= COST_RTOL * rref.final_cost
+    assert abs(rep.final_rmse - rref.final_rmse) <= RMSE_ATOL   # outliers included, no loss
 
 
 def test_medium_grid_mixed_vs_fp64_oracle(gba):

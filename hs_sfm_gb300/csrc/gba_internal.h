@@ -150,6 +150,7 @@ struct DevPlan {
   void* pcg_q;               // T: [6I] S p
   void* pcg_p[2];            // T: [6I] search directions (by iteration parity)
   double* pcg_part;          // [kPcgSlots * n_img_chunks]: p.q, r.z (x2), r.r (x2), b.b, x.r
+  int* pcg_done;             // [B] 1 once a problem's inner solve has stopped
   // Schur assembly
   const int2* pairs;         // (key_a, key_b) per pair, grouped by block
   const int4* items;         // (block, pair_begin, pair_end, prob)

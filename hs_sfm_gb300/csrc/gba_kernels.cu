@@ -1866,6 +1866,7 @@ __global__ void __launch_bounds__(256) k_pcg_init(DevPlan d) {
     part[3] = rr;
     part[5] = rr;
     part[6] = 0.0;
+    if (blockIdx.x == d.prob_img_chunk_off[ch.prob]) d.pcg_done[ch.prob] = 0;
   }
 }
 
@@ -1877,7 +1878,7 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(DevPlan d, int it) {
   const Chunk ch = d.img_chunks[blockIdx.x];
   const int p = ch.prob;
   const LMState& st = d.state[p];
-  if (!st.active || d.factor_flag[p]) return;
+  if (!st.active || d.factor_flag[p] || d.pcg_done[p]) return;
   const int par = it & 1;
   const double rz = pcg_prob_sum(d, p, 1 + par, red);
   const double rr = pcg_prob_sum(d, p, 3 + par, red);
@@ -1939,7 +1940,8 @@ __global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
   const Chunk ch = d.img_chunks[blockIdx.x];
   const int p = ch.prob;
   LMState& st = d.state[p];
-  if (!st.active || d.factor_flag[p]) return;
+  if (!st.active || d.factor_flag[p] || d.pcg_done[p]) return;
+  const bool lead = blockIdx.x == d.prob_img_chunk_off[p];
   const int par = it & 1;
   const double rz = pcg_prob_sum(d, p, 1 + par, red);
   const double rr = pcg_prob_sum(d, p, 3 + par, red);
@@ -1951,6 +1953,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
     if (threadIdx.x == 0) {
       part[1 + (par ^ 1)] = part[1 + par];
       part[3 + (par ^ 1)] = part[3 + par];
+      if (lead) d.pcg_done[p] = 1;   // later launches return at once
     }
     return;
   }
@@ -1996,7 +1999,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
     part[1 + (par ^ 1)] = rzn;
     part[3 + (par ^ 1)] = rrn;
     part[6] = xr;
-    if (blockIdx.x == d.prob_img_chunk_off[p]) st.pcg_iters += 1;
+    if (lead) st.pcg_iters += 1;
   }
 }
 

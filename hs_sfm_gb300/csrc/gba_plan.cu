@@ -561,6 +561,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     D.pcg_p[0] = arena.alloc<char>(v6);
     D.pcg_p[1] = arena.alloc<char>(v6);
     D.pcg_part = arena.alloc<double>(kPcgSlots * std::max<size_t>(img_chunks.size(), 1));
+    D.pcg_done = arena.alloc<int>(nprob);
   }
   if (!pcg && nprob == 1 && !opt.shared_device && max_nt >= 2) {
     int grid = 0, mo = 0;

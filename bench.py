@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--pool", type=int, default=256, help="serving: distinct request scenes")
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--max-in-flight", type=int, default=4)
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="grid workload only: skip the window-batch and serving summaries")
     ap.add_argument("--windows", type=int, default=512)
     ap.add_argument("--per-problem-sample", type=int, default=512,
                     help="windows solved one by one on the FP64 path (all by default)")
@@ -374,6 +376,30 @@ def run_gba(args, ws, rank, local):
                           f"time scaled by {args.cpu_sample_stride} ({wall:.1f} s wall)"),
                "seconds_per_iteration": est}
 
+    secondary = None
+    if rank == 0 and ws == 1 and not args.no_secondary:
+        # the batched and the serving metrics, each on its own workload after
+        # the timed region above (summaries; the full lines come from
+        # --workload windows / serving)
+        import copy
+        a2 = copy.copy(args)
+        a2.windows, a2.per_problem_sample, a2.steps, a2.warmup = 512, 64, 3, 3
+        w = run_windows(a2, ws, rank, local)
+        a3 = copy.copy(args)
+        a3.rates, a3.duration, a3.pool = "100,1000", 4.0, 96
+        sv = run_serving(a3, ws, rank, local)
+        secondary = {
+            "windows": {k: w[k] for k in ("metric", "value", "unit", "ms_per_step",
+                                          "speedup_vs_per_problem_fp64",
+                                          "final_cost_max_rel_diff_vs_fp64")},
+            "windows_per_problem_fp64": w["per_problem_fp64"],
+            "serving": {"metric": sv["metric"], "value": sv["value"], "unit": sv["unit"],
+                        "p50_ms": sv["p50_ms"], "p99_ms": sv["p99_ms"],
+                        "sweep": [{k: r[k] for k in ("rate", "solves_per_s", "p50_ms", "p99_ms")}
+                                  for r in sv["sweep"]],
+                        "final_cost_max_rel_diff_vs_fp64": sv["final_cost_max_rel_diff_vs_fp64"]},
+        }
+
     if rank == 0:
         lat = sorted(step_ms)
         out = {
@@ -399,6 +425,7 @@ def run_gba(args, ws, rank, local):
             "clocks": clk,
             "cpu_baseline": cpu,
             "wall_s_timed": t_wall,
+            "secondary": secondary,
         }
         print(json.dumps(out), flush=True)
     plan.close()
@@ -484,8 +511,7 @@ def run_windows(args, ws, rank, local):
         "clocks": clk,
     }
     del h2d
-    print(json.dumps(out), flush=True)
-    return 0
+    return out
 
 
 WALK_ITERS = 10
@@ -682,8 +708,7 @@ def run_serving(args, ws, rank, local):
                 "note": "host buffers through gba_server_submit/wait"},
         "gpu_launches": int(launches), "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def main():
@@ -692,9 +717,11 @@ def main():
     if args.impl == "reference":
         return run_reference(args, ws, rank)
     if args.workload == "windows":
-        return run_windows(args, ws, rank, local)
+        print(json.dumps(run_windows(args, ws, rank, local)), flush=True)
+        return 0
     if args.workload == "serving":
-        return run_serving(args, ws, rank, local)
+        print(json.dumps(run_serving(args, ws, rank, local)), flush=True)
+        return 0
     if args.workload == "walk":
         return run_walk(args, ws, rank, local)
     return run_gba(args, ws, rank, local)

@@ -1024,38 +1024,48 @@ struct TileFetch {
   }
 };
 
-// s[u] = sum_q X[r][q] Y[c][q] for r = tid / 8 and the four columns
-// c = tid % 8 + 8u, q ascending (256 threads).  Rows are read with 16-byte
-// vector loads; the eight Y rows a warp reads at once lie in distinct banks.
+// s[u] = sum_q X[r][q] Y[c][q] (q ascending) for the 128 threads tid < 128:
+// rows r = tid / 8 and r + 16, columns c = tid % 8 + 8u (u = 0..3); s[0..3]
+// is row r, s[4..7] row r + 16.  Rows are read with 16-byte vector loads; the
+// rows a warp reads at once lie in distinct banks.  Two rows per thread halve
+// the shared-memory wavefronts per FMA against one row per thread.
 template <typename T>
-__device__ __forceinline__ void tile_xyt(const Tile<T>& X, const Tile<T>& Y, T s[4]) {
+__device__ __forceinline__ void tile_xyt(const Tile<T>& X, const Tile<T>& Y, T s[8]) {
   using V = Vec16<T>;
   constexpr int N = V::N;
   const int r = threadIdx.x >> 3, c0 = threadIdx.x & 7;
 #pragma unroll
-  for (int u = 0; u < 4; ++u) s[u] = T(0);
+  for (int u = 0; u < 8; ++u) s[u] = T(0);
 #pragma unroll
   for (int q = 0; q < kTile; q += N) {
-    T x[N];
-    V::unpack(*reinterpret_cast<const typename V::V*>(&X[r][q]), x);
+    T x0[N], x1[N];
+    V::unpack(*reinterpret_cast<const typename V::V*>(&X[r][q]), x0);
+    V::unpack(*reinterpret_cast<const typename V::V*>(&X[r + 16][q]), x1);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       T y[N];
       V::unpack(*reinterpret_cast<const typename V::V*>(&Y[c0 + 8 * u][q]), y);
 #pragma unroll
-      for (int e = 0; e < N; ++e) s[u] = fma(x[e], y[e], s[u]);
+      for (int e = 0; e < N; ++e) {
+        s[u] = fma(x0[e], y[e], s[u]);
+        s[4 + u] = fma(x1[e], y[e], s[4 + u]);
+      }
     }
   }
 }
 
-// A -= X Y^T (32x32x32), 256 threads, 4 outputs each.
+// A -= X Y^T (32x32x32) by threads 0..127, 8 outputs each.
 template <typename T>
 __device__ __forceinline__ void tile_sub_xyt(Tile<T>& A, const Tile<T>& X, const Tile<T>& Y) {
-  T s[4];
+  if (threadIdx.x >= 128) return;
+  T s[8];
   tile_xyt<T>(X, Y, s);
   const int r = threadIdx.x >> 3, c0 = threadIdx.x & 7;
 #pragma unroll
-  for (int u = 0; u < 4; ++u) A[r][c0 + 8 * u] -= s[u];
+  for (int u = 0; u < 4; ++u) {
+    A[r][c0 + 8 * u] -= s[u];
+    A[r + 16][c0 + 8 * u] -= s[4 + u];
+  }
 }
 
 // Factor the SPD tile D (lower triangle used; identity-padded) in one warp and
@@ -1215,14 +1225,17 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_chol_step(DevPl
   }
   // i > c: L_ic = A_ic L_cc^-T, and the column-k part of the forward solve
   if (tid < mi) b[kTile * i + tid] = tv[tid];
-  {
-    T sv[4];
+  if (tid < 128) {
+    T sv[8];
     tile_xyt<T>(A, Dinv, sv);
     const int r = tid >> 3, c0 = tid & 7;
-    if (r < mi) {
-      T* row = S + (long long)(kTile * i + r) * n + kTile * c;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) row[c0 + 8 * u] = sv[u];
+    for (int h = 0; h < 2; ++h) {
+      if (r + 16 * h < mi) {
+        T* row = S + (long long)(kTile * i + r + 16 * h) * n + kTile * c;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) row[c0 + 8 * u] = sv[4 * h + u];
+      }
     }
   }
 }
@@ -1526,12 +1539,17 @@ __global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
       __syncthreads();
     }
     {
-      T sv[4];
-      tile_xyt<T>(A[t], Dinv, sv);
+      T sv[8];
+      if (tid < 128) tile_xyt<T>(A[t], Dinv, sv);
       __syncthreads();
-      const int r = tid >> 3, c0 = tid & 7;
+      if (tid < 128) {
+        const int r = tid >> 3, c0 = tid & 7;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) A[t][r][c0 + 8 * u] = sv[u];
+        for (int u = 0; u < 4; ++u) {
+          A[t][r][c0 + 8 * u] = sv[u];
+          A[t][r + 16][c0 + 8 * u] = sv[4 + u];
+        }
+      }
     }
     __syncthreads();
     {

@@ -169,6 +169,16 @@ struct DevPlan {
   const int* prob_pt_chunk_off;   // [B+1]
   const int* prob_img_chunk_off;  // [B+1]
   double* key_chunk_sum;          // [2 * n_key_chunks] cost, sum of squared plain residuals
+  // soft constraints on points and images (rows of y after the keys)
+  int n_cons;
+  const int4* cons;               // (group 0 point / 1 image, global index, parameter, problem)
+  const double2* cons_yw;         // (observed value, weight)
+  const int* pt_cons_off;         // [P + 1] into cons_by_pt, or null without constraints
+  const int* cons_by_pt;
+  const int* img_cons_off;        // [I + 1] into cons_by_img
+  const int* cons_by_img;
+  const int* prob_cons_off;       // [B + 1] rows of each problem
+  double* cons_cost;              // [B] sum w (x - y)^2 at the x of the last cost launch
   double* pt_chunk_sum;           // [3 * n_pt_chunks] dn2, xn2, gd
   double* img_chunk_sum;          // [3 * n_img_chunks]
   unsigned long long* launch_counter; // device-side count (unused: host counts)

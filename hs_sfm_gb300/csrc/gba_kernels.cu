@@ -417,6 +417,26 @@ __global__ void k_image_prep(DevPlan d, int which) {
   IL[6] = T(ct); IL[7] = T(s); IL[8] = T(c); IL[9] = T(a1); IL[10] = T(a2); IL[11] = T(0);
 }
 
+// Soft-constraint part of the cost, sum w (x - y)^2 (no loss), one CTA per
+// problem over its rows (camera_shared_mahalanobis_distance_calculator.hpp:28-58).
+__global__ void __launch_bounds__(256) k_cons_cost(DevPlan d, int which) {
+  __shared__ double red[32];
+  const int p = blockIdx.x;
+  const LMState& st = d.state[p];
+  if (which == 0 ? !st.active : !st.evaluate) return;
+  const int par = which ? 1 - st.parity : st.parity;
+  double acc = 0.0;
+  for (int r = d.prob_cons_off[p] + threadIdx.x; r < d.prob_cons_off[p + 1]; r += blockDim.x) {
+    const int4 c = d.cons[r];
+    const double2 yw = d.cons_yw[r];
+    const double x = c.x == 0 ? d.x_pt[par][3LL * c.y + c.z] : d.x_img[par][6LL * c.y + c.z];
+    const double v = x - yw.x;
+    acc += yw.y * v * v;
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) d.cons_cost[p] = acc;
+}
+
 // ---------------------------------------------------------------------------
 // cost: FP64 residual per key, whitened and weighted residual stored in T
 // ---------------------------------------------------------------------------
@@ -645,6 +665,16 @@ __global__ void __launch_bounds__(kPointChunk) k_point_reduce(DevPlan d) {
       g[1] += jp[1] * rr[0] + jp[4] * rr[1];
       g[2] += jp[2] * rr[0] + jp[5] * rr[1];
     }
+    if (d.pt_cons_off) {   // soft constraints: weight on the diagonal, w (x - y) in g
+      const double* xp = d.x_pt[st.parity] + 3LL * pt;
+      for (int c = d.pt_cons_off[pt]; c < d.pt_cons_off[pt + 1]; ++c) {
+        const int row = d.cons_by_pt[c];
+        const int b = d.cons[row].z;
+        const double2 yw = d.cons_yw[row];
+        V[b == 0 ? 0 : (b == 1 ? 3 : 5)] += T(yw.y);
+        g[b] += T(yw.y * (xp[b] - yw.x));
+      }
+    }
     T pv[12] = {V[0], V[1], V[2], V[3], V[4], V[5], g[0], g[1], g[2], T(0), T(0), T(0)};
     store_vec<12>(tptr_mut<T>(d.PV) + 12LL * pt, pv);
     vmax = fmax(fmax(double(V[0]), double(V[3])), double(V[5]));
@@ -726,6 +756,23 @@ __global__ void __launch_bounds__(256) k_image_finalize(DevPlan d) {
   // lane e holds entry e of (upper U in row order, then g)
   double* U = d.U + 36LL * img;
   double dmax = 0.0, gmax = 0.0;
+  if (d.img_cons_off && lane < 27) {   // soft constraints on this image's parameters
+    int a = -1, b = -1;
+    if (lane < 21) {
+      int e = lane;
+      a = 0;
+      while (e >= 6 - a) { e -= 6 - a; ++a; }
+      b = a + e;
+    }
+    const double* xi = d.x_img[st.parity] + 6LL * img;
+    for (int c = d.img_cons_off[img]; c < d.img_cons_off[img + 1]; ++c) {
+      const int row = d.cons_by_img[c];
+      const int prm = d.cons[row].z;
+      const double2 yw = d.cons_yw[row];
+      if (lane < 21 && a == b && a == prm) v += yw.y;
+      if (lane >= 21 && lane - 21 == prm) v += yw.y * (xi[prm] - yw.x);
+    }
+  }
   if (lane < 21) {
     int a = 0, e = lane;
     while (e >= 6 - a) { e -= 6 - a; ++a; }
@@ -851,7 +898,7 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
 #pragma unroll
       for (int e = 0; e < kZStride; ++e) zb[e] = za[e];
       T ps[12];
-      load_vec<12>(PS + 12LL * __ldg(d.key_pt + pr.x), ps);
+      load_vec<12>(PS + 12LL * pr.y, ps);   // a diagonal block's pair carries the point
 #pragma unroll
       for (int r = 0; r < 6; ++r) racc[r] += za[r] * ps[6] + za[6 + r] * ps[7] + za[12 + r] * ps[8];
     } else {
@@ -2120,6 +2167,7 @@ __global__ void k_ctrl_initial_cost(DevPlan d) {
   if (!st.active) return;
   double F = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, lane);
   const double raw = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, lane);
+  if (d.cons_cost) F += d.cons_cost[p];
   if (lane == 0) {
     st.F = F;
     st.raw = raw;
@@ -2207,7 +2255,8 @@ __global__ void k_ctrl_accept(DevPlan d) {
   if (p >= d.B) return;
   LMState& st = d.state[p];
   if (!st.evaluate) return;
-  const double Fn = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, lane);
+  const double Fn = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, lane) +
+                    (d.cons_cost ? d.cons_cost[p] : 0.0);
   const double raw_n = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, lane);
   if (lane != 0) return;
   st.evaluate = 0;
@@ -2346,12 +2395,19 @@ int launch_image_prep(const DevPlan& d, int which, cudaStream_t s) {
 }
 
 int launch_cost(const DevPlan& d, int which, cudaStream_t s) {
-  if (d.n_key_chunks <= 0) return 0;
-  if (d.precision == GBA_PRECISION_MIXED)
-    k_cost_ff<<<d.n_key_chunks, 256, 0, s>>>(d, which);
-  else
-    k_cost<double><<<d.n_key_chunks, 256, 0, s>>>(d, which);
-  return 1;
+  int n = 0;
+  if (d.n_key_chunks > 0) {
+    if (d.precision == GBA_PRECISION_MIXED)
+      k_cost_ff<<<d.n_key_chunks, 256, 0, s>>>(d, which);
+    else
+      k_cost<double><<<d.n_key_chunks, 256, 0, s>>>(d, which);
+    ++n;
+  }
+  if (d.n_cons > 0) {
+    k_cons_cost<<<d.B, 256, 0, s>>>(d, which);
+    ++n;
+  }
+  return n;
 }
 
 int launch_ctrl_initial_cost(const DevPlan& d, cudaStream_t s) {

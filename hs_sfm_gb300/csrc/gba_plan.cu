@@ -181,8 +181,16 @@ int validate(const gba_problem& p, bool pcg) {
   if (p.number_of_cameras > 0 && params_per_camera(p.intrinsic_computations_mask) > 0 &&
       !p.fix_cameras)
     return GBA_ERR_INVALID;
-  if (p.number_of_point_constraints > 0 || p.number_of_image_constraints > 0)
-    return GBA_ERR_UNSUPPORTED;
+  if ((p.number_of_point_constraints > 0 && !p.point_constraints) ||
+      (p.number_of_image_constraints > 0 && !p.image_constraints) ||
+      p.number_of_point_constraints < 0 || p.number_of_image_constraints < 0)
+    return GBA_ERR_INVALID;
+  for (int64_t c = 0; c < p.number_of_point_constraints; ++c)
+    if (p.point_constraints[c].point_id < 0 || p.point_constraints[c].point_id >= p.number_of_points)
+      return GBA_ERR_BAD_INDEX;
+  for (int64_t c = 0; c < p.number_of_image_constraints; ++c)
+    if (p.image_constraints[c].image_id < 0 || p.image_constraints[c].image_id >= p.number_of_images)
+      return GBA_ERR_BAD_INDEX;
   if (p.number_of_points > INT32_MAX / 4 || p.number_of_keys > INT32_MAX / 4)
     return GBA_ERR_INVALID;
   // the dense reduced system of one problem is at most 12288^2 doubles
@@ -260,6 +268,9 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   std::vector<int4> img_items;
   std::vector<int> img_item_off(1, 0);
   std::vector<int> prob_key_chunk_off(1, 0), prob_pt_chunk_off(1, 0), prob_img_chunk_off(1, 0);
+  std::vector<int4> cons;          // (group 0 point / 1 image, global index, parameter, problem)
+  std::vector<double2> cons_yw;    // (observed value, weight)
+  std::vector<int> prob_cons_off(1, 0);
   prob.resize(nprob);
   key_sorted_to_orig.resize(nprob);
   x_size.resize(nprob);
@@ -401,7 +412,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
           for (int c = a; c < b1; ++c) {
             const int ic2 = key_img[kb + c] - int(ib);
             const int blk = bid[(size_t)ia * ni + ic2] - block_begin;
-            pairs[cur[blk]++] = make_int2(int(kb + a), int(kb + c));
+            // a pair of a diagonal block is a key with itself: carry its point instead
+            pairs[cur[blk]++] = make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
           }
         }
       }
@@ -438,6 +450,33 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     for (int s = 0; s < ni; s += kImageChunk)
       img_chunks.push_back(Chunk{q, int(ib + s), int(ib + std::min(ni, s + kImageChunk)), 0});
     prob_img_chunk_off.push_back(int(img_chunks.size()));
+    // soft constraints on points and images, in y order
+    // (camera_shared_vector_function.hpp:483-629): the rows after the keys,
+    // each a copy of one parameter with its own weight; camera constraints
+    // have no rows while the cameras are fixed
+    {
+      int64_t r = 0;
+      auto add = [&](int group, int64_t index, int param) {
+        cons.push_back(make_int4(group, int(index), param, q));
+        cons_yw.push_back(make_double2(y[2LL * nk + r],
+                                       p.constraint_weights ? p.constraint_weights[r] : 1.0));
+        ++r;
+      };
+      for (int64_t c = 0; c < p.number_of_point_constraints; ++c) {
+        const gba_point_constraint& pc = p.point_constraints[c];
+        for (int b = 0; b < 3; ++b)
+          if (pc.mask & (1u << b)) add(0, pb + pc.point_id, b);
+      }
+      for (int64_t c = 0; c < p.number_of_image_constraints; ++c) {
+        const gba_image_constraint& ic = p.image_constraints[c];
+        if (ic.mask & GBA_IMAGE_CONSTRAIN_ROTATION)
+          for (int b = 0; b < 3; ++b) add(1, ib + ic.image_id, b);
+        if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_X) add(1, ib + ic.image_id, 3);
+        if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Y) add(1, ib + ic.image_id, 4);
+        if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Z) add(1, ib + ic.image_id, 5);
+      }
+      prob_cons_off.push_back(int(cons.size()));
+    }
     pb += np;
     ib += ni;
     kb += nk;
@@ -602,6 +641,32 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.prob_pt_chunk_off = arena.upload(prob_pt_chunk_off);
   D.prob_img_chunk_off = arena.upload(prob_img_chunk_off);
   D.key_chunk_sum = arena.alloc<double>(2 * std::max<size_t>(key_chunks.size(), 1));
+  D.n_cons = int(cons.size());
+  D.cons = nullptr;
+  D.pt_cons_off = nullptr;
+  D.img_cons_off = nullptr;
+  D.cons_cost = nullptr;
+  if (!cons.empty()) {
+    // rows of each point / image in y order, for the linearization
+    std::vector<int> pt_off(P + 1, 0), img_off(I + 1, 0);
+    for (const int4& c : cons) (c.x == 0 ? pt_off[c.y + 1] : img_off[c.y + 1])++;
+    for (int64_t i = 0; i < P; ++i) pt_off[i + 1] += pt_off[i];
+    for (int64_t i = 0; i < I; ++i) img_off[i + 1] += img_off[i];
+    std::vector<int> by_pt(pt_off[P]), by_img(img_off[I]);
+    std::vector<int> fp(pt_off.begin(), pt_off.end() - 1), fi(img_off.begin(), img_off.end() - 1);
+    for (size_t r = 0; r < cons.size(); ++r) {
+      if (cons[r].x == 0) by_pt[fp[cons[r].y]++] = int(r);
+      else by_img[fi[cons[r].y]++] = int(r);
+    }
+    D.cons = arena.upload(cons);
+    D.cons_yw = arena.upload(cons_yw);
+    D.pt_cons_off = arena.upload(pt_off);
+    D.cons_by_pt = arena.upload(by_pt);
+    D.img_cons_off = arena.upload(img_off);
+    D.cons_by_img = arena.upload(by_img);
+    D.prob_cons_off = arena.upload(prob_cons_off);
+    D.cons_cost = arena.alloc<double>(nprob);
+  }
   D.pt_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(pt_chunks.size(), 1));
   D.img_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(img_chunks.size(), 1));
   D.launch_counter = nullptr;
@@ -1104,6 +1169,23 @@ int gba_vector_function(const gba_problem* problem, const double* x, double* y, 
     for (int t = 0; t < P.d.K; ++t) {
       y[2 * perm[t]] = ys[2 * t];
       y[2 * perm[t] + 1] = ys[2 * t + 1];
+    }
+    // constraint rows copy their parameter (x = [points 3P][images 6I])
+    int64_t r = 2 * problem->number_of_keys;
+    const int64_t img0 = 3 * problem->number_of_points;
+    for (int64_t c = 0; c < problem->number_of_point_constraints; ++c) {
+      const gba_point_constraint& pc = problem->point_constraints[c];
+      for (int b = 0; b < 3; ++b)
+        if (pc.mask & (1u << b)) y[r++] = x[3 * pc.point_id + b];
+    }
+    for (int64_t c = 0; c < problem->number_of_image_constraints; ++c) {
+      const gba_image_constraint& ic = problem->image_constraints[c];
+      const double* xi = x + img0 + 6 * ic.image_id;
+      if (ic.mask & GBA_IMAGE_CONSTRAIN_ROTATION)
+        for (int b = 0; b < 3; ++b) y[r++] = xi[b];
+      if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_X) y[r++] = xi[3];
+      if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Y) y[r++] = xi[4];
+      if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Z) y[r++] = xi[5];
     }
     return GBA_OK;
   });

@@ -287,7 +287,7 @@ class Server:
 def vector_function(scene, x, precision=abi.PRECISION_FP64):
     cp = abi.CProblem(scene)
     x = _f64(x)
-    y = np.zeros(2 * scene.number_of_keys)
+    y = np.zeros(abi.y_size(scene))   # keys, then the constraint rows
     _check(lib().gba_vector_function(cp.ref, abi.dptr(x), abi.dptr(y), precision),
            "gba_vector_function")
     return y

@@ -135,6 +135,7 @@ struct DevPlan {
   unsigned* df_flags;        // [nt * nt] epoch at which tile (i, j) was published
   unsigned* df_sync;         // [0] epoch of the last launch, [1] finished CTAs, [2] aborted epoch
   unsigned long long* df_trace; // optional task timeline: [grid][kDfTraceCap][4], or null
+  long long df_spin_limit;   // idle polls before a CTA gives up (GBA_ERR_TIMEOUT)
   // block-Jacobi PCG on the block-sparse reduced system (linear_solver PCG)
   int pcg;                   // 1: PCG instead of the dense factorization
   int pcg_max_iterations;

@@ -1304,11 +1304,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_chol_step(DevPl
 // their loads in flight together.  Per element the arithmetic is exactly
 // that of k_chol_step (same tile routines, same order of updates), so both
 // schedules give the same bits.  Every wait is bounded: a CTA that sees
-// nothing ready for kDfSpinLimit polls records a timeout and leaves; a
+// nothing ready for DevPlan::df_spin_limit polls records a timeout and leaves; a
 // failed pivot or a timeout raises the abort word, which every waiting CTA
 // checks.
 constexpr int kDfThreads = 256;
-constexpr long long kDfSpinLimit = 1LL << 22;
 
 template <typename T>
 __host__ __device__ constexpr int df_batch() { return 2; }
@@ -1495,7 +1494,7 @@ __global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
         // the abort word is read every 16th idle round, the limit counted always
         if ((++idle & 15) == 0 && ld_acquire_u32(d.df_sync + 2) == epoch) {
           mode = kExit;
-        } else if (idle > kDfSpinLimit) {
+        } else if (idle > d.df_spin_limit) {
           d.factor_flag[p] = 2;                       // timed out
           __threadfence();
           atomicExch(d.df_sync + 2, epoch);

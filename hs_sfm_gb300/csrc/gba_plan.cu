@@ -609,6 +609,13 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     if (dataflow_layout(max_nt, mixed, device, &grid, &mo, &own_off, &own)) {
       D.df_grid = grid;
       D.df_max_own = mo;
+      // bounded waits: a CTA that finds nothing ready for this many polls
+      // records GBA_ERR_TIMEOUT; GBA_DF_SPIN_LIMIT lowers it to test that path
+      D.df_spin_limit = 1LL << 22;
+      if (const char* sl = std::getenv("GBA_DF_SPIN_LIMIT")) {
+        const long long v = std::atoll(sl);
+        if (v > 0) D.df_spin_limit = v;
+      }
       D.df_own_off = arena.upload(own_off);
       D.df_own = arena.upload(own);
       D.df_flags = arena.alloc<unsigned>(size_t(max_nt) * max_nt);

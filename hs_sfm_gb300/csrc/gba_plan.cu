@@ -21,6 +21,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace gba {
@@ -39,6 +40,27 @@ std::atomic<long long> g_launches{0};
                                                       : GBA_ERR_CUDA};      \
     }                                                                       \
   } while (0)
+
+// Runs f(begin, end, t) over [0, n) split into contiguous pieces, piece t
+// in thread t (piece 0 in the calling thread).  cuts, if given, are the
+// piece boundaries; otherwise the pieces are equal.
+template <typename F>
+void host_parallel(int64_t n, int threads, F f, const std::vector<int64_t>* cuts = nullptr) {
+  if (threads <= 1 || n <= 1) {
+    f(int64_t(0), n, 0);
+    return;
+  }
+  std::vector<std::thread> pool;
+  auto lo = [&](int t) { return cuts ? (*cuts)[t] : n * t / threads; };
+  for (int t = 1; t < threads; ++t) pool.emplace_back([&, t] { f(lo(t), lo(t + 1), t); });
+  f(lo(0), lo(1), 0);
+  for (auto& th : pool) th.join();
+}
+
+int host_threads() {
+  const unsigned hw = std::thread::hardware_concurrency();
+  return int(std::max(1u, std::min(hw, 16u)));
+}
 
 int64_t params_per_camera(uint32_t m) {
   return ((m & GBA_COMPUTE_RADIAL_DISTORTION) ? 3 : 0) +
@@ -212,6 +234,14 @@ int validate(const gba_problem& p, bool pcg) {
 int Plan::build(const gba_problem* problems, const double* const* near_ys, int nprob,
                 const gba_options* options) {
   auto t0 = std::chrono::steady_clock::now();
+  // GBA_BUILD_TIMING=1 prints the host build's phases to stderr
+  const bool timing = std::getenv("GBA_BUILD_TIMING") != nullptr;
+  std::vector<std::pair<const char*, double>> phases;
+  auto phase = [&](const char* name) {
+    if (timing)
+      phases.emplace_back(name, std::chrono::duration<double, std::milli>(
+                                    std::chrono::steady_clock::now() - t0).count());
+  };
   opt = *options;
   B = nprob;
   device = opt.device;
@@ -238,6 +268,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     if (err) return err;
     if (!near_ys || !near_ys[q]) return GBA_ERR_INVALID;
   }
+  phase("validate");
   // ---- global sizes
   int64_t P = 0, I = 0, K = 0, C = 0;
   for (int q = 0; q < nprob; ++q) {
@@ -318,42 +349,59 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       std::vector<int> cur(cnt.begin(), cnt.end() - 1);
       for (int k = 0; k < nk; ++k) order[cur[p.feature_maps[2 * k + 1]]++] = k;
     }
-    for (int i = 0; i < np; ++i) {
-      std::sort(order.begin() + cnt[i], order.begin() + cnt[i + 1], [&](int a, int b) {
-        return p.feature_maps[2 * a] < p.feature_maps[2 * b];
+    {
+      const int nth = nk > 200000 ? host_threads() : 1;
+      std::vector<char> dup(nth, 0);
+      host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
+        for (int64_t i = i0; i < i1; ++i) {
+          std::sort(order.begin() + cnt[i], order.begin() + cnt[i + 1], [&](int a, int b) {
+            return p.feature_maps[2 * a] < p.feature_maps[2 * b];
+          });
+          for (int u = cnt[i] + 1; u < cnt[i + 1]; ++u)
+            if (p.feature_maps[2 * order[u]] == p.feature_maps[2 * order[u - 1]]) dup[t] = 1;
+        }
       });
-      for (int t = cnt[i] + 1; t < cnt[i + 1]; ++t)
-        if (p.feature_maps[2 * order[t]] == p.feature_maps[2 * order[t - 1]]) return GBA_ERR_DUPLICATE;
+      for (char v : dup)
+        if (v) return GBA_ERR_DUPLICATE;
     }
     key_sorted_to_orig[q] = order;
     const double* y = near_ys[q];
-    for (int t = 0; t < nk; ++t) {
-      const int k = order[t];
-      key_img[kb + t] = int(ib + p.feature_maps[2 * k]);
-      key_pt[kb + t] = int(pb + p.feature_maps[2 * k + 1]);
-      key_obs[kb + t] = make_double2(y[2 * k], y[2 * k + 1]);
-      if (any_weights) {
-        double l00 = 1, l10 = 0, l11 = 1;
-        if (p.key_covariance_inverse) {
-          const double* L = p.key_covariance_inverse + 4 * k;
-          double a = L[0], bb = 0.5 * (L[1] + L[2]), dd = L[3];
-          if (!(a > 0)) return GBA_ERR_INVALID;
-          l00 = std::sqrt(a);
-          l10 = bb / l00;
-          double r = dd - l10 * l10;
-          if (!(r > 0)) return GBA_ERR_INVALID;
-          l11 = std::sqrt(r);
+    {
+      const int nth = nk > 200000 ? host_threads() : 1;
+      std::vector<char> bad(nth, 0);
+      host_parallel(nk, nth, [&](int64_t t0_, int64_t t1_, int th) {
+        for (int64_t t = t0_; t < t1_; ++t) {
+          const int k = order[t];
+          key_img[kb + t] = int(ib + p.feature_maps[2 * k]);
+          key_pt[kb + t] = int(pb + p.feature_maps[2 * k + 1]);
+          key_obs[kb + t] = make_double2(y[2 * k], y[2 * k + 1]);
+          if (any_weights) {
+            double l00 = 1, l10 = 0, l11 = 1;
+            if (p.key_covariance_inverse) {
+              const double* L = p.key_covariance_inverse + 4 * k;
+              double a = L[0], bb = 0.5 * (L[1] + L[2]), dd = L[3];
+              if (!(a > 0)) { bad[th] = 1; continue; }
+              l00 = std::sqrt(a);
+              l10 = bb / l00;
+              double r = dd - l10 * l10;
+              if (!(r > 0)) { bad[th] = 1; continue; }
+              l11 = std::sqrt(r);
+            }
+            key_wl[3 * (kb + t)] = l00;
+            key_wl[3 * (kb + t) + 1] = l10;
+            key_wl[3 * (kb + t) + 2] = l11;
+          }
         }
-        key_wl[3 * (kb + t)] = l00;
-        key_wl[3 * (kb + t) + 1] = l10;
-        key_wl[3 * (kb + t) + 2] = l11;
-      }
+      });
+      for (char v : bad)
+        if (v) return GBA_ERR_INVALID;
     }
     for (int i = 0; i < np; ++i) {
       pt_key_off[pb + i + 1] = int(kb + cnt[i + 1]);
       pt_prob[pb + i] = q;
     }
     pt_key_off[pb] = int(kb);
+    phase("keys");
     // per-image key lists (by point, since keys are point-major)
     {
       std::vector<int> ic(ni + 1, 0);
@@ -372,22 +420,37 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         img_item_off.push_back(int(img_items.size()));
       }
     }
+    phase("images");
     // reduced-system blocks: (i <= j) with their key pairs, point order
     {
-      std::vector<long long> bcount((size_t)ni * ni, 0);  // index j*ni + i? use (lo*ni + hi)
-      for (int i = 0; i < np; ++i) {
-        const int b0 = cnt[i], b1 = cnt[i + 1];
-        for (int a = b0; a < b1; ++a) {
-          const int ia = key_img[kb + a] - int(ib);
-          for (int c = a; c < b1; ++c) {
-            const int ic2 = key_img[kb + c] - int(ib);
-            bcount[(size_t)ia * ni + ic2]++;
+      // pairs are counted and placed by point ranges in parallel: each piece
+      // counts its pairs per image pair, a piece's pairs of a block follow
+      // those of the pieces before it, so every block lists its pairs in
+      // point order whatever the number of pieces
+      const size_t nn = (size_t)ni * ni;
+      int nth = nk > 200000 ? host_threads() : 1;
+      while (nth > 1 && nn * size_t(nth) * sizeof(int) > (size_t(256) << 20)) --nth;
+      std::vector<int64_t> cuts(nth + 1, np);
+      for (int t = 0; t < nth; ++t)   // pieces of about equal key counts
+        cuts[t] = std::lower_bound(cnt.begin(), cnt.end() - 1, int((int64_t)nk * t / nth)) - cnt.begin();
+      cuts[0] = 0;
+      std::vector<std::vector<int>> cnt_t(nth, std::vector<int>(nn, 0));
+      host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
+        int* bc = cnt_t[t].data();
+        for (int64_t i = i0; i < i1; ++i) {
+          const int b0 = cnt[i], b1 = cnt[i + 1];
+          for (int a = b0; a < b1; ++a) {
+            const size_t row = (size_t)(key_img[kb + a] - int(ib)) * ni;
+            for (int c = a; c < b1; ++c) bc[row + key_img[kb + c] - int(ib)]++;
           }
         }
-      }
+      }, &cuts);
+      std::vector<long long> bcount(nn, 0);
+      for (int t = 0; t < nth; ++t)
+        for (size_t e = 0; e < nn; ++e) bcount[e] += cnt_t[t][e];
       // every image gets a diagonal block (so S keeps U_i + mu I even for an
       // image without keys)
-      std::vector<int> bid((size_t)ni * ni, -1);
+      std::vector<int> bid(nn, -1);
       const int block_begin = int(blk_ij.size());
       std::vector<long long> boff;
       long long pair_base = (long long)pairs.size();
@@ -403,20 +466,31 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         }
       const int nblk = int(blk_ij.size()) - block_begin;
       if (acc > INT32_MAX) return GBA_ERR_INVALID;
-      pairs.resize(acc);
-      std::vector<long long> cur(boff);
-      for (int i = 0; i < np; ++i) {
-        const int b0 = cnt[i], b1 = cnt[i + 1];
-        for (int a = b0; a < b1; ++a) {
-          const int ia = key_img[kb + a] - int(ib);
-          for (int c = a; c < b1; ++c) {
-            const int ic2 = key_img[kb + c] - int(ib);
-            const int blk = bid[(size_t)ia * ni + ic2] - block_begin;
-            // a pair of a diagonal block is a key with itself: carry its point instead
-            pairs[cur[blk]++] = make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
-          }
+      // cnt_t[t][e] becomes piece t's first slot in block e
+      for (size_t e = 0; e < nn; ++e) {
+        if (bid[e] < 0) continue;
+        long long o = boff[bid[e] - block_begin];
+        for (int t = 0; t < nth; ++t) {
+          const int c_ = cnt_t[t][e];
+          cnt_t[t][e] = int(o);
+          o += c_;
         }
       }
+      pairs.resize(acc);
+      host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
+        int* slot = cnt_t[t].data();
+        for (int64_t i = i0; i < i1; ++i) {
+          const int b0 = cnt[i], b1 = cnt[i + 1];
+          for (int a = b0; a < b1; ++a) {
+            const size_t row = (size_t)(key_img[kb + a] - int(ib)) * ni;
+            for (int c = a; c < b1; ++c) {
+              // a pair of a diagonal block is a key with itself: carry its point instead
+              pairs[slot[row + key_img[kb + c] - int(ib)]++] =
+                  make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
+            }
+          }
+        }
+      }, &cuts);
       pi.block_begin = block_begin;
       pi.num_blocks = nblk;
       pi.item_begin = int(items.size());
@@ -440,6 +514,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
             blk_map[blk_map_off[q] + (size_t)a * ni + c] = bid[(size_t)a * ni + c];
       }
     }
+    phase("blocks+pairs");
     // work chunks
     for (int s = 0; s < nk; s += kKeyChunk)
       key_chunks.push_back(Chunk{q, int(kb + s), int(kb + std::min(nk, s + kKeyChunk)), 0});
@@ -483,6 +558,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     cb += p.number_of_cameras;
   }
 
+  phase("host structure");
   // ---- device allocations
   DevPlan& D = d;
   D.B = nprob;
@@ -678,8 +754,17 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.img_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(img_chunks.size(), 1));
   D.launch_counter = nullptr;
   GBA_CUDA(cudaMemsetAsync(D.state, 0, sizeof(LMState) * nprob, stream));
+  phase("uploads issued");
   GBA_CUDA(cudaStreamSynchronize(stream));
+  phase("uploads done");
   setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (timing) {
+    double prev = 0;
+    for (const auto& ph : phases) {
+      std::fprintf(stderr, "gba build: %-16s %8.2f ms (+%.2f)\n", ph.first, ph.second, ph.second - prev);
+      prev = ph.second;
+    }
+  }
   return GBA_OK;
 }
 

@@ -306,19 +306,20 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   key_sorted_to_orig.resize(nprob);
   x_size.resize(nprob);
 
-  int64_t pb = 0, ib = 0, kb = 0, cb = 0;
+  // ---- per-problem bases
+  std::vector<int64_t> pbase(nprob + 1, 0), ibase(nprob + 1, 0), kbase(nprob + 1, 0),
+      cbase(nprob + 1, 0);
   long long s_off = 0;
   int max_n = 0, max_nt = 0;
   for (int q = 0; q < nprob; ++q) {
     const gba_problem& p = problems[q];
     const int np = int(p.number_of_points), ni = int(p.number_of_images), nk = int(p.number_of_keys);
-    const int64_t cps = params_per_camera(p.intrinsic_computations_mask);
     ProbInfo& pi = prob[q];
-    pi.point_begin = int(pb);
+    pi.point_begin = int(pbase[q]);
     pi.num_points = np;
-    pi.image_begin = int(ib);
+    pi.image_begin = int(ibase[q]);
     pi.num_images = ni;
-    pi.key_begin = int(kb);
+    pi.key_begin = int(kbase[q]);
     pi.num_keys = nk;
     pi.n = 6 * ni;
     pi.nt = (pi.n + kTile - 1) / kTile;
@@ -327,6 +328,34 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     max_n = std::max(max_n, pi.n);
     max_nt = std::max(max_nt, pi.nt);
     x_size[q] = 3LL * np + 6LL * ni;
+    pbase[q + 1] = pbase[q] + np;
+    ibase[q + 1] = ibase[q] + ni;
+    kbase[q + 1] = kbase[q] + nk;
+    cbase[q + 1] = cbase[q] + p.number_of_cameras;
+  }
+
+  // ---- each problem's structure: the per-key, per-point and per-image
+  // arrays are written in place (disjoint ranges), the appended lists go to
+  // a piece per problem; problems are built in parallel, or one problem's
+  // points in parallel when there is only one
+  struct Piece {
+    int err = GBA_OK;
+    std::vector<int4> img_items;       // image reduction items, image order
+    std::vector<int> img_item_cnt;     // items per image
+    std::vector<int2> pairs;           // key pairs of every block, block order
+    std::vector<int2> blk_ij;          // (i, j) local image ids, i <= j
+    std::vector<long long> blk_off;    // [nblk + 1] first pair of each block
+    std::vector<int> blk_map;          // [ni * ni] local block id or -1 (dense solver)
+    std::vector<int4> cons;
+    std::vector<double2> cons_yw;
+  };
+  std::vector<Piece> pieces(nprob);
+  auto build_one = [&](int q, int inner) {
+    Piece& out = pieces[q];
+    const gba_problem& p = problems[q];
+    const int np = int(p.number_of_points), ni = int(p.number_of_images), nk = int(p.number_of_keys);
+    const int64_t cps = params_per_camera(p.intrinsic_computations_mask);
+    const int64_t pb = pbase[q], ib = ibase[q], kb = kbase[q], cb = cbase[q];
     // cameras
     for (int64_t c = 0; c < p.number_of_cameras; ++c) {
       double full[10];
@@ -349,10 +378,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       std::vector<int> cur(cnt.begin(), cnt.end() - 1);
       for (int k = 0; k < nk; ++k) order[cur[p.feature_maps[2 * k + 1]]++] = k;
     }
+    const int nth0 = nk > 200000 ? inner : 1;
     {
-      const int nth = nk > 200000 ? host_threads() : 1;
-      std::vector<char> dup(nth, 0);
-      host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
+      std::vector<char> dup(nth0, 0);
+      host_parallel(np, nth0, [&](int64_t i0, int64_t i1, int t) {
         for (int64_t i = i0; i < i1; ++i) {
           std::sort(order.begin() + cnt[i], order.begin() + cnt[i + 1], [&](int a, int b) {
             return p.feature_maps[2 * a] < p.feature_maps[2 * b];
@@ -362,14 +391,15 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         }
       });
       for (char v : dup)
-        if (v) return GBA_ERR_DUPLICATE;
+        if (v) {
+          out.err = GBA_ERR_DUPLICATE;
+          return;
+        }
     }
-    key_sorted_to_orig[q] = order;
     const double* y = near_ys[q];
     {
-      const int nth = nk > 200000 ? host_threads() : 1;
-      std::vector<char> bad(nth, 0);
-      host_parallel(nk, nth, [&](int64_t t0_, int64_t t1_, int th) {
+      std::vector<char> bad(nth0, 0);
+      host_parallel(nk, nth0, [&](int64_t t0_, int64_t t1_, int th) {
         for (int64_t t = t0_; t < t1_; ++t) {
           const int k = order[t];
           key_img[kb + t] = int(ib + p.feature_maps[2 * k]);
@@ -394,14 +424,16 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         }
       });
       for (char v : bad)
-        if (v) return GBA_ERR_INVALID;
+        if (v) {
+          out.err = GBA_ERR_INVALID;
+          return;
+        }
     }
-    for (int i = 0; i < np; ++i) {
+    key_sorted_to_orig[q] = std::move(order);
+    for (int i = 0; i < np; ++i) {   // entry pb is set by the caller
       pt_key_off[pb + i + 1] = int(kb + cnt[i + 1]);
       pt_prob[pb + i] = q;
     }
-    pt_key_off[pb] = int(kb);
-    phase("keys");
     // per-image key lists (by point, since keys are point-major)
     {
       std::vector<int> ic(ni + 1, 0);
@@ -412,23 +444,24 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         int li = key_img[kb + t] - int(ib);
         img_keys[kb + cur[li]++] = int(kb + t);
       }
-      for (int i = 0; i <= ni; ++i) img_key_off[ib + i] = int(kb + ic[i]);
+      for (int i = 1; i <= ni; ++i) img_key_off[ib + i] = int(kb + ic[i]);   // entry ib: the caller
+      out.img_item_cnt.assign(ni, 0);
       for (int i = 0; i < ni; ++i) {
-        const int q0 = img_key_off[ib + i], q1 = img_key_off[ib + i + 1];
-        for (int qq = q0; qq < q1; qq += kImageItem)
-          img_items.push_back(make_int4(int(ib + i), qq, std::min(q1, qq + kImageItem), q));
-        img_item_off.push_back(int(img_items.size()));
+        const int q0 = int(kb + ic[i]), q1 = int(kb + ic[i + 1]);
+        for (int qq = q0; qq < q1; qq += kImageItem) {
+          out.img_items.push_back(make_int4(int(ib + i), qq, std::min(q1, qq + kImageItem), q));
+          out.img_item_cnt[i]++;
+        }
       }
     }
-    phase("images");
-    // reduced-system blocks: (i <= j) with their key pairs, point order
+    // reduced-system blocks: (i <= j) with their key pairs, point order.
+    // Pairs are counted and placed by point ranges in parallel: each piece
+    // counts its pairs per image pair, a piece's pairs of a block follow
+    // those of the pieces before it, so every block lists its pairs in
+    // point order whatever the number of pieces.
     {
-      // pairs are counted and placed by point ranges in parallel: each piece
-      // counts its pairs per image pair, a piece's pairs of a block follow
-      // those of the pieces before it, so every block lists its pairs in
-      // point order whatever the number of pieces
       const size_t nn = (size_t)ni * ni;
-      int nth = nk > 200000 ? host_threads() : 1;
+      int nth = nth0;
       while (nth > 1 && nn * size_t(nth) * sizeof(int) > (size_t(256) << 20)) --nth;
       std::vector<int64_t> cuts(nth + 1, np);
       for (int t = 0; t < nth; ++t)   // pieces of about equal key counts
@@ -451,32 +484,32 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       // every image gets a diagonal block (so S keeps U_i + mu I even for an
       // image without keys)
       std::vector<int> bid(nn, -1);
-      const int block_begin = int(blk_ij.size());
-      std::vector<long long> boff;
-      long long pair_base = (long long)pairs.size();
-      long long acc = pair_base;
+      long long acc = 0;
       for (int a = 0; a < ni; ++a)
         for (int c = a; c < ni; ++c) {
           const long long n_ = bcount[(size_t)a * ni + c];
           if (n_ == 0 && a != c) continue;
-          bid[(size_t)a * ni + c] = int(blk_ij.size());
-          blk_ij.push_back(make_int2(a, c));
-          boff.push_back(acc);
+          bid[(size_t)a * ni + c] = int(out.blk_ij.size());
+          out.blk_ij.push_back(make_int2(a, c));
+          out.blk_off.push_back(acc);
           acc += n_;
         }
-      const int nblk = int(blk_ij.size()) - block_begin;
-      if (acc > INT32_MAX) return GBA_ERR_INVALID;
+      out.blk_off.push_back(acc);
+      if (acc > INT32_MAX) {
+        out.err = GBA_ERR_INVALID;
+        return;
+      }
       // cnt_t[t][e] becomes piece t's first slot in block e
       for (size_t e = 0; e < nn; ++e) {
         if (bid[e] < 0) continue;
-        long long o = boff[bid[e] - block_begin];
+        long long o = out.blk_off[bid[e]];
         for (int t = 0; t < nth; ++t) {
           const int c_ = cnt_t[t][e];
           cnt_t[t][e] = int(o);
           o += c_;
         }
       }
-      pairs.resize(acc);
+      out.pairs.resize(acc);
       host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
         int* slot = cnt_t[t].data();
         for (int64_t i = i0; i < i1; ++i) {
@@ -485,46 +518,15 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
             const size_t row = (size_t)(key_img[kb + a] - int(ib)) * ni;
             for (int c = a; c < b1; ++c) {
               // a pair of a diagonal block is a key with itself: carry its point instead
-              pairs[slot[row + key_img[kb + c] - int(ib)]++] =
+              out.pairs[slot[row + key_img[kb + c] - int(ib)]++] =
                   make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
             }
           }
         }
       }, &cuts);
-      pi.block_begin = block_begin;
-      pi.num_blocks = nblk;
-      pi.item_begin = int(items.size());
-      for (int t = 0; t < nblk; ++t) {
-        const long long s0 = boff[t], s1 = (t + 1 < nblk) ? boff[t + 1] : acc;
-        long long s = s0;
-        do {
-          long long e = std::min(s1, s + kPairItem);
-          items.push_back(make_int4(block_begin + t, int(s), int(e), q));
-          s = e;
-        } while (s < s1);
-        blk_item_off.push_back(int(items.size()));
-      }
-      pi.num_items = int(items.size()) - pi.item_begin;
       // dense map for the assembly of the lower triangle: map[j*ni + i], j <= i
-      blk_map_off[q] = (long long)blk_map.size();
-      if (!pcg) {
-        blk_map.resize(blk_map.size() + (size_t)ni * ni, -1);
-        for (int a = 0; a < ni; ++a)
-          for (int c = a; c < ni; ++c)
-            blk_map[blk_map_off[q] + (size_t)a * ni + c] = bid[(size_t)a * ni + c];
-      }
+      if (!pcg) out.blk_map.swap(bid);
     }
-    phase("blocks+pairs");
-    // work chunks
-    for (int s = 0; s < nk; s += kKeyChunk)
-      key_chunks.push_back(Chunk{q, int(kb + s), int(kb + std::min(nk, s + kKeyChunk)), 0});
-    prob_key_chunk_off.push_back(int(key_chunks.size()));
-    for (int s = 0; s < np; s += kPointChunk)
-      pt_chunks.push_back(Chunk{q, int(pb + s), int(pb + std::min(np, s + kPointChunk)), 0});
-    prob_pt_chunk_off.push_back(int(pt_chunks.size()));
-    for (int s = 0; s < ni; s += kImageChunk)
-      img_chunks.push_back(Chunk{q, int(ib + s), int(ib + std::min(ni, s + kImageChunk)), 0});
-    prob_img_chunk_off.push_back(int(img_chunks.size()));
     // soft constraints on points and images, in y order
     // (camera_shared_vector_function.hpp:483-629): the rows after the keys,
     // each a copy of one parameter with its own weight; camera constraints
@@ -532,9 +534,9 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     {
       int64_t r = 0;
       auto add = [&](int group, int64_t index, int param) {
-        cons.push_back(make_int4(group, int(index), param, q));
-        cons_yw.push_back(make_double2(y[2LL * nk + r],
-                                       p.constraint_weights ? p.constraint_weights[r] : 1.0));
+        out.cons.push_back(make_int4(group, int(index), param, q));
+        out.cons_yw.push_back(make_double2(y[2LL * nk + r],
+                                           p.constraint_weights ? p.constraint_weights[r] : 1.0));
         ++r;
       };
       for (int64_t c = 0; c < p.number_of_point_constraints; ++c) {
@@ -550,13 +552,75 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Y) add(1, ib + ic.image_id, 4);
         if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Z) add(1, ib + ic.image_id, 5);
       }
-      prob_cons_off.push_back(int(cons.size()));
     }
-    pb += np;
-    ib += ni;
-    kb += nk;
-    cb += p.number_of_cameras;
+  };
+  if (nprob == 1) {
+    build_one(0, host_threads());
+  } else {
+    const int nth = std::min(host_threads(), nprob);
+    std::atomic<int> next{0};
+    host_parallel(nth, nth, [&](int64_t, int64_t, int) {
+      for (int q = next++; q < nprob; q = next++) build_one(q, 1);
+    });
   }
+  for (int q = 0; q < nprob; ++q)
+    if (pieces[q].err) return pieces[q].err;
+  phase("problems");
+
+  // ---- concatenation in problem order
+  for (int q = 0; q < nprob; ++q) {
+    Piece& pc = pieces[q];
+    ProbInfo& pi = prob[q];
+    const gba_problem& p = problems[q];
+    const int np = int(p.number_of_points), ni = int(p.number_of_images), nk = int(p.number_of_keys);
+    const int64_t pb = pbase[q], ib = ibase[q], kb = kbase[q];
+    pt_key_off[pb] = int(kb);
+    img_key_off[ib] = int(kb);
+    for (int i = 0, t = 0; i < ni; ++i) {
+      for (int u = 0; u < pc.img_item_cnt[i]; ++u) img_items.push_back(pc.img_items[t++]);
+      img_item_off.push_back(int(img_items.size()));
+    }
+    const int block_begin = int(blk_ij.size());
+    const long long pair_base = (long long)pairs.size();
+    if (pair_base + (long long)pc.pairs.size() > INT32_MAX) return GBA_ERR_INVALID;
+    pairs.insert(pairs.end(), pc.pairs.begin(), pc.pairs.end());
+    blk_ij.insert(blk_ij.end(), pc.blk_ij.begin(), pc.blk_ij.end());
+    const int nblk = int(pc.blk_ij.size());
+    pi.block_begin = block_begin;
+    pi.num_blocks = nblk;
+    pi.item_begin = int(items.size());
+    for (int t = 0; t < nblk; ++t) {
+      const long long s0 = pair_base + pc.blk_off[t], s1 = pair_base + pc.blk_off[t + 1];
+      long long s = s0;
+      do {
+        long long e = std::min(s1, s + kPairItem);
+        items.push_back(make_int4(block_begin + t, int(s), int(e), q));
+        s = e;
+      } while (s < s1);
+      blk_item_off.push_back(int(items.size()));
+    }
+    pi.num_items = int(items.size()) - pi.item_begin;
+    blk_map_off[q] = (long long)blk_map.size();
+    if (!pcg)
+      for (int v : pc.blk_map) blk_map.push_back(v >= 0 ? v + block_begin : -1);
+    // work chunks
+    for (int s = 0; s < nk; s += kKeyChunk)
+      key_chunks.push_back(Chunk{q, int(kb + s), int(kb + std::min(nk, s + kKeyChunk)), 0});
+    prob_key_chunk_off.push_back(int(key_chunks.size()));
+    for (int s = 0; s < np; s += kPointChunk)
+      pt_chunks.push_back(Chunk{q, int(pb + s), int(pb + std::min(np, s + kPointChunk)), 0});
+    prob_pt_chunk_off.push_back(int(pt_chunks.size()));
+    for (int s = 0; s < ni; s += kImageChunk)
+      img_chunks.push_back(Chunk{q, int(ib + s), int(ib + std::min(ni, s + kImageChunk)), 0});
+    prob_img_chunk_off.push_back(int(img_chunks.size()));
+    cons.insert(cons.end(), pc.cons.begin(), pc.cons.end());
+    cons_yw.insert(cons_yw.end(), pc.cons_yw.begin(), pc.cons_yw.end());
+    prob_cons_off.push_back(int(cons.size()));
+    std::vector<int>().swap(pc.blk_map);   // release as we go
+    std::vector<int2>().swap(pc.pairs);
+  }
+  pt_key_off[P] = int(K);
+  img_key_off[I] = int(K);
 
   phase("host structure");
   // ---- device allocations

@@ -21,6 +21,7 @@ namespace gba {
 constexpr int kTile = 32;          // dense Cholesky tile
 constexpr int kDfTraceCap = 1024;   // traced tasks per CTA of the dataflow factorization
 constexpr int kPcgSlots = 8;        // PCG partial sums per image chunk
+constexpr int kImgCamVals = 128;   // per image item: E (6x10), U_c upper (55), g_c (10), pad
 constexpr int kKeyChunk = 1024;    // keys per cost work chunk
 constexpr int kPointChunk = 128;   // points per point work chunk
 constexpr int kImageChunk = 8;     // images per image work chunk (backsub)
@@ -56,11 +57,15 @@ struct ProbInfo {
   int point_begin, num_points;
   int image_begin, num_images;
   int key_begin, num_keys;
-  int n;              // reduced system size = 6 * num_images
+  int n;              // reduced system size = 6 * num_ext
   int nt;             // number of kTile tiles of the reduced system
   long long s_off;    // offset of the n x n dense system (row-major)
   int item_begin, num_items;
   int block_begin, num_blocks;
+  // reduced-system "images": the real images, then, with free cameras, nc
+  // 6-wide parts of each camera's parameters (zero-padded past cps)
+  int ext_begin, num_ext;
+  int cam_begin, num_cams, cps, nc;
 };
 
 struct Chunk {       // a contiguous range of one problem's entities
@@ -100,8 +105,8 @@ struct DevPlan {
   const int4* img_items;     // (image, q begin, q end, prob), <= kImageItem keys
   const int* img_item_off;   // [I+1] items of each image
   double* img_item_partial;  // [items * 28]
-  const double* cam64;       // [C*10]  k1 k2 k3 d1 d2 f s cx cy a
-  const float* cam32;        // [C*10]
+  double* cam64[2];          // [C*10]  k1 k2 k3 d1 d2 f s cx cy a, by parity
+  float* cam32[2];           // [C*10]  (both parities the same array while cameras are fixed)
   // parameters (double buffered by LMState::parity)
   double* x_pt[2];           // [3P]
   double* x_img[2];          // [6I]
@@ -111,7 +116,7 @@ struct DevPlan {
   float2* img_rot_ff[2];     // [12I] double-float mirror (mixed path) or null
   float2* x_ff[2];           // [3P] double-float mirror of x_pt (mixed path) or null
   const float2* key_obs_ff;  // [2K] double-float keys (mixed path) or null
-  const float2* cam_ff;      // [10C] double-float cameras, [9] = f * a (mixed path)
+  float2* cam_ff[2];         // [10C] double-float cameras, [9] = f * a (mixed path), by parity
   void* img_lin[2];          // [12I] T: r(3) t(3) ct s c a1 a2 pad
   // per key
   void* RW[2];               // [4K] T: rw0 rw1 sqrt(w) pad  (whitened, weighted residual)
@@ -170,9 +175,32 @@ struct DevPlan {
   const int* prob_pt_chunk_off;   // [B+1]
   const int* prob_img_chunk_off;  // [B+1]
   double* key_chunk_sum;          // [2 * n_key_chunks] cost, sum of squared plain residuals
+  // free cameras (camera parameters are unknowns; dense solver).  Camera
+  // parameters are kept in the problem's order (the first cps of 10 per
+  // camera); Jacobians and the per-image sums use all ten columns
+  // [k1 k2 k3 d1 d2 f s cx cy a] and pick the computed ones.
+  int free_cams;
+  int Ctot;                       // cameras of the plan
+  int R;                          // camera records (Z records K .. K+R-1)
+  int I_ext;                      // reduced-system images of the plan
+  const int* img_ext;             // [I] reduced-system index of each image
+  const int4* cam_info;           // [Ctot] (cps if free else 0, mask, problem, ext index of part 0)
+  const int* cam_img_off;         // [Ctot + 1] into cam_imgs
+  const int* cam_imgs;            // images of each camera, ascending
+  const int* prob_cam_off;        // [B + 1] cameras of each problem
+  double* x_cam[2];               // [10 * Ctot] by parity
+  double* x0_cam;
+  void* JC;                       // T: [20 K] camera Jacobian, 2 rows x 10 (all parameters)
+  const int* pt_rec_off;          // [P + 1] camera records of each point (indices >= K)
+  const int2* rec_info;           // [R] (global camera, ext index)
+  double* img_item_cam;           // [n_img_items * kImgCamVals] partial sums of image items
+  double* Ei;                     // [60 I] J_i^T J_c per image (full columns)
+  double* Uc;                     // [100 Ctot] camera normal block, cps x cps, row stride 10
+  double* gc;                     // [10 Ctot]
+  double* cam_sum;                // [3 Ctot] dn2, xn2, g^T d of the camera step
   // soft constraints on points and images (rows of y after the keys)
   int n_cons;
-  const int4* cons;               // (group 0 point / 1 image, global index, parameter, problem)
+  const int4* cons;               // (group 0 point / 1 image / 2 camera, global index, parameter, problem)
   const double2* cons_yw;         // (observed value, weight)
   const int* pt_cons_off;         // [P + 1] into cons_by_pt, or null without constraints
   const int* cons_by_pt;
@@ -220,6 +248,6 @@ int launch_ctrl_accept(const DevPlan& d, cudaStream_t s);
 // Stage entry points on a plan (gba_kernels.cu): Jacobian blocks in sorted
 // key order (T precision), vector function (FP64).
 int launch_vector_function(const DevPlan& d, double* y_sorted, cudaStream_t s);
-int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, cudaStream_t s);
+int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, double* jc, cudaStream_t s);
 
 }  // namespace gba

@@ -266,7 +266,8 @@ __device__ __forceinline__ void project64(const double* R, const double* X, cons
 // (:431-470), DecenteringDistortDerivation (:472-503) and the intrinsic
 // chains (:505-524).
 template <typename T>
-__device__ __forceinline__ void key_jacobian(const T* X, const T* IL, const T* cam, T* jp, T* ji) {
+__device__ __forceinline__ void key_jacobian(const T* X, const T* IL, const T* cam, T* jp, T* ji,
+                                             T* nrm = nullptr) {
   const T r0 = IL[0], r1 = IL[1], r2 = IL[2];
   const T ct = IL[6], s = IL[7], c = IL[8], a1 = IL[9], a2 = IL[10];
   const T d = r0 * X[0] + r1 * X[1] + r2 * X[2];
@@ -295,6 +296,10 @@ __device__ __forceinline__ void key_jacobian(const T* X, const T* IL, const T* c
   pp[2][0] = -s * r1 + c * r2 * r0; pp[2][1] = s * r0 + c * r2 * r1; pp[2][2] = ct + c * r2 * r2;
   const T iz = T(1) / y2;
   const T n0 = y0 * iz, n1 = y1 * iz;
+  if (nrm) {
+    nrm[0] = n0;
+    nrm[1] = n1;
+  }
   // normalized-key derivatives A (2 x 9): columns 0..2 point, 3..8 image
   T A0[9], A1[9];
 #pragma unroll
@@ -337,17 +342,73 @@ template <typename T>
 __device__ __forceinline__ T* tptr_mut(void* p) { return static_cast<T*>(p); }
 
 template <typename T>
-__device__ __forceinline__ void load_cam(const DevPlan& d, int cam, T* out);
+__device__ __forceinline__ void load_cam(const DevPlan& d, int par, int cam, T* out);
 template <>
-__device__ __forceinline__ void load_cam<float>(const DevPlan& d, int cam, float* out) {
+__device__ __forceinline__ void load_cam<float>(const DevPlan& d, int par, int cam, float* out) {
 #pragma unroll
-  for (int j = 0; j < 10; ++j) out[j] = __ldg(d.cam32 + 10 * cam + j);
+  for (int j = 0; j < 10; ++j) out[j] = d.cam32[par][10 * cam + j];
 }
 template <>
-__device__ __forceinline__ void load_cam<double>(const DevPlan& d, int cam, double* out) {
+__device__ __forceinline__ void load_cam<double>(const DevPlan& d, int par, int cam, double* out) {
 #pragma unroll
-  for (int j = 0; j < 10; ++j) out[j] = __ldg(d.cam64 + 10 * cam + j);
+  for (int j = 0; j < 10; ++j) out[j] = d.cam64[par][10 * cam + j];
 }
+
+// Derivatives of the image key with respect to all ten camera parameters in
+// the full model's order [k1 k2 k3][d1 d2][f s cx cy a]
+// (camera_shared_analytical_jacobian_matrix_calculator.hpp:526-557), from the
+// undistorted normalized key n: row 0 (u) in jc[0..9], row 1 (v) in
+// jc[10..19].  Consumers pick the computed parameters' columns.
+template <typename T>
+__device__ __forceinline__ void camera_jacobian(T n0, T n1, const T* cam, T* jc) {
+  const T r2 = n0 * n0 + n1 * n1, r4 = r2 * r2, r6 = r4 * r2;
+  const T coeff = cam[0] * r2 + cam[1] * r4 + cam[2] * r6;
+  const T d1 = cam[3], d2 = cam[4];
+  const T e0 = n0 + coeff * n0 + (T(2) * d1 * n0 * n1 + d2 * (r2 + T(2) * n0 * n0));
+  const T e1 = n1 + coeff * n1 + (T(2) * d2 * n0 * n1 + d1 * (r2 + T(2) * n1 * n1));
+  const T f = cam[5], sk = cam[6], a = cam[9];
+  // distortion columns through K: u = f e0 + s e1 + cx, v = f a e1 + cy
+  const T de0[5] = {r2 * n0, r4 * n0, r6 * n0, T(2) * n0 * n1, r2 + T(2) * n0 * n0};
+  const T de1[5] = {r2 * n1, r4 * n1, r6 * n1, r2 + T(2) * n1 * n1, T(2) * n0 * n1};
+#pragma unroll
+  for (int m = 0; m < 5; ++m) {
+    jc[m] = f * de0[m] + sk * de1[m];
+    jc[10 + m] = f * a * de1[m];
+  }
+  jc[5] = e0;    jc[15] = a * e1;   // f
+  jc[6] = e1;    jc[16] = T(0);     // s
+  jc[7] = T(1);  jc[17] = T(0);     // cx
+  jc[8] = T(0);  jc[18] = T(1);     // cy
+  jc[9] = T(0);  jc[19] = f * e1;   // a
+}
+
+// Column of the full ten [k1 k2 k3 d1 d2 f s cx cy a] holding a camera's
+// computed parameter m, or -1 past its count.
+__host__ __device__ __forceinline__ int cam_full_col(unsigned mask, int m) {
+  if (mask & GBA_COMPUTE_RADIAL_DISTORTION) {
+    if (m < 3) return m;
+    m -= 3;
+  }
+  if (mask & GBA_COMPUTE_DECENTERING_DISTORTION) {
+    if (m < 2) return 3 + m;
+    m -= 2;
+  }
+  if ((mask & GBA_COMPUTE_INTRINSIC_PARAMS) && m < 5) return 5 + m;
+  return -1;
+}
+
+// The computed parameter held in full column j, or -1 when j is not computed.
+__device__ __forceinline__ int cam_compact_col(unsigned mask, int j) {
+  const int nr = (mask & GBA_COMPUTE_RADIAL_DISTORTION) ? 3 : 0;
+  const int nd = (mask & GBA_COMPUTE_DECENTERING_DISTORTION) ? 2 : 0;
+  if (j < 3) return nr ? j : -1;
+  if (j < 5) return nd ? nr + j - 3 : -1;
+  return (mask & GBA_COMPUTE_INTRINSIC_PARAMS) ? nr + nd + j - 5 : -1;
+}
+
+// Index of (a, b), a <= b, in the row-major upper triangle of a 10 x 10 block.
+__device__ __forceinline__ int upper10(int a, int b) { return 10 * a - a * (a - 1) / 2 + (b - a); }
+
 
 // ---------------------------------------------------------------------------
 // init / copy x0
@@ -370,12 +431,44 @@ __global__ void k_init(DevPlan d) {
 
 __global__ void k_copy_x0(DevPlan d) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  long long np = 3LL * d.P, ni = 6LL * d.I;
+  long long np = 3LL * d.P, ni = 6LL * d.I, nc = d.free_cams ? 10LL * d.Ctot : 0;
   if (i < np) {
     d.x_pt[0][i] = d.x0_pt[i];
     if (d.x_ff[0]) d.x_ff[0][i] = ff_split(d.x0_pt[i]);
   } else if (i < np + ni) {
     d.x_img[0][i - np] = d.x0_img[i - np];
+  } else if (i < np + ni + nc) {
+    d.x_cam[0][i - np - ni] = d.x0_cam[i - np - ni];
+  }
+}
+
+// Free cameras: the ten-parameter camera of x_cam (which = 0 current, 1
+// candidate) in every form the key kernels read.  Fixed cameras keep the
+// values uploaded at plan creation in both parities.
+__global__ void k_cam_prep(DevPlan d, int which) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.Ctot) return;
+  const int4 ci = d.cam_info[c];
+  if (ci.x == 0) return;
+  const LMState& st = d.state[ci.z];
+  if (which == 0 ? !st.active : !st.evaluate) return;
+  const int par = which ? 1 - st.parity : st.parity;
+  const double* x = d.x_cam[par] + 10LL * c;
+  double full[10] = {0, 0, 0, 0, 0, 1, 0, 0, 0, 1};
+#pragma unroll
+  for (int j = 0; j < 10; ++j) {
+    const int m = cam_compact_col(unsigned(ci.y), j);
+    if (m >= 0) full[j] = x[m];
+  }
+#pragma unroll
+  for (int j = 0; j < 10; ++j) {
+    d.cam64[par][10LL * c + j] = full[j];
+    d.cam32[par][10LL * c + j] = float(full[j]);
+  }
+  if (d.cam_ff[par]) {
+#pragma unroll
+    for (int j = 0; j < 9; ++j) d.cam_ff[par][10LL * c + j] = ff_split(full[j]);
+    d.cam_ff[par][10LL * c + 9] = ff_split(full[5] * full[9]);   // f * a
   }
 }
 
@@ -429,7 +522,9 @@ __global__ void __launch_bounds__(256) k_cons_cost(DevPlan d, int which) {
   for (int r = d.prob_cons_off[p] + threadIdx.x; r < d.prob_cons_off[p + 1]; r += blockDim.x) {
     const int4 c = d.cons[r];
     const double2 yw = d.cons_yw[r];
-    const double x = c.x == 0 ? d.x_pt[par][3LL * c.y + c.z] : d.x_img[par][6LL * c.y + c.z];
+    const double x = c.x == 0   ? d.x_pt[par][3LL * c.y + c.z]
+                     : c.x == 1 ? d.x_img[par][6LL * c.y + c.z]
+                                : d.x_cam[par][10LL * c.y + c.z];
     const double v = x - yw.x;
     acc += yw.y * v * v;
   }
@@ -460,7 +555,7 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
     double cam[10];
     const int ci = __ldg(d.img_cam + img);
 #pragma unroll
-    for (int j = 0; j < 10; ++j) cam[j] = __ldg(d.cam64 + 10 * ci + j);
+    for (int j = 0; j < 10; ++j) cam[j] = d.cam64[par][10 * ci + j];
     double u, v;
     project64(R, X, cam, u, v);
     const double2 ob = __ldg(d.key_obs + k);
@@ -517,7 +612,7 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
     }
     const ff iz = ff_rcp(y[2]);
     ff n0 = ff_mul(y[0], iz), n1 = ff_mul(y[1], iz);
-    const float2* cam = d.cam_ff + 10 * __ldg(d.img_cam + img);
+    const float2* cam = d.cam_ff[par] + 10 * __ldg(d.img_cam + img);
     const ff k1 = ff_ld(cam[0]), k2 = ff_ld(cam[1]), k3 = ff_ld(cam[2]);
     const ff d1 = ff_ld(cam[3]), d2 = ff_ld(cam[4]);
     const ff r2 = ff_add(ff_mul(n0, n0), ff_mul(n1, n1));
@@ -600,12 +695,32 @@ __global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
     T il[12];
     load_vec<12>(IL + 12LL * img, il);
     T cam[10];
-    load_cam<T>(d, __ldg(d.img_cam + img), cam);
-    T jp[6], ji[12];
-    key_jacobian<T>(X, il, cam, jp, ji);
+    const int ci = __ldg(d.img_cam + img);
+    load_cam<T>(d, par, ci, cam);
+    T jp[6], ji[12], nrm[2];
+    key_jacobian<T>(X, il, cam, jp, ji, nrm);
     T rw[4];
     load_vec<4>(rwb + 4LL * k, rw);
     const T sw = rw[2];
+    if (d.free_cams) {   // the camera block, whitened and weighted as the others
+      T jc[20];
+      camera_jacobian<T>(nrm[0], nrm[1], cam, jc);
+      T l00 = T(1), l10 = T(0), l11 = T(1);
+      if (d.key_wl) {
+        l00 = T(__ldg(d.key_wl + 3LL * k));
+        l10 = T(__ldg(d.key_wl + 3LL * k + 1));
+        l11 = T(__ldg(d.key_wl + 3LL * k + 2));
+      }
+#pragma unroll
+      for (int m = 0; m < 10; ++m) {
+        const T a = jc[m], b = jc[10 + m];
+        jc[m] = (l00 * a + l10 * b) * sw;
+        jc[10 + m] = l11 * b * sw;
+      }
+      T* out = tptr_mut<T>(d.JC) + 20LL * k;
+#pragma unroll
+      for (int m = 0; m < 20; ++m) out[m] = jc[m];
+    }
     if (d.key_wl) {
       const T l00 = T(__ldg(d.key_wl + 3LL * k)), l10 = T(__ldg(d.key_wl + 3LL * k + 1)),
               l11 = T(__ldg(d.key_wl + 3LL * k + 2));
@@ -794,6 +909,123 @@ __global__ void __launch_bounds__(256) k_image_finalize(DevPlan d) {
 }
 
 // ---------------------------------------------------------------------------
+// Free cameras: per image work item (the items of k_image_reduce) the sums
+// E = J_i^T J_c (6 x 10), the upper triangle of J_c^T J_c (55) and J_c^T r
+// (10) over its keys (camera_shared_normal_equation_builder.hpp:111-462 for
+// the camera blocks).  A CTA stages 32 keys' rows [J_i | J_c | r] in shared
+// memory; thread e owns sum e (Kahan in T, keys in order).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) k_image_cam_reduce(DevPlan d) {
+  __shared__ T M[64][17];
+  const int4 it = d.img_items[blockIdx.x];   // (image, q begin, q end, prob)
+  const LMState& st = d.state[it.w];
+  if (!st.relin || !st.active) return;
+  if (d.cam_info[d.img_cam[it.x]].x == 0) return;
+  const T* __restrict__ JR = tptr<T>(d.JR);
+  const T* __restrict__ JC = tptr<T>(d.JC);
+  const int e = threadIdx.x;
+  int ca = 0, cb = 0;
+  if (e < 60) {
+    ca = e / 10;
+    cb = 6 + e % 10;
+  } else if (e < 115) {
+    int t = e - 60, m = 0;
+    while (t >= 10 - m) {
+      t -= 10 - m;
+      ++m;
+    }
+    ca = 6 + m;
+    cb = 6 + m + t;
+  } else if (e < 125) {
+    ca = 6 + (e - 115);
+    cb = 16;
+  }
+  T acc = T(0), cmp = T(0);
+  for (int q0 = it.y; q0 < it.z; q0 += 32) {
+    const int nq = min(32, it.z - q0);
+    for (int v = threadIdx.x; v < 64 * 17; v += 128) {
+      const int row = v / 17, col = v - 17 * (v / 17), kq = row >> 1, rr = row & 1;
+      T val = T(0);
+      if (kq < nq) {
+        const long long k = __ldg(d.img_keys + q0 + kq);
+        if (col < 6) val = JR[kJRStride * k + 6 + 6 * rr + col];
+        else if (col < 16) val = JC[20 * k + 10 * rr + (col - 6)];
+        else val = JR[kJRStride * k + 18 + rr];
+      }
+      M[row][col] = val;
+    }
+    __syncthreads();
+    if (e < 125) {
+      for (int row = 0; row < 2 * nq; ++row) {
+        const T y = M[row][ca] * M[row][cb] - cmp;
+        const T t = acc + y;
+        cmp = (t - acc) - y;
+        acc = t;
+      }
+    }
+    __syncthreads();
+  }
+  d.img_item_cam[(long long)kImgCamVals * blockIdx.x + e] = e < 125 ? double(acc - cmp) : 0.0;
+}
+
+// Per free camera: E of each of its images (FP64 sums of the image's items),
+// then U_c and g_c over its images in order, compacted to the computed
+// parameters, with the camera's soft constraints
+// (camera_shared_normal_equation_builder.hpp:309-349,418-459).
+__global__ void __launch_bounds__(128) k_cam_finalize(DevPlan d) {
+  __shared__ double sh[kImgCamVals];
+  const int c = blockIdx.x;
+  const int4 ci = d.cam_info[c];
+  if (ci.x == 0) return;
+  const LMState& st = d.state[ci.z];
+  if (!st.relin || !st.active) return;
+  const int e = threadIdx.x;
+  double tot = 0.0;
+  for (int u = d.cam_img_off[c]; u < d.cam_img_off[c + 1]; ++u) {
+    const int img = d.cam_imgs[u];
+    double v = 0.0;
+    for (int t = d.img_item_off[img]; t < d.img_item_off[img + 1]; ++t)
+      v += d.img_item_cam[(long long)kImgCamVals * t + e];
+    if (e < 60) d.Ei[60LL * img + e] = v;
+    tot += v;
+  }
+  sh[e] = tot;
+  __syncthreads();
+  if (e != 0) return;
+  const int cps = ci.x;
+  const unsigned mask = unsigned(ci.y);
+  double* U = d.Uc + 100LL * c;
+  double* g = d.gc + 10LL * c;
+  for (int m = 0; m < cps; ++m) {
+    const int fm = cam_full_col(mask, m);
+    for (int n = 0; n < cps; ++n) {
+      const int fn = cam_full_col(mask, n);
+      U[10 * m + n] = sh[60 + upper10(min(fm, fn), max(fm, fn))];
+    }
+    g[m] = sh[115 + fm];
+  }
+  if (d.n_cons > 0) {
+    const double* x = d.x_cam[st.parity] + 10LL * c;
+    for (int r = d.prob_cons_off[ci.z]; r < d.prob_cons_off[ci.z + 1]; ++r) {
+      const int4 cr = d.cons[r];
+      if (cr.x != 2 || cr.y != c) continue;
+      const double2 yw = d.cons_yw[r];
+      U[11 * cr.z] += yw.y;
+      g[cr.z] += yw.y * (x[cr.z] - yw.x);
+    }
+  }
+  double dmax = 0.0, gmax = 0.0;
+  for (int m = 0; m < cps; ++m) {
+    dmax = fmax(dmax, U[11 * m]);
+    gmax = fmax(gmax, fabs(g[m]));
+  }
+  LMState* sp = d.state + ci.z;
+  atomicMax(&sp->maxdiag_bits, dbits(dmax));
+  atomicMax(&sp->ginf_bits, dbits(gmax));
+}
+
+// ---------------------------------------------------------------------------
 // point factor: C C^T = V_p + mu I, C^-1 and h_p = C^-1 g_p per point
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -866,6 +1098,60 @@ __global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
   }
 }
 
+// Free cameras: per camera record r of a point (camera c, part h) the Z
+// record C_p^-1 W with W = sum over the point's keys seen through camera c
+// of J_p^T J_c[:, 6h .. 6h+5] (computed parameters; zero past them).
+template <typename T>
+__global__ void __launch_bounds__(kPointChunk) k_camrec_z(DevPlan d) {
+  const Chunk ch = d.pt_chunks[blockIdx.x];
+  const LMState& st = d.state[ch.prob];
+  if (!st.active) return;
+  const int pt = ch.begin + threadIdx.x;
+  if (pt >= ch.end) return;
+  const int rb = d.pt_rec_off[pt], re = d.pt_rec_off[pt + 1];
+  if (rb == re) return;
+  const T* __restrict__ JR = tptr<T>(d.JR);
+  const T* __restrict__ JC = tptr<T>(d.JC);
+  T ps[8];
+  load_vec<8>(tptr<T>(d.PS) + 12LL * pt, ps);
+  const T i00 = ps[0], m10 = ps[1], i11 = ps[2], m20 = ps[3], m21 = ps[4], i22 = ps[5];
+  const int kb = d.pt_key_off[pt], ke = d.pt_key_off[pt + 1];
+  for (int r = rb; r < re; ++r) {
+    const int2 ri = d.rec_info[r - d.K];
+    const int4 ci = d.cam_info[ri.x];
+    const int h = ri.y - ci.w;
+    int col[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) col[a] = 6 * h + a < ci.x ? cam_full_col(unsigned(ci.y), 6 * h + a) : -1;
+    T w[18];
+#pragma unroll
+    for (int e = 0; e < 18; ++e) w[e] = T(0);
+    for (int k = kb; k < ke; ++k) {
+      if (d.img_cam[d.key_img[k]] != ri.x) continue;
+      T jp[6];
+#pragma unroll
+      for (int m = 0; m < 6; ++m) jp[m] = JR[(long long)kJRStride * k + m];
+#pragma unroll
+      for (int a = 0; a < 6; ++a) {
+        if (col[a] < 0) continue;
+        const T j0 = JC[20LL * k + col[a]], j1 = JC[20LL * k + 10 + col[a]];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) w[6 * i + a] += jp[i] * j0 + jp[3 + i] * j1;
+      }
+    }
+    T z[kZStride];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      z[a] = i00 * w[a];
+      z[6 + a] = m10 * w[a] + i11 * w[6 + a];
+      z[12 + a] = m20 * w[a] + m21 * w[6 + a] + i22 * w[12 + a];
+    }
+    z[18] = T(0);
+    z[19] = T(0);
+    store_vec<kZStride>(tptr_mut<T>(d.Z) + (long long)kZStride * r, z);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Schur assembly, one warp per work item (<= kPairItem pairs of one block)
 // ---------------------------------------------------------------------------
@@ -933,7 +1219,11 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
 }
 
 // Dense reduced system (lower triangle) and rhs in precision T; the block
-// sums over work items are taken in FP64.
+// sums over work items are taken in FP64.  Rows and columns run over the
+// problem's reduced-system images: its images, then with free cameras nc
+// 6-wide parts of each camera (camera_shared_normal_equation_solver.hpp:270-392,
+// 422-443: U_c, the image-camera blocks E and g_c enter as the images' U and
+// g do; columns past the camera's parameters hold mu alone).
 template <typename T>
 __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
   const int p = blockIdx.y;
@@ -946,8 +1236,8 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
   const int row = int(idx / n), col = int(idx % n);
   if (col > row) return;
   const int i = row / 6, a = row % 6, j = col / 6, bcol = col % 6;
-  const int I = pi.num_images;
-  const int blk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)j * I + i);
+  const int Ie = pi.num_ext, ni = pi.num_images;
+  const int blk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)j * Ie + i);
   double v = 0.0, rv = 0.0;
   if (blk >= 0) {
     const int ib = __ldg(d.blk_item_off + blk), ie = __ldg(d.blk_item_off + blk + 1);
@@ -955,24 +1245,41 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
       v += d.item_partial[(long long)kItemStride * t + 6 * bcol + a];
     }
   }
-  const int gi_img = pi.image_begin + i;
-  double s;
-  if (i == j) {
-    s = d.U[36LL * gi_img + 6 * a + bcol] - v;
-    if (a == bcol) s += st.mu;
+  double base = 0.0, g = 0.0;
+  if (i < ni) {
+    const int gi_img = pi.image_begin + i;
+    if (i == j) base = d.U[36LL * gi_img + 6 * a + bcol];
+    if (col == 0) g = d.gi[6LL * gi_img + a];
   } else {
-    s = -v;
+    // camera part: global camera ci, parameter m of the row
+    const int ci = pi.cam_begin + (i - ni) / pi.nc;
+    const int4 cinf = d.cam_info[ci];
+    const int m = 6 * ((i - ni) % pi.nc) + a;
+    if (m < cinf.x) {
+      if (j >= ni) {
+        const int cj = pi.cam_begin + (j - ni) / pi.nc;
+        const int mj = 6 * ((j - ni) % pi.nc) + bcol;
+        if (cj == ci && mj < cinf.x) base = d.Uc[100LL * ci + 10 * m + mj];
+      } else {
+        const int gj = pi.image_begin + j;
+        if (d.img_cam[gj] == ci)
+          base = d.Ei[60LL * gj + 10 * bcol + cam_full_col(unsigned(cinf.y), m)];
+      }
+      if (col == 0) g = d.gc[10LL * ci + m];
+    }
   }
+  double s = base - v;
+  if (row == col) s += st.mu;
   tptr_mut<T>(d.S)[pi.s_off + (long long)row * n + col] = T(s);
   if (col == 0) {
     // rhs b_i[a] = g_i[a] - sum over the diagonal block's items
-    const int dblk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)i * I + i);
+    const int dblk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)i * Ie + i);
     rv = 0.0;
     if (dblk >= 0) {
       const int ib = __ldg(d.blk_item_off + dblk), ie = __ldg(d.blk_item_off + dblk + 1);
       for (int t = ib; t < ie; ++t) rv += d.item_partial[(long long)kItemStride * t + 36 + a];
     }
-    tptr_mut<T>(d.b)[6LL * gi_img + a] = T(d.gi[6LL * gi_img + a] - rv);
+    tptr_mut<T>(d.b)[6LL * (pi.ext_begin + i) + a] = T(g - rv);
   }
 }
 
@@ -1200,7 +1507,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_chol_step(DevPl
   }
   const int n = pi.n;
   T* S = tptr_mut<T>(d.S) + pi.s_off;
-  T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.ext_begin;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // own tile and, for k >= 0, the column-k factors: all loads issued first
   TileFetch<T> fa, fi, fj, fd;
@@ -1366,7 +1673,7 @@ __global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
   int* rd_s = kt_s + mo;       // ready tasks found by the last poll
   int* pr_s = rd_s + mo;       // tile (i, i-1): local index of (i, i); otherwise -1
   T* S = tptr_mut<T>(d.S) + pi.s_off;
-  T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.ext_begin;
   T* Lg = tptr_mut<T>(d.Linv) + (long long)p * d.max_nt * kTile * kTile;
   unsigned* flags = d.df_flags;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1687,7 +1994,7 @@ __device__ __forceinline__ void chol_solve_body(const DevPlan& d, int q) {
   const ProbInfo pi = d.prob[p];
   const int nt = pi.nt, n = pi.n;
   const T* S = tptr<T>(d.S) + pi.s_off;
-  T* b = tptr_mut<T>(d.b) + 6LL * pi.image_begin;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.ext_begin;
   const T* Linv = tptr<T>(d.Linv) + (long long)p * d.max_nt * kTile * kTile;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nown = nt > q ? (nt - q + R - 1) / R : 0;
@@ -2086,10 +2393,17 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       T t0 = ps[6], t1 = ps[7], t2 = ps[8];
       const T* __restrict__ Z = tptr<T>(d.Z);
       const int kb = __ldg(d.pt_key_off + pt), ke = __ldg(d.pt_key_off + pt + 1);
-      for (int k = kb; k < ke; ++k) {
+      // every Z record of the point: its keys, then (free cameras) its
+      // camera records, each against its reduced-system image's delta
+      const int rb = d.pt_rec_off ? __ldg(d.pt_rec_off + pt) : 0;
+      const int re = d.pt_rec_off ? ke + (__ldg(d.pt_rec_off + pt + 1) - rb) : ke;
+      for (int k = kb; k < re; ++k) {
+        const int r = k < ke ? k : rb + (k - ke);
         T z[kZStride];
-        load_vec<kZStride>(Z + (long long)kZStride * k, z);
-        const T* di = tptr<T>(d.b) + 6LL * __ldg(d.key_img + k);
+        load_vec<kZStride>(Z + (long long)kZStride * r, z);
+        const int ext = k < ke ? (d.img_ext ? __ldg(d.img_ext + __ldg(d.key_img + k)) : __ldg(d.key_img + k))
+                               : __ldg(&d.rec_info[r - d.K].y);
+        const T* di = tptr<T>(d.b) + 6LL * ext;
         T dl[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) dl[c] = di[c];
@@ -2132,8 +2446,10 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
     const int par = st.parity;
     double dn2 = 0.0, xn2 = 0.0, gd = 0.0;
     const long long e0 = 6LL * ch.begin, e1 = 6LL * ch.end;
+    const ProbInfo& pi = d.prob[ch.prob];
+    const long long boff = 6LL * (pi.ext_begin - pi.image_begin);
     for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      double dv = double(tptr<T>(d.b)[e]), xv = d.x_img[par][e];
+      double dv = double(tptr<T>(d.b)[e + boff]), xv = d.x_img[par][e];
       d.x_img[1 - par][e] = xv - dv;
       dn2 += dv * dv;
       xn2 += xv * xv;
@@ -2146,6 +2462,33 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       d.img_chunk_sum[3LL * c + 2] = s2;
     }
   }
+}
+
+// Free cameras: delta_c from the camera's parts of the reduced-system
+// solution, the candidate x_c - delta_c, and the camera's terms of
+// ||delta||^2, ||x||^2 and g^T delta.
+template <typename T>
+__global__ void k_cam_backsub(DevPlan d) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.Ctot) return;
+  const int4 ci = d.cam_info[c];
+  const LMState& st = d.state[ci.z];
+  if (!st.active || d.factor_flag[ci.z]) return;
+  double dn2 = 0.0, xn2 = 0.0, gd = 0.0;
+  if (ci.x > 0) {
+    const int par = st.parity;
+    const T* b = tptr<T>(d.b) + 6LL * ci.w;
+    for (int m = 0; m < ci.x; ++m) {
+      const double dv = double(b[m]), xv = d.x_cam[par][10LL * c + m];
+      d.x_cam[1 - par][10LL * c + m] = xv - dv;
+      dn2 += dv * dv;
+      xn2 += xv * xv;
+      gd += d.gc[10LL * c + m] * dv;
+    }
+  }
+  d.cam_sum[3LL * c] = dn2;
+  d.cam_sum[3LL * c + 1] = xn2;
+  d.cam_sum[3LL * c + 2] = gd;
 }
 
 // ---------------------------------------------------------------------------
@@ -2219,6 +2562,11 @@ __global__ void k_ctrl_step(DevPlan d) {
          prob_sum(d.img_chunk_sum, 3, 2, d.prob_img_chunk_off, p, lane);
     // PCG leaves the image rows with residual r: the model decrease gains r^T delta_i
     if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_img_chunk_off, p, lane);
+    if (d.free_cams) {
+      dn2 += prob_sum(d.cam_sum, 3, 0, d.prob_cam_off, p, lane);
+      xn2 += prob_sum(d.cam_sum, 3, 1, d.prob_cam_off, p, lane);
+      gd += prob_sum(d.cam_sum, 3, 2, d.prob_cam_off, p, lane);
+    }
   }
   if (lane != 0) return;
   st.iter += 1;
@@ -2295,7 +2643,7 @@ __global__ void k_vector_function(DevPlan d, double* y) {
   const double* xp = d.x_pt[par] + 3LL * pt;
   double X[3] = {xp[0], xp[1], xp[2]};
   double cam[10];
-  for (int j = 0; j < 10; ++j) cam[j] = d.cam64[10 * d.img_cam[img] + j];
+  for (int j = 0; j < 10; ++j) cam[j] = d.cam64[par][10 * d.img_cam[img] + j];
   double u, v;
   project64(R, X, cam, u, v);
   y[2LL * k] = u;
@@ -2303,7 +2651,7 @@ __global__ void k_vector_function(DevPlan d, double* y) {
 }
 
 template <typename T>
-__global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out) {
+__global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out, double* jc_out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.K) return;
   const int img = d.key_img[k], pt = d.key_pt[k];
@@ -2313,11 +2661,16 @@ __global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out) {
   T il[12];
   for (int j = 0; j < 12; ++j) il[j] = tptr<T>(d.img_lin[par])[12LL * img + j];
   T cam[10];
-  load_cam<T>(d, d.img_cam[img], cam);
-  T jp[6], ji[12];
-  key_jacobian<T>(X, il, cam, jp, ji);
+  load_cam<T>(d, par, d.img_cam[img], cam);
+  T jp[6], ji[12], nrm[2];
+  key_jacobian<T>(X, il, cam, jp, ji, nrm);
   for (int j = 0; j < 6; ++j) jp_out[6LL * k + j] = double(jp[j]);
   for (int j = 0; j < 12; ++j) ji_out[12LL * k + j] = double(ji[j]);
+  if (jc_out) {   // all ten columns; the host keeps the computed ones
+    T jc[20];
+    camera_jacobian<T>(nrm[0], nrm[1], cam, jc);
+    for (int j = 0; j < 20; ++j) jc_out[20LL * k + j] = double(jc[j]);
+  }
 }
 
 template <typename T>
@@ -2379,7 +2732,7 @@ void run_image_prep(const DevPlan& d, int which, cudaStream_t s) {
 
 int launch_init(const DevPlan& d, cudaStream_t s) {
   k_init<<<(d.B + 127) / 128, 128, 0, s>>>(d);
-  long long tot = 3LL * d.P + 6LL * d.I;
+  long long tot = 3LL * d.P + 6LL * d.I + (d.free_cams ? 10LL * d.Ctot : 0);
   if (tot > 0) {
     k_copy_x0<<<int((tot + 255) / 256), 256, 0, s>>>(d);
     return 2;
@@ -2388,9 +2741,14 @@ int launch_init(const DevPlan& d, cudaStream_t s) {
 }
 
 int launch_image_prep(const DevPlan& d, int which, cudaStream_t s) {
-  if (d.I <= 0) return 0;
+  int n = 0;
+  if (d.free_cams && d.Ctot > 0) {
+    k_cam_prep<<<(d.Ctot + 127) / 128, 128, 0, s>>>(d, which);
+    ++n;
+  }
+  if (d.I <= 0) return n;
   GBA_DISPATCH(d, run_image_prep<T>(d, which, s));
-  return 1;
+  return n + 1;
 }
 
 int launch_cost(const DevPlan& d, int which, cudaStream_t s) {
@@ -2431,7 +2789,10 @@ int launch_image_reduce(const DevPlan& d, cudaStream_t s) {
   if (d.n_img_items <= 0) return 0;
   GBA_DISPATCH(d, (k_image_reduce<T><<<(d.n_img_items + 7) / 8, 256, 0, s>>>(d)));
   k_image_finalize<<<(d.I + 7) / 8, 256, 0, s>>>(d);
-  return 2;
+  if (!d.free_cams) return 2;
+  GBA_DISPATCH(d, (k_image_cam_reduce<T><<<d.n_img_items, 128, 0, s>>>(d)));
+  k_cam_finalize<<<d.Ctot, 128, 0, s>>>(d);
+  return 4;
 }
 
 int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s) {
@@ -2447,6 +2808,10 @@ int launch_point_schur(const DevPlan& d, cudaStream_t s) {
   }
   if (d.n_key_chunks > 0) {
     GBA_DISPATCH(d, (k_key_z<T><<<d.n_key_chunks, 256, 0, s>>>(d)));
+    ++n;
+  }
+  if (d.free_cams && d.R > 0) {
+    GBA_DISPATCH(d, (k_camrec_z<T><<<d.n_pt_chunks, kPointChunk, 0, s>>>(d)));
     ++n;
   }
   return n;
@@ -2588,7 +2953,9 @@ int launch_backsub(const DevPlan& d, cudaStream_t s) {
   const int g = d.n_pt_chunks + d.n_img_chunks;
   if (g <= 0) return 0;
   GBA_DISPATCH(d, (k_backsub<T><<<g, kPointChunk, 0, s>>>(d)));
-  return 1;
+  if (!d.free_cams || d.Ctot <= 0) return 1;
+  GBA_DISPATCH(d, (k_cam_backsub<T><<<(d.Ctot + 127) / 128, 128, 0, s>>>(d)));
+  return 2;
 }
 
 int launch_ctrl_step(const DevPlan& d, cudaStream_t s) {
@@ -2607,9 +2974,9 @@ int launch_vector_function(const DevPlan& d, double* y, cudaStream_t s) {
   return 1;
 }
 
-int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, cudaStream_t s) {
+int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, double* jc, cudaStream_t s) {
   if (d.K <= 0) return 0;
-  GBA_DISPATCH(d, (k_jacobian_out<T><<<(d.K + 255) / 256, 256, 0, s>>>(d, jp, ji)));
+  GBA_DISPATCH(d, (k_jacobian_out<T><<<(d.K + 255) / 256, 256, 0, s>>>(d, jp, ji, jc)));
   return 1;
 }
 

@@ -86,7 +86,25 @@ void expand_camera(uint32_t mask, const double* c, double out[10]) {
   }
 }
 
-// Device buffer registry.
+// Column of the full ten holding a camera's computed parameter m.
+int camera_full_column(uint32_t mask, int m) {
+  if (mask & GBA_COMPUTE_RADIAL_DISTORTION) {
+    if (m < 3) return m;
+    m -= 3;
+  }
+  if (mask & GBA_COMPUTE_DECENTERING_DISTORTION) {
+    if (m < 2) return 3 + m;
+    m -= 2;
+  }
+  return 5 + m;
+}
+
+// Whether a problem's shared cameras are unknowns of the device path.
+bool cameras_free(const gba_problem& p) {
+  return !(p.fix_mask & GBA_FIX_CAMERAS) && p.number_of_cameras > 0 &&
+         params_per_camera(p.intrinsic_computations_mask) > 0;
+}
+
 // Device buffer registry.  Allocations are stream-ordered on the plan's
 // stream (cudaMallocAsync / cudaFreeAsync from the device's default pool), so
 // creating or destroying a plan never synchronizes other plans' streams.
@@ -190,19 +208,37 @@ struct Plan {
 
 namespace {
 
-// Validates a problem for the device path.  The device path covers the
-// configuration of the benchmark workloads: points and images free, cameras
-// (shared intrinsics) fixed, no soft constraints.
+// Validates a problem for the device path: points and images free, the
+// shared cameras fixed or (dense solver) free, soft constraints on any free
+// group.
 int validate(const gba_problem& p, bool pcg) {
   if (p.number_of_points < 0 || p.number_of_images < 0 || p.number_of_cameras < 0 ||
       p.number_of_keys < 0)
     return GBA_ERR_INVALID;
   if (p.number_of_keys > 0 && !p.feature_maps) return GBA_ERR_INVALID;
   if (p.number_of_images > 0 && !p.image_camera_map) return GBA_ERR_INVALID;
-  if (p.fix_mask != GBA_FIX_CAMERAS) return GBA_ERR_UNSUPPORTED;
-  if (p.number_of_cameras > 0 && params_per_camera(p.intrinsic_computations_mask) > 0 &&
-      !p.fix_cameras)
+  if (p.fix_mask != GBA_FIX_CAMERAS && p.fix_mask != 0) return GBA_ERR_UNSUPPORTED;
+  const int64_t cps = params_per_camera(p.intrinsic_computations_mask);
+  const bool free_cams = p.fix_mask == 0 && cps > 0 && p.number_of_cameras > 0;
+  if (free_cams && pcg) return GBA_ERR_UNSUPPORTED;
+  if (p.fix_mask == GBA_FIX_CAMERAS && p.number_of_cameras > 0 && cps > 0 && !p.fix_cameras)
     return GBA_ERR_INVALID;
+  if (p.fix_mask == 0) {
+    if ((p.number_of_camera_constraints > 0 && !p.camera_constraints) ||
+        p.number_of_camera_constraints < 0)
+      return GBA_ERR_INVALID;
+    const uint32_t m = p.intrinsic_computations_mask;
+    for (int64_t c = 0; c < p.number_of_camera_constraints; ++c) {
+      const gba_camera_constraint& cc = p.camera_constraints[c];
+      if (cc.camera_id < 0 || cc.camera_id >= p.number_of_cameras) return GBA_ERR_BAD_INDEX;
+      // a constraint on a group that is not computed fails
+      // (camera_shared_vector_function.hpp:549-557)
+      if ((cc.radial_mask && !(m & GBA_COMPUTE_RADIAL_DISTORTION)) ||
+          (cc.decentering_mask && !(m & GBA_COMPUTE_DECENTERING_DISTORTION)) ||
+          (cc.intrinsic_mask && !(m & GBA_COMPUTE_INTRINSIC_PARAMS)))
+        return GBA_ERR;
+    }
+  }
   if ((p.number_of_point_constraints > 0 && !p.point_constraints) ||
       (p.number_of_image_constraints > 0 && !p.image_constraints) ||
       p.number_of_point_constraints < 0 || p.number_of_image_constraints < 0)
@@ -216,7 +252,9 @@ int validate(const gba_problem& p, bool pcg) {
   if (p.number_of_points > INT32_MAX / 4 || p.number_of_keys > INT32_MAX / 4)
     return GBA_ERR_INVALID;
   // the dense reduced system of one problem is at most 12288^2 doubles
-  if (!pcg && p.number_of_images > 2048) return GBA_ERR_UNSUPPORTED;
+  // (2048 reduced-system images: the images and the cameras' 6-wide parts)
+  const int64_t n_ext = p.number_of_images + (free_cams ? p.number_of_cameras * ((cps + 5) / 6) : 0);
+  if (!pcg && n_ext > 2048) return GBA_ERR_UNSUPPORTED;
   for (int64_t i = 0; i < p.number_of_images; ++i) {
     int64_t c = p.image_camera_map[i];
     if (c < 0 || c >= p.number_of_cameras) return GBA_ERR_BAD_INDEX;
@@ -299,7 +337,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   std::vector<int4> img_items;
   std::vector<int> img_item_off(1, 0);
   std::vector<int> prob_key_chunk_off(1, 0), prob_pt_chunk_off(1, 0), prob_img_chunk_off(1, 0);
-  std::vector<int4> cons;          // (group 0 point / 1 image, global index, parameter, problem)
+  std::vector<int4> cons;          // (group 0 point / 1 image / 2 camera, global index, parameter, problem)
   std::vector<double2> cons_yw;    // (observed value, weight)
   std::vector<int> prob_cons_off(1, 0);
   prob.resize(nprob);
@@ -311,9 +349,13 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       cbase(nprob + 1, 0);
   long long s_off = 0;
   int max_n = 0, max_nt = 0;
+  int64_t I_ext = 0;
+  bool any_free = false;
   for (int q = 0; q < nprob; ++q) {
     const gba_problem& p = problems[q];
     const int np = int(p.number_of_points), ni = int(p.number_of_images), nk = int(p.number_of_keys);
+    const bool fc = cameras_free(p);
+    const int cps = int(params_per_camera(p.intrinsic_computations_mask));
     ProbInfo& pi = prob[q];
     pi.point_begin = int(pbase[q]);
     pi.num_points = np;
@@ -321,18 +363,27 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     pi.num_images = ni;
     pi.key_begin = int(kbase[q]);
     pi.num_keys = nk;
-    pi.n = 6 * ni;
+    pi.cam_begin = int(cbase[q]);
+    pi.num_cams = int(p.number_of_cameras);
+    pi.cps = fc ? cps : 0;
+    pi.nc = fc ? (cps + 5) / 6 : 0;
+    pi.ext_begin = int(I_ext);
+    pi.num_ext = ni + pi.num_cams * pi.nc;
+    any_free |= fc;
+    pi.n = 6 * pi.num_ext;
     pi.nt = (pi.n + kTile - 1) / kTile;
     pi.s_off = s_off;
     if (!pcg) s_off += (long long)pi.n * pi.n;   // the dense system only for the factorization
     max_n = std::max(max_n, pi.n);
     max_nt = std::max(max_nt, pi.nt);
-    x_size[q] = 3LL * np + 6LL * ni;
+    x_size[q] = 3LL * np + 6LL * ni + (p.fix_mask & GBA_FIX_CAMERAS ? 0 : int64_t(cps) * pi.num_cams);
     pbase[q + 1] = pbase[q] + np;
     ibase[q + 1] = ibase[q] + ni;
     kbase[q + 1] = kbase[q] + nk;
     cbase[q + 1] = cbase[q] + p.number_of_cameras;
+    I_ext += pi.num_ext;
   }
+  if (I_ext > INT32_MAX / 64) return GBA_ERR_INVALID;
 
   // ---- each problem's structure: the per-key, per-point and per-image
   // arrays are written in place (disjoint ranges), the appended lists go to
@@ -348,6 +399,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     std::vector<int> blk_map;          // [ni * ni] local block id or -1 (dense solver)
     std::vector<int4> cons;
     std::vector<double2> cons_yw;
+    std::vector<int> pt_rec_off;       // [np + 1] camera records of each point (free cameras)
+    std::vector<int> rec_ext;          // local reduced-system image of each camera record
   };
   std::vector<Piece> pieces(nprob);
   auto build_one = [&](int q, int inner) {
@@ -356,10 +409,12 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     const int np = int(p.number_of_points), ni = int(p.number_of_images), nk = int(p.number_of_keys);
     const int64_t cps = params_per_camera(p.intrinsic_computations_mask);
     const int64_t pb = pbase[q], ib = ibase[q], kb = kbase[q], cb = cbase[q];
-    // cameras
+    const bool fc = cameras_free(p);
+    const int Ie = prob[q].num_ext, ncp = prob[q].nc;
+    // cameras (free ones are written on the device from x)
     for (int64_t c = 0; c < p.number_of_cameras; ++c) {
-      double full[10];
-      expand_camera(p.intrinsic_computations_mask, p.fix_cameras + cps * c, full);
+      double full[10] = {0, 0, 0, 0, 0, 1, 0, 0, 0, 1};
+      if (!fc) expand_camera(p.intrinsic_computations_mask, p.fix_cameras + cps * c, full);
       for (int j = 0; j < 10; ++j) {
         cam64[10 * (cb + c) + j] = full[j];
         cam32[10 * (cb + c) + j] = float(full[j]);
@@ -454,13 +509,51 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         }
       }
     }
-    // reduced-system blocks: (i <= j) with their key pairs, point order.
+    // free cameras: each point has nc camera records (one per 6-wide part)
+    // for every distinct camera among its keys, ascending
+    if (fc) {
+      out.pt_rec_off.assign(np + 1, 0);
+      auto point_cams = [&](int64_t i, std::vector<int>& cams) {
+        cams.clear();
+        for (int a = cnt[i]; a < cnt[i + 1]; ++a) cams.push_back(img_cam[key_img[kb + a]] - int(cb));
+        std::sort(cams.begin(), cams.end());
+        cams.erase(std::unique(cams.begin(), cams.end()), cams.end());
+      };
+      host_parallel(np, nth0, [&](int64_t i0, int64_t i1, int) {
+        std::vector<int> cams;
+        for (int64_t i = i0; i < i1; ++i) {
+          point_cams(i, cams);
+          out.pt_rec_off[i + 1] = int(cams.size()) * ncp;
+        }
+      });
+      for (int i = 0; i < np; ++i) out.pt_rec_off[i + 1] += out.pt_rec_off[i];
+      out.rec_ext.resize(out.pt_rec_off[np]);
+      host_parallel(np, nth0, [&](int64_t i0, int64_t i1, int) {
+        std::vector<int> cams;
+        for (int64_t i = i0; i < i1; ++i) {
+          point_cams(i, cams);
+          int o = out.pt_rec_off[i];
+          for (int c : cams)
+            for (int h = 0; h < ncp; ++h) out.rec_ext[o++] = ni + c * ncp + h;
+        }
+      });
+    }
+    // The Z records of point i with their reduced-system images, ascending:
+    // its keys (the key index), then its camera records (-(local record + 1)).
+    auto point_records = [&](int64_t i, std::vector<int2>& rec) {
+      rec.clear();
+      for (int a = cnt[i]; a < cnt[i + 1]; ++a) rec.push_back(make_int2(key_img[kb + a] - int(ib), int(kb + a)));
+      if (fc)
+        for (int r = out.pt_rec_off[i]; r < out.pt_rec_off[i + 1]; ++r)
+          rec.push_back(make_int2(out.rec_ext[r], -(r + 1)));
+    };
+    // reduced-system blocks: (i <= j) with their record pairs, point order.
     // Pairs are counted and placed by point ranges in parallel: each piece
     // counts its pairs per image pair, a piece's pairs of a block follow
     // those of the pieces before it, so every block lists its pairs in
     // point order whatever the number of pieces.
     {
-      const size_t nn = (size_t)ni * ni;
+      const size_t nn = (size_t)Ie * Ie;
       int nth = nth0;
       while (nth > 1 && nn * size_t(nth) * sizeof(int) > (size_t(256) << 20)) --nth;
       std::vector<int64_t> cuts(nth + 1, np);
@@ -470,26 +563,36 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       std::vector<std::vector<int>> cnt_t(nth, std::vector<int>(nn, 0));
       host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
         int* bc = cnt_t[t].data();
+        std::vector<int2> rec;
         for (int64_t i = i0; i < i1; ++i) {
-          const int b0 = cnt[i], b1 = cnt[i + 1];
-          for (int a = b0; a < b1; ++a) {
-            const size_t row = (size_t)(key_img[kb + a] - int(ib)) * ni;
-            for (int c = a; c < b1; ++c) bc[row + key_img[kb + c] - int(ib)]++;
+          if (!fc) {   // keys only: straight from the point's key range
+            const int b0 = cnt[i], b1 = cnt[i + 1];
+            for (int a = b0; a < b1; ++a) {
+              const size_t row = (size_t)(key_img[kb + a] - int(ib)) * Ie;
+              for (int c = a; c < b1; ++c) bc[row + key_img[kb + c] - int(ib)]++;
+            }
+            continue;
+          }
+          point_records(i, rec);
+          const int nr = int(rec.size());
+          for (int a = 0; a < nr; ++a) {
+            const size_t row = (size_t)rec[a].x * Ie;
+            for (int c = a; c < nr; ++c) bc[row + rec[c].x]++;
           }
         }
       }, &cuts);
       std::vector<long long> bcount(nn, 0);
       for (int t = 0; t < nth; ++t)
         for (size_t e = 0; e < nn; ++e) bcount[e] += cnt_t[t][e];
-      // every image gets a diagonal block (so S keeps U_i + mu I even for an
-      // image without keys)
+      // every reduced-system image gets a diagonal block (so S keeps U_i + mu I
+      // even for an image without keys)
       std::vector<int> bid(nn, -1);
       long long acc = 0;
-      for (int a = 0; a < ni; ++a)
-        for (int c = a; c < ni; ++c) {
-          const long long n_ = bcount[(size_t)a * ni + c];
+      for (int a = 0; a < Ie; ++a)
+        for (int c = a; c < Ie; ++c) {
+          const long long n_ = bcount[(size_t)a * Ie + c];
           if (n_ == 0 && a != c) continue;
-          bid[(size_t)a * ni + c] = int(out.blk_ij.size());
+          bid[(size_t)a * Ie + c] = int(out.blk_ij.size());
           out.blk_ij.push_back(make_int2(a, c));
           out.blk_off.push_back(acc);
           acc += n_;
@@ -512,25 +615,36 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       out.pairs.resize(acc);
       host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
         int* slot = cnt_t[t].data();
+        std::vector<int2> rec;
         for (int64_t i = i0; i < i1; ++i) {
-          const int b0 = cnt[i], b1 = cnt[i + 1];
-          for (int a = b0; a < b1; ++a) {
-            const size_t row = (size_t)(key_img[kb + a] - int(ib)) * ni;
-            for (int c = a; c < b1; ++c) {
-              // a pair of a diagonal block is a key with itself: carry its point instead
-              out.pairs[slot[row + key_img[kb + c] - int(ib)]++] =
-                  make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
+          if (!fc) {
+            const int b0 = cnt[i], b1 = cnt[i + 1];
+            for (int a = b0; a < b1; ++a) {
+              const size_t row = (size_t)(key_img[kb + a] - int(ib)) * Ie;
+              for (int c = a; c < b1; ++c)
+                out.pairs[slot[row + key_img[kb + c] - int(ib)]++] =
+                    make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
+            }
+            continue;
+          }
+          point_records(i, rec);
+          const int nr = int(rec.size());
+          for (int a = 0; a < nr; ++a) {
+            const size_t row = (size_t)rec[a].x * Ie;
+            for (int c = a; c < nr; ++c) {
+              // a pair of a diagonal block is a record with itself: carry its point instead
+              out.pairs[slot[row + rec[c].x]++] =
+                  make_int2(rec[a].y, a == c ? int(pb + i) : rec[c].y);
             }
           }
         }
       }, &cuts);
-      // dense map for the assembly of the lower triangle: map[j*ni + i], j <= i
+      // dense map for the assembly of the lower triangle: map[j*Ie + i], j <= i
       if (!pcg) out.blk_map.swap(bid);
     }
-    // soft constraints on points and images, in y order
-    // (camera_shared_vector_function.hpp:483-629): the rows after the keys,
-    // each a copy of one parameter with its own weight; camera constraints
-    // have no rows while the cameras are fixed
+    // soft constraints in y order (camera_shared_vector_function.hpp:483-629):
+    // the rows after the keys, each a copy of one parameter with its own
+    // weight; camera constraints have rows only while the cameras are free
     {
       int64_t r = 0;
       auto add = [&](int group, int64_t index, int param) {
@@ -552,6 +666,21 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Y) add(1, ib + ic.image_id, 4);
         if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Z) add(1, ib + ic.image_id, 5);
       }
+      if (fc) {   // parameter indices in the problem's camera order
+        const uint32_t m = p.intrinsic_computations_mask;
+        for (int64_t c = 0; c < p.number_of_camera_constraints; ++c) {
+          const gba_camera_constraint& cc = p.camera_constraints[c];
+          int off = 0;
+          for (int b = 0; b < 3; ++b)
+            if (cc.radial_mask & (1u << b)) add(2, cb + cc.camera_id, off + b);
+          if (m & GBA_COMPUTE_RADIAL_DISTORTION) off += 3;
+          for (int b = 0; b < 2; ++b)
+            if (cc.decentering_mask & (1u << b)) add(2, cb + cc.camera_id, off + b);
+          if (m & GBA_COMPUTE_DECENTERING_DISTORTION) off += 2;
+          for (int b = 0; b < 5; ++b)
+            if (cc.intrinsic_mask & (1u << b)) add(2, cb + cc.camera_id, off + b);
+        }
+      }
     }
   };
   if (nprob == 1) {
@@ -568,6 +697,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   phase("problems");
 
   // ---- concatenation in problem order
+  // camera records are Z records K .. K+R-1, after the keys
+  std::vector<int> pt_rec_off;
+  std::vector<int2> rec_info;
+  if (any_free) pt_rec_off.assign(P + 1, int(K));
   for (int q = 0; q < nprob; ++q) {
     Piece& pc = pieces[q];
     ProbInfo& pi = prob[q];
@@ -583,6 +716,19 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     const int block_begin = int(blk_ij.size());
     const long long pair_base = (long long)pairs.size();
     if (pair_base + (long long)pc.pairs.size() > INT32_MAX) return GBA_ERR_INVALID;
+    const long long rec_base = (long long)K + (long long)rec_info.size();
+    if (rec_base + (long long)pc.rec_ext.size() > INT32_MAX) return GBA_ERR_INVALID;
+    if (!pc.rec_ext.empty()) {
+      for (int2& pr : pc.pairs) {   // camera records: -(local + 1) -> global record
+        if (pr.x < 0) pr.x = int(rec_base - 1 - pr.x);
+        if (pr.y < 0) pr.y = int(rec_base - 1 - pr.y);
+      }
+      for (int i = 0; i < np; ++i) pt_rec_off[pb + i] = int(rec_base + pc.pt_rec_off[i]);
+      for (int e : pc.rec_ext)
+        rec_info.push_back(make_int2(int(cbase[q]) + (e - ni) / pi.nc, pi.ext_begin + e));
+    } else if (any_free) {
+      for (int i = 0; i < np; ++i) pt_rec_off[pb + i] = int(rec_base);
+    }
     pairs.insert(pairs.end(), pc.pairs.begin(), pc.pairs.end());
     blk_ij.insert(blk_ij.end(), pc.blk_ij.begin(), pc.blk_ij.end());
     const int nblk = int(pc.blk_ij.size());
@@ -621,6 +767,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   }
   pt_key_off[P] = int(K);
   img_key_off[I] = int(K);
+  const int R = int(rec_info.size());
+  if (any_free) pt_rec_off[P] = int(K) + R;
 
   phase("host structure");
   // ---- device allocations
@@ -655,8 +803,13 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.img_items = arena.upload(img_items);
   D.img_item_off = arena.upload(img_item_off);
   D.img_item_partial = arena.alloc<double>(28 * std::max<size_t>(img_items.size(), 1));
-  D.cam64 = arena.upload(cam64);
-  D.cam32 = arena.upload(cam32);
+  // with free cameras each parity has its own camera arrays (the fixed
+  // cameras' values in both)
+  D.cam64[0] = arena.upload(cam64);
+  D.cam32[0] = arena.upload(cam32);
+  D.cam64[1] = any_free ? arena.upload(cam64) : D.cam64[0];
+  D.cam32[1] = any_free ? arena.upload(cam32) : D.cam32[0];
+  D.cam_ff[0] = D.cam_ff[1] = nullptr;
   if (mixed) {
     std::vector<float2> obs_ff(2 * K), cam_ff(10 * std::max<int64_t>(C, 1));
     auto split = [](double v) {
@@ -672,7 +825,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       cam_ff[10 * c + 9] = split(cam64[10 * c + 5] * cam64[10 * c + 9]);   // f * a
     }
     D.key_obs_ff = arena.upload(obs_ff);
-    D.cam_ff = arena.upload(cam_ff);
+    D.cam_ff[0] = arena.upload(cam_ff);
+    D.cam_ff[1] = any_free ? arena.upload(cam_ff) : D.cam_ff[0];
   }
   for (int t = 0; t < 2; ++t) {
     D.img_rot_ff[t] = mixed ? arena.alloc<float2>(12 * I) : nullptr;
@@ -686,15 +840,57 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.x0_pt = arena.alloc<double>(3 * P);
   D.x0_img = arena.alloc<double>(6 * I);
   D.JR = arena.alloc<char>(size_t(kJRStride) * K * tsz);
-  D.Z = arena.alloc<char>(size_t(kZStride) * K * tsz);
+  D.Z = arena.alloc<char>(size_t(kZStride) * (K + R) * tsz);
   D.PV = arena.alloc<char>(12 * P * tsz);
   D.PS = arena.alloc<char>(12 * P * tsz);
   D.U = arena.alloc<double>(36 * I);
   D.gi = arena.alloc<double>(6 * I);
   D.S = arena.alloc<char>(size_t(std::max<long long>(s_off, 1)) * tsz);
-  D.b = arena.alloc<char>(size_t(std::max<int64_t>(6 * I, 1)) * tsz);
+  D.b = arena.alloc<char>(size_t(std::max<int64_t>(6 * I_ext, 1)) * tsz);
   D.Linv = arena.alloc<char>(pcg ? 1 : size_t(nprob) * std::max(max_nt, 1) * kTile * kTile * tsz);
   D.factor_flag = arena.alloc<int>(nprob);
+  D.free_cams = any_free ? 1 : 0;
+  D.Ctot = int(C);
+  D.R = R;
+  D.I_ext = int(I_ext);
+  if (any_free) {
+    std::vector<int> img_ext(I), cam_img_off(C + 1, 0), cam_imgs(I);
+    std::vector<int4> cam_info(C);
+    for (int q = 0; q < nprob; ++q) {
+      const ProbInfo& pq = prob[q];
+      for (int i = 0; i < pq.num_images; ++i) img_ext[pq.image_begin + i] = pq.ext_begin + i;
+      for (int c = 0; c < pq.num_cams; ++c)
+        cam_info[pq.cam_begin + c] =
+            make_int4(pq.cps, int(problems[q].intrinsic_computations_mask), q,
+                      pq.cps ? pq.ext_begin + pq.num_images + c * pq.nc : 0);
+    }
+    for (int64_t i = 0; i < I; ++i) cam_img_off[img_cam[i] + 1]++;
+    for (int64_t c = 0; c < C; ++c) cam_img_off[c + 1] += cam_img_off[c];
+    {
+      std::vector<int> fill(cam_img_off.begin(), cam_img_off.end() - 1);
+      for (int64_t i = 0; i < I; ++i) cam_imgs[fill[img_cam[i]]++] = int(i);
+    }
+    std::vector<int> prob_cam_off(nprob + 1);
+    for (int q = 0; q <= nprob; ++q) prob_cam_off[q] = int(cbase[q]);
+    D.img_ext = arena.upload(img_ext);
+    D.cam_info = arena.upload(cam_info);
+    D.cam_img_off = arena.upload(cam_img_off);
+    D.cam_imgs = arena.upload(cam_imgs);
+    D.prob_cam_off = arena.upload(prob_cam_off);
+    D.x_cam[0] = arena.alloc<double>(10 * C);
+    D.x_cam[1] = arena.alloc<double>(10 * C);
+    D.x0_cam = arena.alloc<double>(10 * C);
+    GBA_CUDA(cudaMemsetAsync(D.x0_cam, 0, sizeof(double) * 10 * std::max<int64_t>(C, 1), stream));
+    D.JC = arena.alloc<char>(size_t(20) * K * tsz);
+    D.pt_rec_off = arena.upload(pt_rec_off);
+    D.rec_info = arena.upload(rec_info);
+    D.img_item_cam = arena.alloc<double>(size_t(kImgCamVals) * std::max<size_t>(img_items.size(), 1));
+    D.Ei = arena.alloc<double>(60 * I);
+    D.Uc = arena.alloc<double>(100 * C);
+    D.gc = arena.alloc<double>(10 * C);
+    D.cam_sum = arena.alloc<double>(3 * C);
+    GBA_CUDA(cudaMemsetAsync(D.cam_sum, 0, sizeof(double) * 3 * std::max<int64_t>(C, 1), stream));
+  }
   D.df_grid = 0;
   D.df_trace = nullptr;
   D.pcg = pcg ? 1 : 0;
@@ -796,14 +992,15 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   if (!cons.empty()) {
     // rows of each point / image in y order, for the linearization
     std::vector<int> pt_off(P + 1, 0), img_off(I + 1, 0);
-    for (const int4& c : cons) (c.x == 0 ? pt_off[c.y + 1] : img_off[c.y + 1])++;
+    for (const int4& c : cons)
+      if (c.x < 2) (c.x == 0 ? pt_off[c.y + 1] : img_off[c.y + 1])++;
     for (int64_t i = 0; i < P; ++i) pt_off[i + 1] += pt_off[i];
     for (int64_t i = 0; i < I; ++i) img_off[i + 1] += img_off[i];
     std::vector<int> by_pt(pt_off[P]), by_img(img_off[I]);
     std::vector<int> fp(pt_off.begin(), pt_off.end() - 1), fi(img_off.begin(), img_off.end() - 1);
     for (size_t r = 0; r < cons.size(); ++r) {
       if (cons[r].x == 0) by_pt[fp[cons[r].y]++] = int(r);
-      else by_img[fi[cons[r].y]++] = int(r);
+      else if (cons[r].x == 1) by_img[fi[cons[r].y]++] = int(r);
     }
     D.cons = arena.upload(cons);
     D.cons_yw = arena.upload(cons_yw);
@@ -1126,8 +1323,18 @@ int gba_plan_set_initial_x(gba_plan* p, int32_t q, const double* x0) {
     GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_img) + 6LL * pi.image_begin,
                              x0 + 3LL * pi.num_points, sizeof(double) * 6 * pi.num_images,
                              cudaMemcpyHostToDevice, P.stream));
+    std::vector<double> cams;
+    if (pi.cps > 0) {   // free cameras: cps parameters each, ten-wide on the device
+      const double* xc = x0 + 3LL * pi.num_points + 6LL * pi.num_images;
+      cams.assign(10 * size_t(pi.num_cams), 0.0);
+      for (int c = 0; c < pi.num_cams; ++c)
+        std::copy(xc + (size_t)pi.cps * c, xc + (size_t)pi.cps * (c + 1), cams.begin() + 10 * c);
+      GBA_CUDA(cudaMemcpyAsync(P.d.x0_cam + 10LL * pi.cam_begin, cams.data(),
+                               sizeof(double) * cams.size(), cudaMemcpyHostToDevice, P.stream));
+    }
     GBA_CUDA(cudaStreamSynchronize(P.stream));
-    P.h2d_bytes += (long long)sizeof(double) * (3LL * pi.num_points + 6LL * pi.num_images);
+    P.h2d_bytes += (long long)sizeof(double) *
+                   (3LL * pi.num_points + 6LL * pi.num_images + (long long)cams.size());
     return GBA_OK;
   });
 }
@@ -1157,9 +1364,20 @@ int gba_plan_get_x(gba_plan* p, int32_t q, double* x) {
                              cudaMemcpyDeviceToHost, P.stream));
     GBA_CUDA(cudaMemcpyAsync(x + 3LL * pi.num_points, xi + 6LL * pi.image_begin,
                              sizeof(double) * 6 * pi.num_images, cudaMemcpyDeviceToHost, P.stream));
+    std::vector<double> cams;
+    if (pi.cps > 0) {
+      const double* xc = P.ran ? P.d.x_cam[par] : P.d.x0_cam;
+      cams.resize(10 * size_t(pi.num_cams));
+      GBA_CUDA(cudaMemcpyAsync(cams.data(), xc + 10LL * pi.cam_begin, sizeof(double) * cams.size(),
+                               cudaMemcpyDeviceToHost, P.stream));
+    }
     GBA_CUDA(cudaStreamSynchronize(P.stream));
+    double* xo = x + 3LL * pi.num_points + 6LL * pi.num_images;
+    for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
+      std::copy(cams.begin() + 10 * c, cams.begin() + 10 * c + pi.cps, xo + (size_t)pi.cps * c);
     P.d2h_bytes += (long long)sizeof(st) +
-                   (long long)sizeof(double) * (3LL * pi.num_points + 6LL * pi.num_images);
+                   (long long)sizeof(double) * (3LL * pi.num_points + 6LL * pi.num_images +
+                                                (long long)cams.size());
     return GBA_OK;
   });
 }
@@ -1343,6 +1561,24 @@ int gba_vector_function(const gba_problem* problem, const double* x, double* y, 
       if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Y) y[r++] = xi[4];
       if (ic.mask & GBA_IMAGE_CONSTRAIN_POSITION_Z) y[r++] = xi[5];
     }
+    if (!(problem->fix_mask & GBA_FIX_CAMERAS)) {
+      const uint32_t m = problem->intrinsic_computations_mask;
+      const int64_t cps = gba::params_per_camera(m);
+      const double* xc = x + img0 + 6 * problem->number_of_images;
+      for (int64_t c = 0; c < problem->number_of_camera_constraints; ++c) {
+        const gba_camera_constraint& cc = problem->camera_constraints[c];
+        const double* xv = xc + cps * cc.camera_id;
+        int off = 0;
+        for (int b = 0; b < 3; ++b)
+          if (cc.radial_mask & (1u << b)) y[r++] = xv[off + b];
+        if (m & GBA_COMPUTE_RADIAL_DISTORTION) off += 3;
+        for (int b = 0; b < 2; ++b)
+          if (cc.decentering_mask & (1u << b)) y[r++] = xv[off + b];
+        if (m & GBA_COMPUTE_DECENTERING_DISTORTION) off += 2;
+        for (int b = 0; b < 5; ++b)
+          if (cc.intrinsic_mask & (1u << b)) y[r++] = xv[off + b];
+      }
+    }
     return GBA_OK;
   });
   gba_plan_destroy(plan);
@@ -1351,7 +1587,6 @@ int gba_vector_function(const gba_problem* problem, const double* x, double* y, 
 
 int gba_jacobian(const gba_problem* problem, const double* x, double* point_blocks,
                  double* image_blocks, double* camera_blocks, int32_t precision) {
-  (void)camera_blocks;
   if (!problem || !x) return GBA_ERR_INVALID;
   gba_plan* plan = nullptr;
   int err = stage_plan(problem, nullptr, x, precision, &plan, nullptr);
@@ -1364,17 +1599,26 @@ int gba_jacobian(const gba_problem* problem, const double* x, double* point_bloc
     const int K = std::max(P.d.K, 1);
     double* jp = P.arena.alloc<double>(6 * K);
     double* ji = P.arena.alloc<double>(12 * K);
-    gba::launch_jacobian_out(P.d, jp, ji, s);
+    const int cps = P.prob[0].cps;   // > 0 only with free cameras
+    double* jc = (camera_blocks && cps > 0) ? P.arena.alloc<double>(20 * K) : nullptr;
+    gba::launch_jacobian_out(P.d, jp, ji, jc, s);
     gba::g_launches += 4;
     GBA_CUDA(cudaStreamSynchronize(s));
     GBA_CUDA(cudaGetLastError());
-    std::vector<double> hp(6 * P.d.K), hi(12 * P.d.K);
+    std::vector<double> hp(6 * P.d.K), hi(12 * P.d.K), hc(jc ? 20 * P.d.K : 0);
     GBA_CUDA(cudaMemcpy(hp.data(), jp, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost));
     GBA_CUDA(cudaMemcpy(hi.data(), ji, sizeof(double) * hi.size(), cudaMemcpyDeviceToHost));
+    if (jc) GBA_CUDA(cudaMemcpy(hc.data(), jc, sizeof(double) * hc.size(), cudaMemcpyDeviceToHost));
     const auto& perm = P.key_sorted_to_orig[0];
+    const uint32_t mask = problem->intrinsic_computations_mask;
     for (int t = 0; t < P.d.K; ++t) {
       if (point_blocks) std::copy(&hp[6 * t], &hp[6 * t] + 6, point_blocks + 6LL * perm[t]);
       if (image_blocks) std::copy(&hi[12 * t], &hi[12 * t] + 12, image_blocks + 12LL * perm[t]);
+      if (jc)   // 2 x cps, row-major, the computed columns
+        for (int r = 0; r < 2; ++r)
+          for (int m = 0; m < cps; ++m)
+            camera_blocks[2LL * cps * perm[t] + cps * r + m] =
+                hc[20 * t + 10 * r + gba::camera_full_column(mask, m)];
     }
     return GBA_OK;
   });
@@ -1468,6 +1712,14 @@ int gba_schur_step(const gba_problem* problem, const double* x, const double* ne
     }
     for (size_t i = 0; i < x0p.size(); ++i) delta_x[i] = x0p[i] - x1p[i];
     std::copy(di.begin(), di.end(), delta_x + x0p.size());
+    if (pi.cps > 0) {   // free cameras: x_c - (x_c - delta_c)
+      std::vector<double> c0(10 * size_t(pi.num_cams)), c1(c0.size());
+      GBA_CUDA(cudaMemcpy(c0.data(), P.d.x_cam[0], sizeof(double) * c0.size(), cudaMemcpyDeviceToHost));
+      GBA_CUDA(cudaMemcpy(c1.data(), P.d.x_cam[1], sizeof(double) * c1.size(), cudaMemcpyDeviceToHost));
+      double* dc = delta_x + x0p.size() + di.size();
+      for (int c = 0; c < pi.num_cams; ++c)
+        for (int m = 0; m < pi.cps; ++m) dc[(size_t)pi.cps * c + m] = c0[10 * c + m] - c1[10 * c + m];
+    }
     return GBA_OK;
   });
   gba_plan_destroy(plan);

@@ -293,15 +293,19 @@ def vector_function(scene, x, precision=abi.PRECISION_FP64):
     return y
 
 
-def jacobian(scene, x, precision=abi.PRECISION_FP64):
+def jacobian(scene, x, precision=abi.PRECISION_FP64, camera=False):
+    """Per-key blocks (jp [K,2,3], ji [K,2,6]; with camera=True also the
+    free cameras' jc [K,2,cps])."""
     cp = abi.CProblem(scene)
     x = _f64(x)
     K = scene.number_of_keys
     jp = np.zeros((K, 2, 3))
     ji = np.zeros((K, 2, 6))
-    _check(lib().gba_jacobian(cp.ref, abi.dptr(x), abi.dptr(jp), abi.dptr(ji), None, precision),
+    jc = np.zeros((K, 2, max(cp.cps, 1))) if camera else None
+    _check(lib().gba_jacobian(cp.ref, abi.dptr(x), abi.dptr(jp), abi.dptr(ji),
+                              abi.dptr(jc) if camera else None, precision),
            "gba_jacobian")
-    return jp, ji
+    return (jp, ji, jc[:, :, :cp.cps]) if camera else (jp, ji)
 
 
 def cost(scene, x, near_y=None, options=None):

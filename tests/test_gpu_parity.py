@@ -249,10 +249,10 @@ def test_errors_are_reported(gba):
     with pytest.raises(gba.GbaError) as e:
         gba.solve(dup)
     assert e.value.status == abi.GBA_ERR_DUPLICATE
-    free_cams = synthetic.Scene(**{**s.__dict__})
-    free_cams.fix_mask = 0
+    fixed_points = synthetic.Scene(**{**s.__dict__})
+    fixed_points.fix_mask = abi.FIX_POINTS | abi.FIX_CAMERAS
     with pytest.raises(gba.GbaError) as e:
-        gba.solve(free_cams, x0=np.concatenate([s.x0, s.cameras.reshape(-1)]))
+        gba.solve(fixed_points, x0=s.x0[3 * s.number_of_points:])
     assert e.value.status == abi.GBA_ERR_UNSUPPORTED
 
 

@@ -44,6 +44,11 @@ LINEAR_DENSE_CHOLESKY = 0
 LINEAR_PCG = 1
 
 NUM_STAGES = 12
+STOP_MAX_ITERATIONS = 0
+STOP_SMALL_GRADIENT = 1
+STOP_SMALL_STEP = 2
+STOP_ERROR = 3
+STOP_SMALL_COST_CHANGE = 4
 STAGE_NAMES = ["linearize", "point_schur", "assemble", "factor", "backsub", "cost",
                "control", "assemble_dense", "solve", "image_reduce", "image_prep", "reserved"]
 
@@ -90,7 +95,8 @@ class Options(C.Structure):
         ("huber_delta", C.c_double), ("linear_solver", C.c_int32),
         ("pcg_max_iterations", C.c_int32), ("pcg_relative_tolerance", C.c_double),
         ("use_cuda_graph", C.c_int32), ("profile", C.c_int32), ("device", C.c_int32),
-        ("shared_device", C.c_int32), ("reserved_", C.c_int32 * 6),
+        ("shared_device", C.c_int32), ("function_tolerance", C.c_double),
+        ("reserved_", C.c_int32 * 4),
     ]
 
 
@@ -131,7 +137,7 @@ class ServerStats(C.Structure):
 def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PRECISION_FP64,
                  loss=LOSS_TRIVIAL, huber_delta=1.0, linear_solver=LINEAR_DENSE_CHOLESKY,
                  pcg_max_iterations=100, pcg_relative_tolerance=1e-6, use_cuda_graph=1,
-                 profile=0, device=0, shared_device=0) -> Options:
+                 profile=0, device=0, shared_device=0, function_tolerance=0.0) -> Options:
     """Defaults of the reference's relative-pair test
     (test_camera_shared_relative_pair.cpp:976-979)."""
     o = Options()
@@ -142,6 +148,7 @@ def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PR
     o.pcg_max_iterations, o.pcg_relative_tolerance = pcg_max_iterations, pcg_relative_tolerance
     o.use_cuda_graph, o.profile, o.device = use_cuda_graph, profile, device
     o.shared_device = shared_device
+    o.function_tolerance = function_tolerance
     return o
 
 

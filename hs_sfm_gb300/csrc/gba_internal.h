@@ -78,6 +78,7 @@ struct DevPlan {
   int loss;
   double huber_delta;
   double tau, eps1, eps2;
+  double ftol;        // relative cost decrease that stops (0: off)
   int max_iterations;
   int has_key_weights;
   int max_n, max_nt;  // largest reduced system in the batch

@@ -2613,6 +2613,10 @@ __global__ void k_ctrl_accept(DevPlan d) {
   const double denom = st.mu * st.dn2 + st.gd + st.er;
   const double rho = (st.F - Fn) / denom;
   if (isfinite(Fn) && denom > 0.0 && rho > 0.0) {
+    if (d.ftol > 0.0 && st.F - Fn <= d.ftol * st.F) {   // Ceres' function tolerance
+      st.active = 0;
+      st.stop = GBA_STOP_SMALL_COST_CHANGE;
+    }
     st.parity ^= 1;
     st.F = Fn;
     st.raw = raw_n;

@@ -780,6 +780,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.tau = opt.tau;
   D.eps1 = opt.eps1;
   D.eps2 = opt.eps2;
+  D.ftol = opt.function_tolerance;
   D.max_iterations = opt.max_iterations;
   D.has_key_weights = any_weights;
   D.max_n = max_n;
@@ -1290,7 +1291,7 @@ int gba_plan_create(const gba_problem* problems, const double* const* near_ys, i
     return GBA_ERR_INVALID;
   if (options->precision != GBA_PRECISION_FP64 && options->precision != GBA_PRECISION_MIXED)
     return GBA_ERR_INVALID;
-  if (options->max_iterations < 0) return GBA_ERR_INVALID;
+  if (options->max_iterations < 0 || !(options->function_tolerance >= 0.0)) return GBA_ERR_INVALID;
   gba_plan* p = nullptr;
   try {
     p = new gba_plan();

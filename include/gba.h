@@ -163,7 +163,11 @@ typedef struct gba_options {
    * it); the grid-wide dataflow factorization, which wants every SM, is then
    * not used. */
   int32_t shared_device;
-  int32_t reserved_[6];
+  /* Stop after an accepted step whose cost decrease is at most this
+   * fraction of the cost before it (Ceres' function_tolerance,
+   * camera_shared_ceres_optimizor.hpp:478); 0 disables the test. */
+  double function_tolerance;
+  int32_t reserved_[4];
 } gba_options;
 
 /* Fills the defaults used by the reference's relative-pair test
@@ -175,6 +179,7 @@ GBA_API void gba_default_options(gba_options* options);
 #define GBA_STOP_SMALL_GRADIENT 1
 #define GBA_STOP_SMALL_STEP     2
 #define GBA_STOP_ERROR          3
+#define GBA_STOP_SMALL_COST_CHANGE 4
 
 #define GBA_NUM_STAGES 12
 /* stage indices of gba_report.stage_ms */

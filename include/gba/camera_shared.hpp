@@ -5,6 +5,7 @@
 //   CameraSharedVectorFunction<S>            camera_shared_vector_function.hpp:20-764
 //   CameraSharedYCovarianceInverse<S>        camera_shared_y_covariance_inverse.hpp:18-149
 //   CameraSharedLevenbergMarquardtOptimizor  camera_shared_levenberg_marquardt_optimizor.hpp:19-63
+//   CameraSharedCeresOptimizor               camera_shared_ceres_optimizor.hpp:163-500
 //
 // The optimizer's operator() marshals the problem into a gba_problem (the
 // feature maps and the image-camera map are passed without copying: they
@@ -370,6 +371,70 @@ class CameraSharedLevenbergMarquardtOptimizor<CameraSharedVectorFunction<_Scalar
   gba_options options_;
   mutable int last_status_ = GBA_OK;
   mutable gba_report last_report_ = {};
+};
+
+// ---------------------------------------------------------------------------
+// CameraSharedCeresOptimizor (camera_shared_ceres_optimizor.hpp:163-500), the
+// optimizer of the production pipeline (sfm_pipeline/bundle_adjustment_optimizor.hpp:48-49),
+// with its constructor: (initial_x, number_of_threads = 1,
+// max_num_iterations = 50, function_tolerance = 1e-6,
+// parameter_tolerance = 1e-8).  The same model is solved by the device LM
+// with the reference's robust loss, Huber(1.0) on every key (:253), and its
+// stops: max_num_iterations iterations, an accepted step lowering the cost
+// by at most function_tolerance of it, a step with
+// ||delta|| <= parameter_tolerance (||x|| + parameter_tolerance), and
+// Ceres' default gradient tolerance 1e-10 on ||g||inf.  number_of_threads
+// is kept and not used (one GPU solves).  As in the reference, every group
+// must be free and all three intrinsic groups computed (:193-202), else -1.
+// ---------------------------------------------------------------------------
+template <typename _VectorFunction>
+class CameraSharedCeresOptimizor;
+
+template <typename _Scalar>
+class CameraSharedCeresOptimizor<CameraSharedVectorFunction<_Scalar> > {
+ public:
+  typedef _Scalar Scalar;
+  typedef int Err;
+  typedef CameraSharedVectorFunction<Scalar> VectorFunction;
+  typedef typename VectorFunction::Index Index;
+  typedef typename VectorFunction::XVector XVector;
+  typedef typename VectorFunction::YVector YVector;
+  typedef CameraSharedYCovarianceInverse<Scalar> YCovarianceInverse;
+
+  template <typename XV>
+  explicit CameraSharedCeresOptimizor(const XV& initial_x, int number_of_threads = 1,
+                                      int max_num_iterations = 50,
+                                      double function_tolerance = 1e-6,
+                                      double parameter_tolerance = 1e-8)
+      : lm_(initial_x, size_t(max_num_iterations > 0 ? max_num_iterations : 0), Scalar(1e-3),
+            Scalar(1e-10), Scalar(parameter_tolerance)),
+        number_of_threads_(number_of_threads) {
+    gba_options& o = lm_.options();
+    o.loss = GBA_LOSS_HUBER;
+    o.huber_delta = 1.0;
+    o.function_tolerance = function_tolerance;
+  }
+
+  // Solver choices beyond the reference's constructor (precision, device).
+  gba_options& options() { return lm_.options(); }
+  int number_of_threads() const { return number_of_threads_; }
+  int last_status() const { return lm_.last_status(); }
+  const gba_report& last_report() const { return lm_.last_report(); }
+
+  template <typename YV, typename XV>
+  Err operator()(const VectorFunction& vf, const YV& near_y, const YCovarianceInverse& cov,
+                 XV& optimized_x) const {
+    const IntrinsicComputationsMask& m = vf.intrinsic_computations_mask();
+    if (vf.is_fix_points() || vf.is_fix_images() || vf.is_fix_cameras() ||
+        !m[COMPUTE_RADIAL_DISTORTION] || !m[COMPUTE_DECENTERING_DISTORTION] ||
+        !m[COMPUTE_INTRINSIC_PARAMS])
+      return -1;
+    return lm_(vf, near_y, cov, optimized_x);
+  }
+
+ private:
+  CameraSharedLevenbergMarquardtOptimizor<VectorFunction> lm_;
+  int number_of_threads_;
 };
 
 }  // namespace gba

@@ -1374,9 +1374,19 @@ int oracle_lm_solve(const gba_problem* problem, const double* near_y,
     double denom = mu * dn * dn + gradient_dot(B, dx.data());
     double rho = (F - F_new) / denom;
     if (std::isfinite(F_new) && rho > 0) {
+      // Ceres' function tolerance (camera_shared_ceres_optimizor.hpp:478):
+      // stop once an accepted step lowers F by at most ftol F
+      const bool small_change = opt->function_tolerance > 0 && F - F_new <= opt->function_tolerance * F;
       std::copy(x_new.begin(), x_new.end(), x);
       r.swap(r_new);
       F = F_new;
+      if (small_change) {
+        R.accepted++;
+        R.stop_reason = GBA_STOP_SMALL_COST_CHANGE;
+        double t = 2 * rho - 1;
+        mu *= std::max(1.0 / 3.0, 1 - t * t * t);
+        break;
+      }
       build_blocks(m, x, r, L, B);
       ginf = gradient_inf_norm(B);
       found = ginf <= opt->eps1;

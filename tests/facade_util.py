@@ -20,10 +20,10 @@ def build_facade(out_dir):
     return exe
 
 
-def write_problem(path, scene, iters):
+def write_problem(path, scene, iters, mode=0):
     with open(path, "wb") as fh:
         np.array([scene.number_of_points, scene.number_of_images, scene.number_of_cameras,
-                  scene.number_of_keys, scene.intrinsic_mask, iters], np.int64).tofile(fh)
+                  scene.number_of_keys, scene.intrinsic_mask, iters, mode], np.int64).tofile(fh)
         np.ascontiguousarray(scene.feature_maps, np.int64).tofile(fh)
         np.ascontiguousarray(scene.image_camera_map, np.int64).tofile(fh)
         np.ascontiguousarray(scene.cameras, np.float64).tofile(fh)

@@ -38,3 +38,42 @@ def test_facade_solve_matches_oracle(tmp_path):
                                                                     eps2=0.0))
     c = oracle.cost(s, x, s.near_y)
     assert abs(c - rref.final_cost) <= 1e-6 * rref.final_cost
+
+
+def test_ceres_signature_refuses_fixed_cameras(tmp_path):
+    # CameraSharedCeresOptimizor needs every group free (camera_shared_ceres_optimizor.hpp:193-202)
+    exe = build_facade(str(tmp_path))
+    s = synthetic.full_model_scene(seed=2, num_images=5, num_points=60, fix_mask=abi.FIX_CAMERAS,
+                                   constraints=False, covariances=False)
+    prob = tmp_path / "p.bin"
+    write_problem(prob, s, 5, mode=2)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin")], capture_output=True, text=True)
+    assert r.returncode == 1
+    assert r.stdout.startswith("err -1")
+
+
+@pytest.mark.gpu
+def test_ceres_signature_solve_matches_oracle(tmp_path):
+    # the production caller's optimizer: free full-model cameras, Huber(1.0),
+    # Ceres' stops, against the oracle run with the same options
+    import oracle
+    exe = build_facade(str(tmp_path))
+    s = synthetic.full_model_scene(seed=4, num_images=12, num_points=500, num_cameras=1,
+                                   fix_mask=0, constraints=False, covariances=False,
+                                   obs_per_point=4)
+    prob = tmp_path / "p.bin"
+    write_problem(prob, s, 30, mode=1)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    x = np.fromfile(tmp_path / "x.bin", dtype=np.float64)
+    assert x.shape == s.x0.shape
+    opt = abi.make_options(max_iterations=30, eps1=1e-10, eps2=1e-8, loss=abi.LOSS_HUBER,
+                           huber_delta=1.0, function_tolerance=1e-6)
+    err, x_ref, rref = oracle.lm_solve(s, options=opt)
+    assert err == 0
+    toks = r.stdout.split()
+    fields = dict(zip(toks[0::2], toks[1::2]))
+    assert int(fields["iterations"]) == rref.iterations
+    assert int(fields["stop"]) == rref.stop_reason
+    c = oracle.cost(s, x, s.near_y, loss=abi.LOSS_HUBER, huber_delta=1.0)
+    assert abs(c - rref.final_cost) <= 1e-9 * rref.final_cost

@@ -151,6 +151,19 @@ def test_lm_with_stopping_criteria_fp64(gba):
     np.testing.assert_allclose(x, x_ref, rtol=0, atol=1e-7)
 
 
+def test_lm_function_tolerance_stop(gba):
+    # Ceres' function_tolerance: stop after an accepted step that lowers the
+    # cost by at most ftol of it (camera_shared_ceres_optimizor.hpp:478)
+    s = synthetic.config(0)
+    opt = abi.make_options(max_iterations=50, eps1=0.0, eps2=0.0, function_tolerance=1e-6)
+    x, rep = gba.solve(s, opt)
+    err, x_ref, rref = oracle.lm_solve(s, options=opt)
+    assert rref.stop_reason == abi.STOP_SMALL_COST_CHANGE and rref.iterations < 50
+    assert rep.stop_reason == rref.stop_reason
+    assert rep.iterations == rref.iterations and rep.accepted == rref.accepted
+    np.testing.assert_allclose(x, x_ref, rtol=0, atol=1e-7)
+
+
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
 def test_lm_distorted_with_key_weights(gba, precision):
     s = shuffled(distorted_ring(num_images=12, num_points=500, k=5), seed=4)

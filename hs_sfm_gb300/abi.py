@@ -85,6 +85,8 @@ class Problem(C.Structure):
         ("number_of_camera_constraints", C.c_int64),
         ("camera_constraints", C.POINTER(CameraConstraint)),
         ("key_covariance_inverse", _dp), ("constraint_weights", _dp),
+        ("number_of_point_priors", C.c_int64), ("point_prior_ids", _i64p),
+        ("point_prior_information", _dp),
     ]
 
 
@@ -208,8 +210,14 @@ def constraint_rows(s):
     return rows
 
 
+def point_priors(s):
+    """Point ids of the problem's priors (ground control points), or []."""
+    return list(getattr(s, "point_priors", None) or [])
+
+
 def y_size(s) -> int:
-    return 2 * s.number_of_keys + len(constraint_rows(s))
+    """Keys, constraint rows, then 3 rows per point prior."""
+    return 2 * s.number_of_keys + len(constraint_rows(s)) + 3 * len(point_priors(s))
 
 
 def _ptr(a, typ):
@@ -267,6 +275,13 @@ class CProblem:
         kci = getattr(s, "key_covariance_inverse", None)
         p.key_covariance_inverse = dbl(kci)
         p.constraint_weights = dbl(getattr(s, "constraint_weights", None))
+        pri = point_priors(s)
+        p.number_of_point_priors = len(pri)
+        if pri:
+            ids = np.ascontiguousarray(pri, dtype=np.int64)
+            self.keep.append(ids)
+            p.point_prior_ids = _ptr(ids, C.c_int64)
+            p.point_prior_information = dbl(getattr(s, "prior_information", None))
         self.problem = p
         self.x_size = x_size(s)
         self.y_size = y_size(s)

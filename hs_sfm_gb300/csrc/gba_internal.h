@@ -208,7 +208,15 @@ struct DevPlan {
   const int* img_cons_off;        // [I + 1] into cons_by_img
   const int* cons_by_img;
   const int* prob_cons_off;       // [B + 1] rows of each problem
-  double* cons_cost;              // [B] sum w (x - y)^2 at the x of the last cost launch
+  double* cons_cost;              // [B] constraint and prior terms of the cost at the x of the last cost launch
+  // point priors (ground control points): 3 rows each after the constraint rows
+  int n_priors;
+  const int* pt_prior_off;        // [P + 1] into prior_by_pt, or null without priors
+  const int* prior_by_pt;
+  const int* prior_pt;            // [n] global point of each prior
+  const double* prior_y;          // [3 n] observed coordinates
+  const double* prior_info;       // [9 n] inverse covariance, row-major
+  const int* prob_prior_off;      // [B + 1] priors of each problem
   double* pt_chunk_sum;           // [3 * n_pt_chunks] dn2, xn2, gd
   double* img_chunk_sum;          // [3 * n_img_chunks]
   unsigned long long* launch_counter; // device-side count (unused: host counts)

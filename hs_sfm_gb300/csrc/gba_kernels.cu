@@ -510,8 +510,9 @@ __global__ void k_image_prep(DevPlan d, int which) {
   IL[6] = T(ct); IL[7] = T(s); IL[8] = T(c); IL[9] = T(a1); IL[10] = T(a2); IL[11] = T(0);
 }
 
-// Soft-constraint part of the cost, sum w (x - y)^2 (no loss), one CTA per
-// problem over its rows (camera_shared_mahalanobis_distance_calculator.hpp:28-58).
+// Soft-constraint and point-prior part of the cost, sum w (x - y)^2 and
+// (x - y)^T L (x - y) (no loss), one CTA per problem over its rows
+// (camera_shared_mahalanobis_distance_calculator.hpp:28-58).
 __global__ void __launch_bounds__(256) k_cons_cost(DevPlan d, int which) {
   __shared__ double red[32];
   const int p = blockIdx.x;
@@ -519,15 +520,25 @@ __global__ void __launch_bounds__(256) k_cons_cost(DevPlan d, int which) {
   if (which == 0 ? !st.active : !st.evaluate) return;
   const int par = which ? 1 - st.parity : st.parity;
   double acc = 0.0;
-  for (int r = d.prob_cons_off[p] + threadIdx.x; r < d.prob_cons_off[p + 1]; r += blockDim.x) {
-    const int4 c = d.cons[r];
-    const double2 yw = d.cons_yw[r];
-    const double x = c.x == 0   ? d.x_pt[par][3LL * c.y + c.z]
-                     : c.x == 1 ? d.x_img[par][6LL * c.y + c.z]
-                                : d.x_cam[par][10LL * c.y + c.z];
-    const double v = x - yw.x;
-    acc += yw.y * v * v;
-  }
+  if (d.n_cons > 0)
+    for (int r = d.prob_cons_off[p] + threadIdx.x; r < d.prob_cons_off[p + 1]; r += blockDim.x) {
+      const int4 c = d.cons[r];
+      const double2 yw = d.cons_yw[r];
+      const double x = c.x == 0   ? d.x_pt[par][3LL * c.y + c.z]
+                       : c.x == 1 ? d.x_img[par][6LL * c.y + c.z]
+                                  : d.x_cam[par][10LL * c.y + c.z];
+      const double v = x - yw.x;
+      acc += yw.y * v * v;
+    }
+  if (d.n_priors > 0)   // (x - y)^T L (x - y) per prior (ba_gcp_constrained_mahalanobis_distance_calculator.hpp:55-62)
+    for (int i = d.prob_prior_off[p] + threadIdx.x; i < d.prob_prior_off[p + 1]; i += blockDim.x) {
+      const double* xp = d.x_pt[par] + 3LL * d.prior_pt[i];
+      const double* L = d.prior_info + 9LL * i;
+      double v[3];
+      for (int a = 0; a < 3; ++a) v[a] = xp[a] - d.prior_y[3LL * i + a];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) acc += v[a] * L[3 * a + b] * v[b];
+    }
   acc = block_sum(acc, red);
   if (threadIdx.x == 0) d.cons_cost[p] = acc;
 }
@@ -788,6 +799,25 @@ __global__ void __launch_bounds__(kPointChunk) k_point_reduce(DevPlan d) {
         const double2 yw = d.cons_yw[row];
         V[b == 0 ? 0 : (b == 1 ? 3 : 5)] += T(yw.y);
         g[b] += T(yw.y * (xp[b] - yw.x));
+      }
+    }
+    if (d.pt_prior_off) {   // point priors: V += L (its symmetric part), g += L (x - y)
+      // (ba_gcp_constrained_normal_equation_builder.hpp:59-72)
+      const double* xp = d.x_pt[st.parity] + 3LL * pt;
+      for (int c = d.pt_prior_off[pt]; c < d.pt_prior_off[pt + 1]; ++c) {
+        const int i = d.prior_by_pt[c];
+        const double* L = d.prior_info + 9LL * i;
+        const double v0 = xp[0] - d.prior_y[3LL * i], v1 = xp[1] - d.prior_y[3LL * i + 1],
+                     v2 = xp[2] - d.prior_y[3LL * i + 2];
+        V[0] += T(L[0]);
+        V[1] += T(0.5 * (L[1] + L[3]));
+        V[2] += T(0.5 * (L[2] + L[6]));
+        V[3] += T(L[4]);
+        V[4] += T(0.5 * (L[5] + L[7]));
+        V[5] += T(L[8]);
+        g[0] += T(L[0] * v0 + L[1] * v1 + L[2] * v2);
+        g[1] += T(L[3] * v0 + L[4] * v1 + L[5] * v2);
+        g[2] += T(L[6] * v0 + L[7] * v1 + L[8] * v2);
       }
     }
     T pv[12] = {V[0], V[1], V[2], V[3], V[4], V[5], g[0], g[1], g[2], T(0), T(0), T(0)};
@@ -2764,7 +2794,7 @@ int launch_cost(const DevPlan& d, int which, cudaStream_t s) {
       k_cost<double><<<d.n_key_chunks, 256, 0, s>>>(d, which);
     ++n;
   }
-  if (d.n_cons > 0) {
+  if (d.n_cons > 0 || d.n_priors > 0) {
     k_cons_cost<<<d.B, 256, 0, s>>>(d, which);
     ++n;
   }

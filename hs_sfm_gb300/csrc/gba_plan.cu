@@ -249,6 +249,10 @@ int validate(const gba_problem& p, bool pcg) {
   for (int64_t c = 0; c < p.number_of_image_constraints; ++c)
     if (p.image_constraints[c].image_id < 0 || p.image_constraints[c].image_id >= p.number_of_images)
       return GBA_ERR_BAD_INDEX;
+  if (p.number_of_point_priors < 0 || (p.number_of_point_priors > 0 && !p.point_prior_ids))
+    return GBA_ERR_INVALID;
+  for (int64_t i = 0; i < p.number_of_point_priors; ++i)
+    if (p.point_prior_ids[i] < 0 || p.point_prior_ids[i] >= p.number_of_points) return GBA_ERR_BAD_INDEX;
   if (p.number_of_points > INT32_MAX / 4 || p.number_of_keys > INT32_MAX / 4)
     return GBA_ERR_INVALID;
   // the dense reduced system of one problem is at most 12288^2 doubles
@@ -340,6 +344,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   std::vector<int4> cons;          // (group 0 point / 1 image / 2 camera, global index, parameter, problem)
   std::vector<double2> cons_yw;    // (observed value, weight)
   std::vector<int> prob_cons_off(1, 0);
+  std::vector<int> prior_pt, prob_prior_off(1, 0);
+  std::vector<double> prior_y, prior_info;
   prob.resize(nprob);
   key_sorted_to_orig.resize(nprob);
   x_size.resize(nprob);
@@ -401,6 +407,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     std::vector<double2> cons_yw;
     std::vector<int> pt_rec_off;       // [np + 1] camera records of each point (free cameras)
     std::vector<int> rec_ext;          // local reduced-system image of each camera record
+    std::vector<int> prior_pt;         // point priors: global point, observed y, information
+    std::vector<double> prior_y, prior_info;
   };
   std::vector<Piece> pieces(nprob);
   auto build_one = [&](int q, int inner) {
@@ -681,6 +689,15 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
             if (cc.intrinsic_mask & (1u << b)) add(2, cb + cc.camera_id, off + b);
         }
       }
+      // point priors: 3 rows each after the constraint rows
+      // (ba_gcp_constrained_vector_function.hpp:100-108)
+      for (int64_t i = 0; i < p.number_of_point_priors; ++i) {
+        out.prior_pt.push_back(int(pb + p.point_prior_ids[i]));
+        for (int a = 0; a < 3; ++a) out.prior_y.push_back(y[2LL * nk + r + 3 * i + a]);
+        for (int j = 0; j < 9; ++j)
+          out.prior_info.push_back(p.point_prior_information ? p.point_prior_information[9 * i + j]
+                                                             : double(j % 4 == 0));
+      }
     }
   };
   if (nprob == 1) {
@@ -762,6 +779,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     cons.insert(cons.end(), pc.cons.begin(), pc.cons.end());
     cons_yw.insert(cons_yw.end(), pc.cons_yw.begin(), pc.cons_yw.end());
     prob_cons_off.push_back(int(cons.size()));
+    prior_pt.insert(prior_pt.end(), pc.prior_pt.begin(), pc.prior_pt.end());
+    prior_y.insert(prior_y.end(), pc.prior_y.begin(), pc.prior_y.end());
+    prior_info.insert(prior_info.end(), pc.prior_info.begin(), pc.prior_info.end());
+    prob_prior_off.push_back(int(prior_pt.size()));
     std::vector<int>().swap(pc.blk_map);   // release as we go
     std::vector<int2>().swap(pc.pairs);
   }
@@ -990,6 +1011,25 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.pt_cons_off = nullptr;
   D.img_cons_off = nullptr;
   D.cons_cost = nullptr;
+  D.n_priors = int(prior_pt.size());
+  D.pt_prior_off = nullptr;
+  if (!prior_pt.empty()) {   // priors of each point, in prior order
+    std::vector<int> off(P + 1, 0), by_pt(prior_pt.size());
+    for (int v : prior_pt) off[v + 1]++;
+    for (int64_t i = 0; i < P; ++i) off[i + 1] += off[i];
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (size_t i = 0; i < prior_pt.size(); ++i) by_pt[fill[prior_pt[i]]++] = int(i);
+    D.pt_prior_off = arena.upload(off);
+    D.prior_by_pt = arena.upload(by_pt);
+    D.prior_pt = arena.upload(prior_pt);
+    D.prior_y = arena.upload(prior_y);
+    D.prior_info = arena.upload(prior_info);
+    D.prob_prior_off = arena.upload(prob_prior_off);
+  }
+  if (!cons.empty() || !prior_pt.empty()) {
+    D.prob_cons_off = arena.upload(prob_cons_off);
+    D.cons_cost = arena.alloc<double>(nprob);
+  }
   if (!cons.empty()) {
     // rows of each point / image in y order, for the linearization
     std::vector<int> pt_off(P + 1, 0), img_off(I + 1, 0);
@@ -1009,8 +1049,6 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     D.cons_by_pt = arena.upload(by_pt);
     D.img_cons_off = arena.upload(img_off);
     D.cons_by_img = arena.upload(by_img);
-    D.prob_cons_off = arena.upload(prob_cons_off);
-    D.cons_cost = arena.alloc<double>(nprob);
   }
   D.pt_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(pt_chunks.size(), 1));
   D.img_chunk_sum = arena.alloc<double>(3 * std::max<size_t>(img_chunks.size(), 1));
@@ -1234,6 +1272,7 @@ int64_t gba_y_size(const gba_problem* p) {
       n += __builtin_popcount(cc.radial_mask & 7u) + __builtin_popcount(cc.decentering_mask & 3u) +
            __builtin_popcount(cc.intrinsic_mask & 31u);
     }
+  if (p->number_of_point_priors > 0) n += 3 * p->number_of_point_priors;
   return n;
 }
 
@@ -1580,6 +1619,8 @@ int gba_vector_function(const gba_problem* problem, const double* x, double* y, 
           if (cc.intrinsic_mask & (1u << b)) y[r++] = xv[off + b];
       }
     }
+    for (int64_t i = 0; i < problem->number_of_point_priors; ++i)   // point priors
+      for (int a = 0; a < 3; ++a) y[r++] = x[3 * problem->point_prior_ids[i] + a];
     return GBA_OK;
   });
   gba_plan_destroy(plan);

@@ -153,6 +153,8 @@ class Scene:
     camera_constraints: list | None = None  # [(camera_id, radial, decentering, intrinsic)]
     key_covariance_inverse: np.ndarray | None = None  # [K,2,2]
     constraint_weights: np.ndarray | None = None
+    point_priors: list | None = None             # [point_id] (ground control points)
+    prior_information: np.ndarray | None = None  # [n,3,3] inverse covariances
 
     @property
     def number_of_points(self):
@@ -424,6 +426,30 @@ def config(n: int, **kw):
 # Small full-model scenes for the stage tests: several cameras, every
 # intrinsic group, optional soft constraints and per-key covariances.
 # ---------------------------------------------------------------------------
+def gcp_scene(seed=0, num_images=10, num_points=500, num_gcps=8, obs_per_point=4,
+              key_sigma=1e-3, gcp_sigma=0.02, name="gcp"):
+    """The GCP-constrained model (ba_gcp_constrained_vector_function.hpp):
+    normalized keys (no intrinsics: mask 0, one camera without parameters)
+    of the ring geometry, key noise key_sigma with inverse covariance
+    I / key_sigma^2, and num_gcps ground control points whose observed
+    coordinates carry correlated noise of a random 3x3 covariance
+    (scale gcp_sigma) with that covariance's inverse as their prior."""
+    s = ring_scene(num_images=num_images, num_points=num_points, obs_per_point=obs_per_point,
+                   seed=seed, mask=0, fix_mask=FIX_CAMERAS, name=name)
+    rng = np.random.default_rng(seed + 7919)
+    keys = project_keys(s.points, s.images, s.cameras, s.image_camera_map, s.feature_maps, 0)
+    obs = (keys + rng.normal(0.0, key_sigma, keys.shape)).reshape(-1)
+    gcps = np.sort(rng.choice(num_points, num_gcps, replace=False)).astype(np.int64)
+    A = rng.normal(0.0, 0.4, size=(num_gcps, 3, 3))
+    cov = gcp_sigma ** 2 * (np.einsum('nij,nkj->nik', A, A) + np.eye(3)[None])
+    noise = np.einsum('nij,nj->ni', np.linalg.cholesky(cov), rng.normal(size=(num_gcps, 3)))
+    s.near_y = np.concatenate([obs, (s.points[gcps] + noise).reshape(-1)])
+    s.key_covariance_inverse = np.tile(np.eye(2) / key_sigma ** 2, (s.number_of_keys, 1, 1))
+    s.point_priors = [int(v) for v in gcps]
+    s.prior_information = np.linalg.inv(cov)
+    return s
+
+
 def full_model_scene(seed=0, num_images=6, num_points=60, num_cameras=2, fix_mask=0,
                      mask=COMPUTE_RADIAL | COMPUTE_DECENTERING | COMPUTE_INTRINSIC,
                      constraints=True, covariances=True, obs_per_point=3):

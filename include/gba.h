@@ -123,6 +123,15 @@ typedef struct gba_problem {
    * (NULL = 1 for every constraint row). */
   const double* key_covariance_inverse;
   const double* constraint_weights;
+  /* Point priors: the ground control points of the GCP-constrained model
+   * (ba_gcp_constrained_vector_function.hpp:60-110,
+   * ba_gcp_constrained_normal_equation_builder.hpp:42-75).  y holds the
+   * observed coordinates of each prior's point, 3 rows per prior after the
+   * constraint rows, weighted by the prior's full 3x3 inverse covariance
+   * (ba_gcp_constrained_y_covariance_inverse.hpp:18-25); points must be free. */
+  int64_t number_of_point_priors;
+  const int64_t* point_prior_ids;          /* [n] point ids */
+  const double* point_prior_information;   /* [9n] row-major 3x3; NULL = identity */
 } gba_problem;
 
 /* Sizes derived from a problem (GetXSize / GetYSize,

@@ -35,6 +35,8 @@ struct Model {
   bool radial = false, decent = false, intr = false;
   int64_t x_image_begin = 0, x_camera_begin = 0, x_size = 0;
   std::vector<ConstraintRow> rows;  // constraint rows in y order
+  int64_t n_priors = 0;             // point priors: 3 rows each after the constraint rows
+  int64_t prior_y_begin = 0;
   int64_t y_size = 0;
   std::vector<int32_t> key_image, key_point, key_camera;
 
@@ -122,8 +124,21 @@ struct Model {
           if (cc.intrinsic_mask & (1u << b)) rows.push_back({2, cc.camera_id, off + b});
       }
     }
-    y_size = 2 * K + int64_t(rows.size());
+    // Point priors (ba_gcp_constrained_vector_function.hpp:60-110): copies
+    // of the prior points' coordinates, weighted by a 3x3 block each.
+    n_priors = p->number_of_point_priors;
+    if (n_priors < 0 || (n_priors > 0 && (!p->point_prior_ids || fixP))) return GBA_ERR_INVALID;
+    for (int64_t i = 0; i < n_priors; ++i)
+      if (p->point_prior_ids[i] < 0 || p->point_prior_ids[i] >= P) return GBA_ERR_BAD_INDEX;
+    prior_y_begin = 2 * K + int64_t(rows.size());
+    y_size = prior_y_begin + 3 * n_priors;
     return GBA_OK;
+  }
+
+  // Inverse covariance of prior i (ba_gcp_constrained_y_covariance_inverse.hpp:18-25).
+  void prior_weight(int64_t i, double L[9]) const {
+    for (int j = 0; j < 9; ++j)
+      L[j] = p->point_prior_information ? p->point_prior_information[9 * i + j] : (j % 4 == 0);
   }
 
   const double* point(int64_t id, const double* x) const {
@@ -438,7 +453,23 @@ int residuals(const Model& m, const double* x, const double* near_y, Vec& r) {
     int64_t yi = 2 * m.K + int64_t(c);
     r[yi] = x[m.row_x_index(m.rows[c])] - near_y[yi];
   }
+  for (int64_t i = 0; i < m.n_priors; ++i)
+    for (int a = 0; a < 3; ++a) {
+      const int64_t yi = m.prior_y_begin + 3 * i + a;
+      r[yi] = x[3 * m.p->point_prior_ids[i] + a] - near_y[yi];
+    }
   return GBA_OK;
+}
+
+// r^T L r of prior i (ba_gcp_constrained_mahalanobis_distance_calculator.hpp:55-62).
+double prior_sq(const Model& m, int64_t i, const double* r) {
+  double L[9];
+  m.prior_weight(i, L);
+  const double* v = r + m.prior_y_begin + 3 * i;
+  double s = 0;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) s += v[a] * L[3 * a + b] * v[b];
+  return s;
 }
 
 double key_sq(const Model& m, int64_t k, const double* r) {
@@ -455,6 +486,7 @@ double cost_of(const Model& m, const Vec& r, const Loss& loss) {
     double v = r[2 * m.K + c];
     F += v * m.row_weight(int64_t(c)) * v;
   }
+  for (int64_t i = 0; i < m.n_priors; ++i) F += prior_sq(m, i, r.data());
   return F;
 }
 
@@ -563,6 +595,18 @@ int build_blocks(const Model& m, const double* x, const Vec& r,
       B.Cb[cps * cps * row.block + (cps + 1) * row.param] += wgt;
       B.gc[cps * row.block + row.param] += wgt * rv;
     }
+  }
+  // Point priors: V_p += L, g_p += L r (ba_gcp_constrained_normal_equation_builder.hpp:59-72).
+  for (int64_t i = 0; i < m.n_priors; ++i) {
+    double L[9];
+    m.prior_weight(i, L);
+    const int64_t pt = m.p->point_prior_ids[i];
+    const double* v = &r[m.prior_y_begin + 3 * i];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        B.V[9 * pt + 3 * a + b] += L[3 * a + b];
+        B.gp[3 * pt + a] += L[3 * a + b] * v[b];
+      }
   }
   return GBA_OK;
 }
@@ -1199,6 +1243,8 @@ int oracle_vector_function(const gba_problem* problem, const double* x, double* 
     image_key(m, m.point(m.key_point[k], x), m.image(m.key_image[k], x),
               m.camera(m.key_camera[k], x), &y[2 * k]);
   for (size_t c = 0; c < m.rows.size(); ++c) y[2 * m.K + c] = x[m.row_x_index(m.rows[c])];
+  for (int64_t i = 0; i < m.n_priors; ++i)
+    for (int a = 0; a < 3; ++a) y[m.prior_y_begin + 3 * i + a] = x[3 * problem->point_prior_ids[i] + a];
   return GBA_OK;
 }
 
@@ -1268,6 +1314,9 @@ int oracle_dense_jacobian(const gba_problem* problem, const double* x, double* J
     }
   }
   for (size_t c = 0; c < m.rows.size(); ++c) J[(2 * m.K + c) * n + m.row_x_index(m.rows[c])] = 1.0;
+  for (int64_t i = 0; i < m.n_priors; ++i)
+    for (int a = 0; a < 3; ++a)
+      J[(m.prior_y_begin + 3 * i + a) * n + 3 * problem->point_prior_ids[i] + a] = 1.0;
   return GBA_OK;
 }
 

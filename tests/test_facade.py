@@ -10,7 +10,7 @@ import pytest
 
 from hs_sfm_gb300 import abi, synthetic
 
-from facade_util import build_facade, write_problem
+from facade_util import build_facade, write_gcp_problem, write_problem
 
 
 def test_facade_builds_and_rejects_bad_initial_x(tmp_path):
@@ -77,3 +77,45 @@ def test_ceres_signature_solve_matches_oracle(tmp_path):
     assert int(fields["stop"]) == rref.stop_reason
     c = oracle.cost(s, x, s.near_y, loss=abi.LOSS_HUBER, huber_delta=1.0)
     assert abs(c - rref.final_cost) <= 1e-9 * rref.final_cost
+
+
+def test_gcp_facade_builds_and_rejects_bad_initial_x(tmp_path):
+    exe = build_facade(str(tmp_path), "gcp_solve")
+    s = synthetic.gcp_scene(seed=1, num_images=5, num_points=60, num_gcps=3)
+    prob = tmp_path / "g.bin"
+    write_gcp_problem(prob, s, 5)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin"), "--bad-size"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1
+    assert r.stdout.startswith("err -1 status -2")
+
+
+@pytest.mark.gpu
+def test_gcp_facade_solve_matches_oracle(tmp_path):
+    # BAGCPConstrainedLevenbergMarquardtOptimizor through the facade: the
+    # naive layout in and out, control points last, against the oracle's
+    # solve of the same problem with point priors
+    import oracle
+    exe = build_facade(str(tmp_path), "gcp_solve")
+    s = synthetic.gcp_scene(seed=6, num_images=9, num_points=350, num_gcps=7)
+    prob = tmp_path / "g.bin"
+    perm = write_gcp_problem(prob, s, 30)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = np.fromfile(tmp_path / "x.bin", dtype=np.float64)
+    C6, P3 = 6 * s.number_of_images, 3 * s.number_of_points
+    xn, y0 = out[:C6 + P3], out[C6 + P3:]
+    # back to the point-prior scene's layout [points][images]
+    pts = np.empty((s.number_of_points, 3))
+    pts[perm] = xn[C6:].reshape(-1, 3)
+    x = np.concatenate([pts.reshape(-1), xn[:C6]])
+    err, x_ref, rref = oracle.lm_solve(s, options=abi.make_options(max_iterations=30))
+    assert err == 0 and rref.stop_reason == abi.STOP_SMALL_STEP
+    c = oracle.cost(s, x, s.near_y)
+    assert abs(c - rref.final_cost) <= 1e-9 * rref.final_cost
+    # the facade's vector function at x0: keys, then the control points
+    fmap = s.feature_maps
+    y_ref = oracle.vector_function(s, s.x0)
+    assert np.allclose(y0[:2 * s.number_of_keys], y_ref[:2 * s.number_of_keys], rtol=1e-13, atol=1e-15)
+    np.testing.assert_array_equal(y0[2 * s.number_of_keys:], y_ref[2 * s.number_of_keys:])
+    del fmap

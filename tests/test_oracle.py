@@ -174,3 +174,61 @@ def test_huber_cost_and_weights():
     rho = np.where(sq <= 1.0, sq, 2 * np.sqrt(sq) - 1.0)
     c = oracle.cost(s, s.x0, s.near_y, loss=abi.LOSS_HUBER, huber_delta=1.0)
     np.testing.assert_allclose(c, rho.sum(), rtol=1e-12)
+
+
+def _dense_lambda_with_priors(s):
+    """The dense inverse covariance of y: key blocks, then 3x3 prior blocks
+    (ba_gcp_constrained_y_covariance_inverse.hpp:18-25)."""
+    K = s.number_of_keys
+    n = abi.y_size(s)
+    L = np.zeros((n, n))
+    for k in range(K):
+        L[2 * k:2 * k + 2, 2 * k:2 * k + 2] = s.key_covariance_inverse[k]
+    b = 2 * K + len(abi.constraint_rows(s))
+    for i in range(len(s.point_priors)):
+        L[b + 3 * i:b + 3 * i + 3, b + 3 * i:b + 3 * i + 3] = s.prior_information[i]
+    return L
+
+
+def test_gcp_builder_vs_dense():
+    """test_ba_gcp_constrained_normal_equation_builder.cpp:150-190: the block
+    normal equations with the ground control points' 3x3 priors against
+    dense J^T Lambda J and J^T Lambda r at 1e-8."""
+    s = synthetic.gcp_scene(seed=1, num_images=6, num_points=80, num_gcps=5)
+    assert abi.y_size(s) == len(s.near_y) == 2 * s.number_of_keys + 15
+    N, g = oracle.normal_equation_dense(s, s.x0, s.near_y)
+    J = oracle.dense_jacobian(s, s.x0)
+    L = _dense_lambda_with_priors(s)
+    r = oracle.vector_function(s, s.x0) - s.near_y
+    ok, e, rel = abs_rel_ok(J.T @ L @ J, N, 1e-8)
+    assert ok, (e, rel)
+    ok, e, rel = abs_rel_ok(J.T @ L @ r, g, 1e-8)
+    assert ok, (e, rel)
+    # the prior rows of y are copies of the prior points (ba_gcp_constrained_vector_function.hpp:100-108)
+    y = oracle.vector_function(s, s.x0)
+    P = np.asarray(s.x0[:3 * s.number_of_points]).reshape(-1, 3)
+    np.testing.assert_array_equal(y[2 * s.number_of_keys:].reshape(-1, 3), P[s.point_priors])
+    c = oracle.cost(s, s.x0, s.near_y)
+    assert abs(c - r @ L @ r) <= 1e-10 * c
+
+
+def test_gcp_priors_fix_the_gauge():
+    """test_ba_gcp_constrained_gauge.cpp: with ground control points the
+    solution lands in the points' own frame, off the truth by no more than
+    the control points' own noise, and fits the data better than the truth."""
+    s = synthetic.gcp_scene(seed=2, num_images=8, num_points=200, num_gcps=6)
+    err, x, rep = oracle.lm_solve(s, options=abi.make_options(max_iterations=30))
+    assert err == 0 and rep.stop_reason == abi.STOP_SMALL_STEP
+    assert rep.final_cost < oracle.cost(s, s.x_true, s.near_y)
+    P = x[:3 * s.number_of_points].reshape(-1, 3)
+    e = np.sqrt(np.mean(np.sum((P - s.points) ** 2, axis=1)))
+    gy = s.near_y[2 * s.number_of_keys:].reshape(-1, 3)
+    e_gcp = np.sqrt(np.mean(np.sum((gy - s.points[s.point_priors]) ** 2, axis=1)))
+    assert e < 1.5 * e_gcp, (e, e_gcp)
+
+
+def test_prior_bad_index_rejected():
+    s = synthetic.gcp_scene(seed=1, num_images=6, num_points=80, num_gcps=3)
+    s.point_priors = [0, 1, s.number_of_points]
+    with pytest.raises(RuntimeError):
+        oracle.cost(s, s.x0, s.near_y)

@@ -136,6 +136,40 @@ class ServerStats(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class Triangulation(C.Structure):
+    _fields_ = [("number_of_views", C.c_int64), ("intrinsics", _dp), ("extrinsics", _dp),
+                ("number_of_points", C.c_int64), ("track_offsets", _i64p),
+                ("track_views", _i64p), ("track_keys", _dp)]
+
+
+class CTriangulation:
+    """Contiguous copies of a triangulation batch and the gba_triangulation
+    that points at them."""
+
+    def __init__(self, t):
+        self.keep = []
+
+        def arr(a, dt, typ):
+            a = np.ascontiguousarray(a, dtype=dt).reshape(-1)
+            self.keep.append(a)
+            return _ptr(a, typ)
+
+        p = Triangulation()
+        p.number_of_views = int(len(t.intrinsics))
+        p.intrinsics = arr(t.intrinsics, np.float64, C.c_double)
+        p.extrinsics = arr(t.extrinsics, np.float64, C.c_double)
+        p.number_of_points = int(len(t.track_offsets) - 1)
+        p.track_offsets = arr(t.track_offsets, np.int64, C.c_int64)
+        p.track_views = arr(t.track_views, np.int64, C.c_int64)
+        p.track_keys = arr(t.track_keys, np.float64, C.c_double)
+        self.problem = p
+        self.n = p.number_of_points
+
+    @property
+    def ref(self):
+        return C.byref(self.problem)
+
+
 def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PRECISION_FP64,
                  loss=LOSS_TRIVIAL, huber_delta=1.0, linear_solver=LINEAR_DENSE_CHOLESKY,
                  pcg_max_iterations=100, pcg_relative_tolerance=1e-6, use_cuda_graph=1,

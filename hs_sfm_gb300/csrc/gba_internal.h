@@ -254,6 +254,9 @@ int launch_backsub(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_step(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_accept(const DevPlan& d, cudaStream_t s);
 
+// Adds kernels launched outside a plan to gba_kernel_launch_count() (gba_plan.cu).
+void count_launches(long long n);
+
 // Stage entry points on a plan (gba_kernels.cu): Jacobian blocks in sorted
 // key order (T precision), vector function (FP64).
 int launch_vector_function(const DevPlan& d, double* y_sorted, cudaStream_t s);

@@ -138,6 +138,8 @@ struct DeviceArena {
 
 }  // namespace
 
+void count_launches(long long n) { g_launches += n; }
+
 // ---------------------------------------------------------------------------
 // Plan
 // ---------------------------------------------------------------------------

@@ -79,6 +79,7 @@ def lib():
     L.gba_server_get_stats.argtypes = [vp, C.POINTER(abi.ServerStats)]
     L.gba_estimate_device_bytes.restype = C.c_int64
     L.gba_estimate_device_bytes.argtypes = [P, C.c_int32]
+    L.gba_triangulate.argtypes = [C.POINTER(abi.Triangulation), O, d, C.POINTER(C.c_int32)]
     _lib = L
     return L
 
@@ -331,3 +332,16 @@ def schur_step(scene, x, mu, near_y=None, options=None):
 
 def kernel_launch_count():
     return lib().gba_kernel_launch_count()
+
+
+def triangulate(batch, options=None):
+    """Batched multi-view triangulation (gba_triangulate) of a
+    synthetic.TriangulationBatch-like object.  Returns (points [n,3],
+    per-point status [n])."""
+    ct = abi.CTriangulation(batch)
+    opt = options if options is not None else abi.make_options()
+    pts = np.zeros((ct.n, 3))
+    st = np.zeros(ct.n, dtype=np.int32)
+    _check(lib().gba_triangulate(ct.ref, C.byref(opt), abi.dptr(pts),
+                                 st.ctypes.data_as(C.POINTER(C.c_int32))), "gba_triangulate")
+    return pts, st

@@ -508,3 +508,61 @@ def full_model_scene(seed=0, num_images=6, num_points=60, num_cameras=2, fix_mas
     if rows:
         scene.constraint_weights = rng.uniform(0.5, 2.0, size=len(rows))
     return scene
+
+
+@dataclasses.dataclass
+class TriangulationBatch:
+    """Views (CameraIntrinsicParams [f skew cx cy pixel_ratio k1 k2 k3 d1 d2],
+    CameraExtrinsicParams [angle-axis world to camera, position]) and point
+    tracks (offsets, view of each observation, observed keys)."""
+    intrinsics: np.ndarray     # [V,10]
+    extrinsics: np.ndarray     # [V,6]
+    track_offsets: np.ndarray  # [n+1]
+    track_views: np.ndarray    # [m]
+    track_keys: np.ndarray     # [m,2]
+    points: np.ndarray         # [n,3] truth
+
+
+def project_views(intrinsics, extrinsics, views, X):
+    """Keys of points X [m,3] in views [m] (sfm_utility/projective_functions.hpp:22-52)."""
+    R = rotvec_to_matrix(extrinsics[views, :3])
+    c = np.einsum('mij,mj->mi', R, X - extrinsics[views, 3:])
+    x, y = c[:, 0] / c[:, 2], c[:, 1] / c[:, 2]
+    K = intrinsics[views]
+    f, s, cx, cy, a, k1, k2, k3, d1, d2 = K.T
+    r2 = x * x + y * y
+    coeff = k1 * r2 + k2 * r2 ** 2 + k3 * r2 ** 3
+    ex = x + coeff * x + 2 * d1 * x * y + d2 * (r2 + 2 * x * x)
+    ey = y + coeff * y + 2 * d2 * x * y + d1 * (r2 + 2 * y * y)
+    return np.stack([f * ex + s * ey + cx, f * a * ey + cy], axis=1)
+
+
+def triangulation_batch(seed=0, num_points=1000, num_views=20, views_range=(2, 8),
+                        noise=0.5, distortion=True):
+    """Views on a ring of radius 10 looking at the origin (each with its own
+    intrinsics), points uniform in [-2,2]^3, each seen by a random subset of
+    views_range views, keys with N(0, noise) pixel noise."""
+    rng = np.random.default_rng(seed)
+    phi = 2 * np.pi * np.arange(num_views) / num_views + rng.uniform(0, 0.1, num_views)
+    centers = np.stack([10 * np.cos(phi), 10 * np.sin(phi), rng.uniform(-1, 1, num_views)], axis=1)
+    R = look_at(centers, np.zeros((num_views, 3)), np.array([0.0, 0.0, 1.0]))
+    extr = np.concatenate([matrix_to_rotvec(R), centers], axis=1)
+    intr = np.zeros((num_views, 10))
+    intr[:, 0] = rng.uniform(900, 1100, num_views)
+    intr[:, 1] = rng.uniform(-1, 1, num_views)
+    intr[:, 2] = rng.uniform(940, 980, num_views)
+    intr[:, 3] = rng.uniform(520, 560, num_views)
+    intr[:, 4] = rng.uniform(0.98, 1.02, num_views)
+    if distortion:
+        intr[:, 5:7] = rng.uniform(-0.05, 0.05, (num_views, 2))
+        intr[:, 7] = rng.uniform(-0.01, 0.01, num_views)
+        intr[:, 8:10] = rng.uniform(-1e-3, 1e-3, (num_views, 2))
+    pts = rng.uniform(-2, 2, size=(num_points, 3))
+    k = rng.integers(views_range[0], views_range[1] + 1, size=num_points)
+    k = np.minimum(k, num_views)
+    off = np.concatenate([[0], np.cumsum(k)]).astype(np.int64)
+    views = np.concatenate([rng.choice(num_views, kk, replace=False) for kk in k]).astype(np.int64)
+    X = np.repeat(pts, k, axis=0)
+    keys = project_views(intr, extr, views, X) + rng.normal(0, noise, (len(views), 2))
+    return TriangulationBatch(intrinsics=intr, extrinsics=extr, track_offsets=off,
+                              track_views=views, track_keys=keys, points=pts)

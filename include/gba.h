@@ -387,6 +387,38 @@ typedef struct gba_device_problem {
 GBA_API int gba_cost_noalloc(const gba_device_problem* problem, int32_t loss,
                              double huber_delta, double* d_cost, void* stream);
 
+/* ---- batched multi-view triangulation ----------------------------------
+ * MultipleViewMaximumLikelihoodEstimator / MultipleViewLevenbergMarquardtOptimizor
+ * (triangulate/multiple_view_maximum_likelihood_estimator.hpp:32-84,
+ * multiple_view_levenberg_marquardt_optimizor.hpp:50-99) for many points at
+ * once: each point is initialised by the linear DLT of its undistorted keys
+ * (multiple_view_dlt.hpp:27-52, sfm_utility/undistortor.hpp:24-80) and
+ * refined by Levenberg-Marquardt on its 3 coordinates against its distorted
+ * keys with identity key weights (options: max_iterations, tau, eps1, eps2).
+ * Views carry CameraIntrinsicParams and CameraExtrinsicParams
+ * (sfm_utility/camera_type.hpp): intrinsics [f skew cx cy pixel_ratio k1 k2
+ * k3 d1 d2], extrinsics [rotation (angle-axis, world to camera), position
+ * (the camera centre)].  Point j is seen by views track_views[t] with keys
+ * track_keys[2t], t in [track_offsets[j], track_offsets[j+1]).  One thread
+ * per point, FP64. */
+typedef struct gba_triangulation {
+  int64_t number_of_views;
+  const double* intrinsics;       /* [10 V] */
+  const double* extrinsics;       /* [6 V]  */
+  int64_t number_of_points;
+  const int64_t* track_offsets;   /* [n + 1], ascending, track_offsets[0] = 0 */
+  const int64_t* track_views;     /* [m] view of each observation            */
+  const double* track_keys;       /* [2 m] observed (distorted) keys         */
+} gba_triangulation;
+
+/* points [3n] out; point_status [n] out (may be NULL): GBA_OK, or
+ * GBA_ERR_INVALID for a track with fewer than 2 views (the reference's -1),
+ * GBA_ERR_NAN when the DLT or the refinement produced no finite point.
+ * Returns GBA_OK when the call ran (per-point failures are in point_status),
+ * else an input error. */
+GBA_API int gba_triangulate(const gba_triangulation* problem, const gba_options* options,
+                            double* points, int32_t* point_status);
+
 /* ---- library ------------------------------------------------------------ */
 GBA_API const char* gba_status_string(int status);
 GBA_API const char* gba_version(void);

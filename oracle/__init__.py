@@ -35,6 +35,8 @@ def lib():
         L.oracle_lm_solve.argtypes = [P, d, C.POINTER(abi.Options), C.c_int32, d,
                                       C.POINTER(abi.Report)]
         L.oracle_time_faithful_iteration.argtypes = [P, d, d, C.c_double, C.c_int32, d]
+        L.oracle_triangulate.argtypes = [C.POINTER(abi.Triangulation), C.POINTER(abi.Options), d,
+                                         C.POINTER(C.c_int32)]
         _lib = L
     return _lib
 
@@ -126,3 +128,14 @@ def time_faithful_iteration(scene, x, mu, row_stride=1):
     _chk(lib().oracle_time_faithful_iteration(cp.ref, abi.dptr(y), abi.dptr(x), mu, row_stride,
                                               abi.dptr(sec)))
     return sec
+
+
+def triangulate(batch, options=None):
+    """Points [n,3] and per-point status of a synthetic.TriangulationBatch."""
+    ct = abi.CTriangulation(batch)
+    opt = options if options is not None else abi.make_options()
+    pts = np.zeros((ct.n, 3))
+    st = np.zeros(ct.n, dtype=np.int32)
+    _chk(lib().oracle_triangulate(ct.ref, C.byref(opt), abi.dptr(pts),
+                                  st.ctypes.data_as(C.POINTER(C.c_int32))))
+    return pts, st

@@ -12,7 +12,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgba_oracle.so")
-SOURCES = [os.path.join(HERE, "gba_oracle.cpp")]
+SOURCES = [os.path.join(HERE, "gba_oracle.cpp"), os.path.join(HERE, "gba_oracle_triangulate.cpp")]
 HEADERS = [os.path.join(HERE, "gba_oracle.h"),
            os.path.join(os.path.dirname(HERE), "include", "gba.h")]
 

@@ -83,6 +83,11 @@ int oracle_time_faithful_iteration(const gba_problem* problem,
                                    double mu, int32_t row_stride,
                                    double* seconds);
 
+/* Batched multi-view triangulation (gba_oracle_triangulate.cpp): DLT of the
+ * undistorted keys, then LM on each point (triangulate/multiple_view_*). */
+int oracle_triangulate(const gba_triangulation* problem, const gba_options* options,
+                       double* points, int32_t* point_status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -232,3 +232,23 @@ def test_prior_bad_index_rejected():
     s.point_priors = [0, 1, s.number_of_points]
     with pytest.raises(RuntimeError):
         oracle.cost(s, s.x0, s.near_y)
+
+
+def test_triangulation_oracle_noise_free_and_refines():
+    """Multi-view triangulation restatement: exact on noise-free tracks with
+    distortion (DLT of undistorted keys, then LM), and the LM lowers the
+    reprojection cost of the DLT start."""
+    b = synthetic.triangulation_batch(seed=1, num_points=500, noise=0.0)
+    P, st = oracle.triangulate(b)
+    assert np.all(st == 0) and np.max(np.abs(P - b.points)) < 1e-9
+    b = synthetic.triangulation_batch(seed=2, num_points=500, noise=1.0)
+    P0, _ = oracle.triangulate(b, abi.make_options(max_iterations=0))
+    P1, _ = oracle.triangulate(b)
+    k = np.diff(b.track_offsets)
+
+    def cost(Pts):
+        r = synthetic.project_views(b.intrinsics, b.extrinsics, b.track_views,
+                                    np.repeat(Pts, k, axis=0)) - b.track_keys
+        return float(np.sum(r * r))
+
+    assert cost(P1) < cost(P0)

@@ -52,7 +52,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--points", type=int, default=100_000)
     ap.add_argument("--images", type=int, default=200)
-    ap.add_argument("--workload", default="grid", choices=["grid", "windows", "serving", "walk"])
+    ap.add_argument("--workload", default="grid",
+                    choices=["grid", "windows", "serving", "walk", "triangulation"])
+    ap.add_argument("--tri-points", type=int, default=1_000_000)
+    ap.add_argument("--tri-cpu-sample", type=int, default=20_000)
     ap.add_argument("--rates", default="50,200,800,2000",
                     help="serving: Poisson arrival rates swept (req/s)")
     ap.add_argument("--duration", type=float, default=10.0, help="serving: seconds per rate")
@@ -388,6 +391,9 @@ def run_gba(args, ws, rank, local):
         a3 = copy.copy(args)
         a3.rates, a3.duration, a3.pool = "100,1000", 4.0, 96
         sv = run_serving(a3, ws, rank, local)
+        a4 = copy.copy(args)
+        a4.steps, a4.warmup = 3, 1
+        tr = run_triangulation(a4, ws, rank, local)
         secondary = {
             "windows": {k: w[k] for k in ("metric", "value", "unit", "ms_per_step",
                                           "speedup_vs_per_problem_fp64",
@@ -398,6 +404,8 @@ def run_gba(args, ws, rank, local):
                         "sweep": [{k: r[k] for k in ("rate", "solves_per_s", "p50_ms", "p99_ms")}
                                   for r in sv["sweep"]],
                         "final_cost_max_rel_diff_vs_fp64": sv["final_cost_max_rel_diff_vs_fp64"]},
+            "triangulation": {k: tr[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e",
+                                                 "cpu_baseline", "max_abs_diff_vs_oracle_sample")},
         }
 
     if rank == 0:
@@ -711,6 +719,67 @@ def run_serving(args, ws, rank, local):
     return line
 
 
+TRI_WORKLOAD = ("batched multi-view triangulation: 1,000,000 tracks over 200 ring views, "
+                "2-12 views per track about 15 degrees apart, radial+decentering distortion, 0.5 px noise; "
+                "DLT + LM (<= 50 iterations) per point, FP64")
+
+
+def run_triangulation(args, ws, rank, local):
+    """Points/s of gba_triangulate: device time of the triangulation kernel
+    (CUDA events, options.profile) and end to end with host buffers; the
+    oracle (one thread) on a sample of the same tracks beside it."""
+    from hs_sfm_gb300 import abi, gba, synthetic
+    import oracle
+    n = args.tri_points
+    b = synthetic.triangulation_batch(seed=11, num_points=n, num_views=200, views_range=(2, 12),
+                                      noise=0.5)
+    opt = abi.make_options(profile=1)
+    L = gba.lib()
+    for _ in range(max(args.warmup, 1)):
+        gba.triangulate(b, opt)
+    launches0 = gba.kernel_launch_count()
+    dev_ms, wall_ms = [], []
+    clk = ClockSampler(local)
+    clk.start()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        pts, st = gba.triangulate(b, opt)
+        wall_ms.append(1e3 * (time.perf_counter() - t0))
+        dev_ms.append(L.gba_triangulate_last_kernel_ms())
+    clk_info = clk.stop()
+    launches = gba.kernel_launch_count() - launches0
+    err = float(np.sqrt(np.mean(np.sum((pts - b.points) ** 2, axis=1))))
+    # oracle on a sample (the first tracks) for parity and the CPU rate
+    ns = min(n, args.tri_cpu_sample)
+    sub = synthetic.TriangulationBatch(intrinsics=b.intrinsics, extrinsics=b.extrinsics,
+                                       track_offsets=b.track_offsets[:ns + 1],
+                                       track_views=b.track_views[:b.track_offsets[ns]],
+                                       track_keys=b.track_keys[:b.track_offsets[ns]],
+                                       points=b.points[:ns])
+    t0 = time.perf_counter()
+    ref, _ = oracle.triangulate(sub, abi.make_options())
+    cpu_s = time.perf_counter() - t0
+    m = int(b.track_offsets[-1])
+    h2d = 8 * (n + 1) + 8 * m + 16 * m + 8 * 16 * len(b.intrinsics)
+    d2h = 24 * n + 4 * n
+    return {
+        "metric": "triangulated points/s", "value": n / (np.median(dev_ms) / 1e3), "unit": "points/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.median(dev_ms)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ring views and tracks)",
+        "config": {"workload": TRI_WORKLOAD, "points": n, "views": len(b.intrinsics),
+                   "observations": m},
+        "status_ok": int(np.sum(st == 0)), "rms_error_vs_truth": err,
+        "max_abs_diff_vs_oracle_sample": float(np.max(np.abs(pts[:ns] - ref))),
+        "e2e": {"value": n / (np.median(wall_ms) / 1e3), "unit": "points/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": float(np.median(wall_ms))},
+        "cpu_baseline": {"value": ns / cpu_s, "unit": "points/s", "cores": 1, "kind": "port",
+                         "sample": f"the first {ns} tracks through the oracle ({cpu_s:.1f} s)"},
+        "gpu_launches": int(launches), "clocks": clk_info,
+    }
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -724,6 +793,9 @@ def main():
         return 0
     if args.workload == "walk":
         return run_walk(args, ws, rank, local)
+    if args.workload == "triangulation":
+        print(json.dumps(run_triangulation(args, ws, rank, local)), flush=True)
+        return 0
     return run_gba(args, ws, rank, local)
 
 

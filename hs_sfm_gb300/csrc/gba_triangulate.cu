@@ -33,6 +33,8 @@ namespace {
 
 constexpr int kViewDoubles = 22;   // f s cx cy a k1 k2 k3 d1 d2, R (9), C (3)
 
+thread_local double g_tri_last_ms = 0.0;   // the calling thread's last kernel time (profile)
+
 __global__ void k_tri_views(int V, const double* __restrict__ intr, const double* __restrict__ extr,
                             double* __restrict__ views) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -389,10 +391,26 @@ extern "C" int gba_triangulate(const gba_triangulation* p, const gba_options* o,
       ++launches;
     }
     TriParams prm{o->max_iterations, o->tau, o->eps1, o->eps2};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (o->profile) {
+      TRI_CUDA(cudaEventCreate(&ev[0]));
+      TRI_CUDA(cudaEventCreate(&ev[1]));
+      TRI_CUDA(cudaEventRecord(ev[0], s));
+    }
     k_triangulate<<<unsigned((n + 127) / 128), 128, 0, s>>>(n, d_off, d_tv, d_keys, d_views, prm,
                                                              d_pts, d_st);
     ++launches;
     TRI_CUDA(cudaGetLastError());
+    g_tri_last_ms = 0.0;
+    if (o->profile) {
+      TRI_CUDA(cudaEventRecord(ev[1], s));
+      TRI_CUDA(cudaEventSynchronize(ev[1]));
+      float ms = 0.0f;
+      TRI_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      g_tri_last_ms = ms;
+      cudaEventDestroy(ev[0]);
+      cudaEventDestroy(ev[1]);
+    }
     count_launches(launches);
     TRI_CUDA(cudaMemcpyAsync(points, d_pts, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
     std::vector<int> st(static_cast<size_t>(n));
@@ -410,3 +428,5 @@ extern "C" int gba_triangulate(const gba_triangulation* p, const gba_options* o,
   }
   return err;
 }
+
+extern "C" double gba_triangulate_last_kernel_ms(void) { return gba::g_tri_last_ms; }

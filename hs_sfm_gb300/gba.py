@@ -80,6 +80,7 @@ def lib():
     L.gba_estimate_device_bytes.restype = C.c_int64
     L.gba_estimate_device_bytes.argtypes = [P, C.c_int32]
     L.gba_triangulate.argtypes = [C.POINTER(abi.Triangulation), O, d, C.POINTER(C.c_int32)]
+    L.gba_triangulate_last_kernel_ms.restype = C.c_double
     _lib = L
     return L
 

@@ -540,8 +540,9 @@ def project_views(intrinsics, extrinsics, views, X):
 def triangulation_batch(seed=0, num_points=1000, num_views=20, views_range=(2, 8),
                         noise=0.5, distortion=True):
     """Views on a ring of radius 10 looking at the origin (each with its own
-    intrinsics), points uniform in [-2,2]^3, each seen by a random subset of
-    views_range views, keys with N(0, noise) pixel noise."""
+    intrinsics), points uniform in [-2,2]^3, each seen by k ~ U(views_range)
+    views of the ring about 15 degrees apart from a random first one, keys
+    with N(0, noise) pixel noise."""
     rng = np.random.default_rng(seed)
     phi = 2 * np.pi * np.arange(num_views) / num_views + rng.uniform(0, 0.1, num_views)
     centers = np.stack([10 * np.cos(phi), 10 * np.sin(phi), rng.uniform(-1, 1, num_views)], axis=1)
@@ -561,7 +562,10 @@ def triangulation_batch(seed=0, num_points=1000, num_views=20, views_range=(2, 8
     k = rng.integers(views_range[0], views_range[1] + 1, size=num_points)
     k = np.minimum(k, num_views)
     off = np.concatenate([[0], np.cumsum(k)]).astype(np.int64)
-    views = np.concatenate([rng.choice(num_views, kk, replace=False) for kk in k]).astype(np.int64)
+    start = rng.integers(0, num_views, size=num_points)
+    pos = np.arange(off[-1]) - np.repeat(off[:-1], k)
+    stride = max(1, num_views // 24)   # about 15 degrees between a track's views
+    views = ((np.repeat(start, k) + stride * pos) % num_views).astype(np.int64)
     X = np.repeat(pts, k, axis=0)
     keys = project_views(intr, extr, views, X) + rng.normal(0, noise, (len(views), 2))
     return TriangulationBatch(intrinsics=intr, extrinsics=extr, track_offsets=off,

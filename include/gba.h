@@ -418,6 +418,9 @@ typedef struct gba_triangulation {
  * else an input error. */
 GBA_API int gba_triangulate(const gba_triangulation* problem, const gba_options* options,
                             double* points, int32_t* point_status);
+/* Device time of the calling thread's last gba_triangulate kernel (ms), when
+ * that call had options->profile set; else 0. */
+GBA_API double gba_triangulate_last_kernel_ms(void);
 
 /* ---- library ------------------------------------------------------------ */
 GBA_API const char* gba_status_string(int status);

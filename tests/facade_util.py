@@ -61,3 +61,15 @@ def write_problem(path, scene, iters, mode=0):
         np.ascontiguousarray(scene.cameras, np.float64).tofile(fh)
         np.ascontiguousarray(scene.near_y, np.float64).tofile(fh)
         np.ascontiguousarray(scene.x0, np.float64).tofile(fh)
+
+
+def write_triangulation(path, b):
+    """A synthetic.TriangulationBatch in tests/cpp/triangulate_solve.cpp's input format."""
+    n = len(b.track_offsets) - 1
+    with open(path, "wb") as fh:
+        np.array([len(b.intrinsics), n, len(b.track_views)], np.int64).tofile(fh)
+        np.ascontiguousarray(b.intrinsics, np.float64).tofile(fh)
+        np.ascontiguousarray(b.extrinsics, np.float64).tofile(fh)
+        np.ascontiguousarray(b.track_offsets, np.int64).tofile(fh)
+        np.ascontiguousarray(b.track_views, np.int64).tofile(fh)
+        np.ascontiguousarray(b.track_keys, np.float64).tofile(fh)

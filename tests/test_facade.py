@@ -10,7 +10,7 @@ import pytest
 
 from hs_sfm_gb300 import abi, synthetic
 
-from facade_util import build_facade, write_gcp_problem, write_problem
+from facade_util import build_facade, write_gcp_problem, write_problem, write_triangulation
 
 
 def test_facade_builds_and_rejects_bad_initial_x(tmp_path):
@@ -119,3 +119,36 @@ def test_gcp_facade_solve_matches_oracle(tmp_path):
     assert np.allclose(y0[:2 * s.number_of_keys], y_ref[:2 * s.number_of_keys], rtol=1e-13, atol=1e-15)
     np.testing.assert_array_equal(y0[2 * s.number_of_keys:], y_ref[2 * s.number_of_keys:])
     del fmap
+
+
+def test_triangulation_facade_refuses_one_view(tmp_path):
+    # MultipleViewMaximumLikelihoodEstimator needs two views (:66-69)
+    exe = build_facade(str(tmp_path), "triangulate_solve")
+    b = synthetic.triangulation_batch(seed=1, num_points=5)
+    path = tmp_path / "t.bin"
+    write_triangulation(path, b)
+    r = subprocess.run([exe, str(path), str(tmp_path / "o.bin"), "--one-view"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and r.stdout.startswith("mle -1")
+
+
+@pytest.mark.gpu
+def test_triangulation_facade_matches_oracle(tmp_path):
+    import oracle
+    exe = build_facade(str(tmp_path), "triangulate_solve")
+    b = synthetic.triangulation_batch(seed=7, num_points=500, noise=0.5)
+    path = tmp_path / "t.bin"
+    write_triangulation(path, b)
+    r = subprocess.run([exe, str(path), str(tmp_path / "o.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = (tmp_path / "o.bin").read_bytes()
+    n = len(b.track_offsets) - 1
+    pts = np.frombuffer(raw[:24 * n], dtype=np.float64).reshape(-1, 3)
+    st = np.frombuffer(raw[24 * n:28 * n], dtype=np.int32)
+    p0 = np.frombuffer(raw[28 * n:], dtype=np.float64)
+    ref, sref = oracle.triangulate(b)
+    assert np.array_equal(st, sref)
+    # FP64 on both sides; the device contracts multiply-adds (see
+    # tests/test_gpu_triangulate.py): points within 1e-6
+    assert np.max(np.abs(pts - ref)) < 1e-6
+    assert np.array_equal(p0, pts[0])

@@ -475,13 +475,10 @@ __global__ void k_cam_prep(DevPlan d, int which) {
 // ---------------------------------------------------------------------------
 // image prep: which = 0 current x (at init), 1 candidate x (when evaluating)
 // ---------------------------------------------------------------------------
+// The rotation of image i's parameters in parity par in every form the key
+// kernels read.
 template <typename T>
-__global__ void k_image_prep(DevPlan d, int which) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.I) return;
-  const LMState& st = d.state[d.img_prob[i]];
-  if (which == 0 ? !st.active : !st.evaluate) return;
-  int par = which ? 1 - st.parity : st.parity;
+__device__ void image_prep_one(const DevPlan& d, int i, int par) {
   const double* x = d.x_img[par] + 6LL * i;
   double r0 = x[0], r1 = x[1], r2 = x[2];
   double theta = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
@@ -508,6 +505,18 @@ __global__ void k_image_prep(DevPlan d, int which) {
   IL[0] = T(r0); IL[1] = T(r1); IL[2] = T(r2);
   IL[3] = T(x[3]); IL[4] = T(x[4]); IL[5] = T(x[5]);
   IL[6] = T(ct); IL[7] = T(s); IL[8] = T(c); IL[9] = T(a1); IL[10] = T(a2); IL[11] = T(0);
+}
+
+// which = 0: the current x of active problems (at init); 1: the candidate of
+// problems whose step is evaluated (the back-substitution prepares it too,
+// so the solve loop does not launch this for the candidate).
+template <typename T>
+__global__ void k_image_prep(DevPlan d, int which) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.I) return;
+  const LMState& st = d.state[d.img_prob[i]];
+  if (which == 0 ? !st.active : !st.evaluate) return;
+  image_prep_one<T>(d, i, which ? 1 - st.parity : st.parity);
 }
 
 // Soft-constraint and point-prior part of the cost, sum w (x - y)^2 and
@@ -2486,6 +2495,8 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       gd += d.gi[e] * dv;
     }
     double s0 = block_sum(dn2, red), s1 = block_sum(xn2, red), s2 = block_sum(gd, red);
+    // the candidate's rotations (block_sum's barriers made x_img[1 - par] visible)
+    if (threadIdx.x < ch.end - ch.begin) image_prep_one<T>(d, ch.begin + threadIdx.x, 1 - par);
     if (threadIdx.x == 0) {
       d.img_chunk_sum[3LL * c] = s0;
       d.img_chunk_sum[3LL * c + 1] = s1;
@@ -2524,31 +2535,37 @@ __global__ void k_cam_backsub(DevPlan d) {
 // ---------------------------------------------------------------------------
 // LM control (one warp per problem)
 // ---------------------------------------------------------------------------
+// Sum of one field of a problem's chunk partials by the whole CTA (thread t
+// adds chunks t, t + blockDim, ... in order, then a fixed-shape tree):
+// deterministic, and each thread waits on a few loads instead of one warp
+// walking hundreds of chunks.  Result valid in thread 0.
 __device__ double prob_sum(const double* v, int stride, int off, const int* chunk_off, int p,
-                           int lane) {
+                           double* red) {
   double s = 0.0;
-  for (int c = chunk_off[p] + lane; c < chunk_off[p + 1]; c += 32) s += v[(long long)stride * c + off];
-  return warp_sum(s);
+  for (int c = chunk_off[p] + threadIdx.x; c < chunk_off[p + 1]; c += blockDim.x)
+    s += v[(long long)stride * c + off];
+  return block_sum(s, red);
 }
 
-__global__ void k_ctrl_initial_cost(DevPlan d) {
-  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (p >= d.B) return;
+// LM control: one CTA per problem (kCtrlThreads), thread 0 decides.
+constexpr int kCtrlThreads = 256;
+
+__global__ void __launch_bounds__(kCtrlThreads) k_ctrl_initial_cost(DevPlan d) {
+  __shared__ double red[32];
+  const int p = blockIdx.x;
   LMState& st = d.state[p];
   if (!st.active) return;
-  double F = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, lane);
-  const double raw = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, lane);
+  double F = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, red);
+  const double raw = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, red);
+  if (threadIdx.x != 0) return;
   if (d.cons_cost) F += d.cons_cost[p];
-  if (lane == 0) {
-    st.F = F;
-    st.raw = raw;
-    st.initial_cost = F;
-    if (!isfinite(F)) {
-      st.status = GBA_ERR_NAN;
-      st.stop = GBA_STOP_ERROR;
-      st.active = 0;
-    }
+  st.F = F;
+  st.raw = raw;
+  st.initial_cost = F;
+  if (!isfinite(F)) {
+    st.status = GBA_ERR_NAN;
+    st.stop = GBA_STOP_ERROR;
+    st.active = 0;
   }
 }
 
@@ -2575,30 +2592,29 @@ __global__ void k_ctrl_after_linearize(DevPlan d) {
   d.factor_flag[p] = 0;
 }
 
-__global__ void k_ctrl_step(DevPlan d) {
-  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (p >= d.B) return;
+__global__ void __launch_bounds__(kCtrlThreads) k_ctrl_step(DevPlan d) {
+  __shared__ double red[32];
+  const int p = blockIdx.x;
   LMState& st = d.state[p];
   if (!st.active) return;
   const bool failed = d.factor_flag[p] != 0;
   double dn2 = 0, xn2 = 0, gd = 0, er = 0;
   if (!failed) {
-    dn2 = prob_sum(d.pt_chunk_sum, 3, 0, d.prob_pt_chunk_off, p, lane) +
-          prob_sum(d.img_chunk_sum, 3, 0, d.prob_img_chunk_off, p, lane);
-    xn2 = prob_sum(d.pt_chunk_sum, 3, 1, d.prob_pt_chunk_off, p, lane) +
-          prob_sum(d.img_chunk_sum, 3, 1, d.prob_img_chunk_off, p, lane);
-    gd = prob_sum(d.pt_chunk_sum, 3, 2, d.prob_pt_chunk_off, p, lane) +
-         prob_sum(d.img_chunk_sum, 3, 2, d.prob_img_chunk_off, p, lane);
+    dn2 = prob_sum(d.pt_chunk_sum, 3, 0, d.prob_pt_chunk_off, p, red) +
+          prob_sum(d.img_chunk_sum, 3, 0, d.prob_img_chunk_off, p, red);
+    xn2 = prob_sum(d.pt_chunk_sum, 3, 1, d.prob_pt_chunk_off, p, red) +
+          prob_sum(d.img_chunk_sum, 3, 1, d.prob_img_chunk_off, p, red);
+    gd = prob_sum(d.pt_chunk_sum, 3, 2, d.prob_pt_chunk_off, p, red) +
+         prob_sum(d.img_chunk_sum, 3, 2, d.prob_img_chunk_off, p, red);
     // PCG leaves the image rows with residual r: the model decrease gains r^T delta_i
-    if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_img_chunk_off, p, lane);
+    if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_img_chunk_off, p, red);
     if (d.free_cams) {
-      dn2 += prob_sum(d.cam_sum, 3, 0, d.prob_cam_off, p, lane);
-      xn2 += prob_sum(d.cam_sum, 3, 1, d.prob_cam_off, p, lane);
-      gd += prob_sum(d.cam_sum, 3, 2, d.prob_cam_off, p, lane);
+      dn2 += prob_sum(d.cam_sum, 3, 0, d.prob_cam_off, p, red);
+      xn2 += prob_sum(d.cam_sum, 3, 1, d.prob_cam_off, p, red);
+      gd += prob_sum(d.cam_sum, 3, 2, d.prob_cam_off, p, red);
     }
   }
-  if (lane != 0) return;
+  if (threadIdx.x != 0) return;
   st.iter += 1;
   st.evaluate = 0;
   if (d.factor_flag[p] == 2) {        // a bounded wait of the factorization ran out
@@ -2626,16 +2642,15 @@ __global__ void k_ctrl_step(DevPlan d) {
   }
 }
 
-__global__ void k_ctrl_accept(DevPlan d) {
-  const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (p >= d.B) return;
+__global__ void __launch_bounds__(kCtrlThreads) k_ctrl_accept(DevPlan d) {
+  __shared__ double red[32];
+  const int p = blockIdx.x;
   LMState& st = d.state[p];
   if (!st.evaluate) return;
-  const double Fn = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, lane) +
-                    (d.cons_cost ? d.cons_cost[p] : 0.0);
-  const double raw_n = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, lane);
-  if (lane != 0) return;
+  double Fn = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, red);
+  const double raw_n = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, red);
+  if (threadIdx.x != 0) return;
+  if (d.cons_cost) Fn += d.cons_cost[p];
   st.evaluate = 0;
   st.F_new = Fn;
   // predicted decrease of the quadratic model, 2 g^T d - d^T N d, written
@@ -2780,7 +2795,8 @@ int launch_image_prep(const DevPlan& d, int which, cudaStream_t s) {
     k_cam_prep<<<(d.Ctot + 127) / 128, 128, 0, s>>>(d, which);
     ++n;
   }
-  if (d.I <= 0) return n;
+  // the candidate's image rotations come from k_backsub
+  if (d.I <= 0 || which == 1) return n;
   GBA_DISPATCH(d, run_image_prep<T>(d, which, s));
   return n + 1;
 }
@@ -2802,7 +2818,7 @@ int launch_cost(const DevPlan& d, int which, cudaStream_t s) {
 }
 
 int launch_ctrl_initial_cost(const DevPlan& d, cudaStream_t s) {
-  k_ctrl_initial_cost<<<(d.B + 3) / 4, 128, 0, s>>>(d);
+  k_ctrl_initial_cost<<<d.B, kCtrlThreads, 0, s>>>(d);
   return 1;
 }
 
@@ -2993,12 +3009,12 @@ int launch_backsub(const DevPlan& d, cudaStream_t s) {
 }
 
 int launch_ctrl_step(const DevPlan& d, cudaStream_t s) {
-  k_ctrl_step<<<(d.B + 3) / 4, 128, 0, s>>>(d);
+  k_ctrl_step<<<d.B, kCtrlThreads, 0, s>>>(d);
   return 1;
 }
 
 int launch_ctrl_accept(const DevPlan& d, cudaStream_t s) {
-  k_ctrl_accept<<<(d.B + 3) / 4, 128, 0, s>>>(d);
+  k_ctrl_accept<<<d.B, kCtrlThreads, 0, s>>>(d);
   return 1;
 }
 

@@ -12,6 +12,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <unistd.h>
+#include <condition_variable>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -41,6 +44,77 @@ std::atomic<long long> g_launches{0};
     }                                                                       \
   } while (0)
 
+// Worker threads kept for the host build: a job f(t), t = 1 .. n-1, runs on
+// the workers while the caller runs t = 0, so a parallel phase costs a wake-up
+// instead of thread creation.  One job at a time; a caller that finds the
+// pool busy (another plan building on another thread) gets false and runs
+// the job on fresh threads instead.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool pool;
+    return pool;
+  }
+  bool run(int n, const std::function<void(int)>& f) {
+    if (getpid() != pid_) return false;   // a forked child has no workers
+    std::unique_lock<std::mutex> busy(busy_, std::try_to_lock);
+    if (!busy.owns_lock() || n - 1 > int(workers_.size())) return false;
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      job_ = &f;
+      njob_ = n;
+      pending_ = n - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    f(0);
+    std::unique_lock<std::mutex> lk(m_);
+    done_.wait(lk, [&] { return pending_ == 0; });
+    job_ = nullptr;
+    return true;
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+  }
+
+ private:
+  HostPool() : pid_(getpid()) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int n = int(std::max(1u, std::min(hw, 16u))) - 1;
+    for (int w = 0; w < n; ++w) workers_.emplace_back([this, w] { loop(w + 1); });
+  }
+  void loop(int t) {
+    long long seen = 0;
+    for (;;) {
+      const std::function<void(int)>* f = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+        if (t < njob_) f = job_;
+      }
+      if (!f) continue;
+      (*f)(t);
+      std::lock_guard<std::mutex> lk(m_);
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  const pid_t pid_;
+  std::vector<std::thread> workers_;
+  std::mutex m_, busy_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* job_ = nullptr;
+  int njob_ = 0, pending_ = 0;
+  long long gen_ = 0;
+  bool stop_ = false;
+};
+
 // Runs f(begin, end, t) over [0, n) split into contiguous pieces, piece t
 // in thread t (piece 0 in the calling thread).  cuts, if given, are the
 // piece boundaries; otherwise the pieces are equal.
@@ -50,11 +124,44 @@ void host_parallel(int64_t n, int threads, F f, const std::vector<int64_t>* cuts
     f(int64_t(0), n, 0);
     return;
   }
-  std::vector<std::thread> pool;
   auto lo = [&](int t) { return cuts ? (*cuts)[t] : n * t / threads; };
-  for (int t = 1; t < threads; ++t) pool.emplace_back([&, t] { f(lo(t), lo(t + 1), t); });
-  f(lo(0), lo(1), 0);
+  const std::function<void(int)> piece = [&](int t) { f(lo(t), lo(t + 1), t); };
+  if (HostPool::get().run(threads, piece)) return;
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) pool.emplace_back([&, t] { piece(t); });
+  piece(0);
   for (auto& th : pool) th.join();
+}
+
+// Stable counting sort of the indices [0, n) by key(i) in [0, nb): off
+// [nb + 1] gets each key's first slot and out[off[b] ..] its indices in
+// ascending order.  Pieces of the index range count in parallel; the slots of
+// a key go to the pieces in index order, so the result is the serial one.
+template <typename KeyF>
+void counting_sort(int64_t n, int nb, int threads, KeyF key, std::vector<int>& off,
+                   std::vector<int>& out) {
+  threads = int(std::max<int64_t>(1, std::min<int64_t>(threads, n / 65536)));
+  std::vector<std::vector<int>> hist(threads, std::vector<int>(size_t(nb), 0));
+  host_parallel(n, threads, [&](int64_t i0, int64_t i1, int t) {
+    int* h = hist[t].data();
+    for (int64_t i = i0; i < i1; ++i) h[key(i)]++;
+  });
+  off.assign(size_t(nb) + 1, 0);
+  int run = 0;
+  for (int b = 0; b < nb; ++b) {
+    off[b] = run;
+    for (int t = 0; t < threads; ++t) {
+      const int c = hist[t][b];
+      hist[t][b] = run;
+      run += c;
+    }
+  }
+  off[nb] = run;
+  out.resize(size_t(n));
+  host_parallel(n, threads, [&](int64_t i0, int64_t i1, int t) {
+    int* h = hist[t].data();
+    for (int64_t i = i0; i < i1; ++i) out[h[key(i)]++] = int(i);
+  });
 }
 
 int host_threads() {
@@ -413,6 +520,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     std::vector<double> prior_y, prior_info;
   };
   std::vector<Piece> pieces(nprob);
+  // fine phases of a single problem's build (GBA_BUILD_TIMING)
+  auto sub = [&](const char* name) {
+    if (timing && nprob == 1) phase(name);
+  };
   auto build_one = [&](int q, int inner) {
     Piece& out = pieces[q];
     const gba_problem& p = problems[q];
@@ -435,15 +546,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       img_prob[ib + i] = q;
     }
     // point-major order: counting sort by point, then image within point
-    std::vector<int> cnt(np + 1, 0);
-    for (int k = 0; k < nk; ++k) cnt[p.feature_maps[2 * k + 1] + 1]++;
-    for (int i = 0; i < np; ++i) cnt[i + 1] += cnt[i];
-    std::vector<int> order(nk);
-    {
-      std::vector<int> cur(cnt.begin(), cnt.end() - 1);
-      for (int k = 0; k < nk; ++k) order[cur[p.feature_maps[2 * k + 1]]++] = k;
-    }
     const int nth0 = nk > 200000 ? inner : 1;
+    std::vector<int> cnt, order;
+    counting_sort(nk, np, nth0, [&](int64_t k) { return int(p.feature_maps[2 * k + 1]); }, cnt,
+                  order);
     {
       std::vector<char> dup(nth0, 0);
       host_parallel(np, nth0, [&](int64_t i0, int64_t i1, int t) {
@@ -494,6 +600,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
           return;
         }
     }
+    sub("  keys sorted");
     key_sorted_to_orig[q] = std::move(order);
     for (int i = 0; i < np; ++i) {   // entry pb is set by the caller
       pt_key_off[pb + i + 1] = int(kb + cnt[i + 1]);
@@ -501,14 +608,11 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     }
     // per-image key lists (by point, since keys are point-major)
     {
-      std::vector<int> ic(ni + 1, 0);
-      for (int t = 0; t < nk; ++t) ic[key_img[kb + t] - ib + 1]++;
-      for (int i = 0; i < ni; ++i) ic[i + 1] += ic[i];
-      std::vector<int> cur(ic.begin(), ic.end() - 1);
-      for (int t = 0; t < nk; ++t) {
-        int li = key_img[kb + t] - int(ib);
-        img_keys[kb + cur[li]++] = int(kb + t);
-      }
+      std::vector<int> ic, lst;
+      counting_sort(nk, ni, nth0, [&](int64_t t) { return key_img[kb + t] - int(ib); }, ic, lst);
+      host_parallel(nk, nth0, [&](int64_t t0_, int64_t t1_, int) {
+        for (int64_t t = t0_; t < t1_; ++t) img_keys[kb + t] = int(kb + lst[t]);
+      });
       for (int i = 1; i <= ni; ++i) img_key_off[ib + i] = int(kb + ic[i]);   // entry ib: the caller
       out.img_item_cnt.assign(ni, 0);
       for (int i = 0; i < ni; ++i) {
@@ -519,6 +623,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         }
       }
     }
+    sub("  image lists");
     // free cameras: each point has nc camera records (one per 6-wide part)
     // for every distinct camera among its keys, ascending
     if (fc) {
@@ -557,6 +662,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         for (int r = out.pt_rec_off[i]; r < out.pt_rec_off[i + 1]; ++r)
           rec.push_back(make_int2(out.rec_ext[r], -(r + 1)));
     };
+    sub("  records");
     // reduced-system blocks: (i <= j) with their record pairs, point order.
     // Pairs are counted and placed by point ranges in parallel: each piece
     // counts its pairs per image pair, a piece's pairs of a block follow
@@ -622,6 +728,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
           o += c_;
         }
       }
+    sub("  pair counts");
       out.pairs.resize(acc);
       host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
         int* slot = cnt_t[t].data();
@@ -649,6 +756,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
           }
         }
       }, &cuts);
+    sub("  pairs placed");
       // dense map for the assembly of the lower triangle: map[j*Ie + i], j <= i
       if (!pcg) out.blk_map.swap(bid);
     }
@@ -748,7 +856,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     } else if (any_free) {
       for (int i = 0; i < np; ++i) pt_rec_off[pb + i] = int(rec_base);
     }
-    pairs.insert(pairs.end(), pc.pairs.begin(), pc.pairs.end());
+    if (pairs.empty())   // the first problem's list moves instead of copying
+      pairs.swap(pc.pairs);
+    else
+      pairs.insert(pairs.end(), pc.pairs.begin(), pc.pairs.end());
     blk_ij.insert(blk_ij.end(), pc.blk_ij.begin(), pc.blk_ij.end());
     const int nblk = int(pc.blk_ij.size());
     pi.block_begin = block_begin;
@@ -766,7 +877,9 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     }
     pi.num_items = int(items.size()) - pi.item_begin;
     blk_map_off[q] = (long long)blk_map.size();
-    if (!pcg)
+    if (!pcg && blk_map.empty() && block_begin == 0)
+      blk_map.swap(pc.blk_map);
+    else if (!pcg)
       for (int v : pc.blk_map) blk_map.push_back(v >= 0 ? v + block_begin : -1);
     // work chunks
     for (int s = 0; s < nk; s += kKeyChunk)

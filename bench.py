@@ -364,6 +364,20 @@ def run_gba(args, ws, rank, local):
                 "note": ("latency-bound chain of 38 diagonal 32x32 tiles on FP32 CUDA cores, no "
                          "tensor-core work; traffic from ncu (dram read + write per launch)")}
     roofline["frac"] = roofline["achieved"] / tflops_peak if roofline["achieved"] else None
+    # the roof the factorization actually runs under: FP32 FMA on the CUDA
+    # cores, measured live on this GPU (gba_fma_peak)
+    try:
+        ffma = gba.fma_peak(abi.PRECISION_MIXED, local)
+        dfma = gba.fma_peak(abi.PRECISION_FP64, local)
+    except Exception:
+        ffma = dfma = None
+    roofline_fp32 = None
+    if ffma and roofline["achieved"]:
+        roofline_fp32 = {"bound": "fp32", "kernel": roofline["kernel"],
+                         "achieved": roofline["achieved"], "peak": ffma, "unit": "TFLOP/s",
+                         "frac": roofline["achieved"] / ffma,
+                         "peak_kind": "measured live (gba_fma_peak, FP32 FMA, this run)",
+                         "fp64_fma_tflops": dfma}
     roofline_hbm = None
     if hbm_stages:
         dom = max(hbm_stages, key=lambda k: hbm_stages[k]["ms_per_iteration"])
@@ -440,6 +454,7 @@ def run_gba(args, ws, rank, local):
                       "final_rmse": rep.final_rmse, "accepted": rep.accepted,
                       "rejected": rep.rejected, "setup_ms": rep0.setup_ms},
             "roofline": roofline,
+            "roofline_fp32": roofline_fp32,
             "roofline_hbm": roofline_hbm,
             "stages": stages,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

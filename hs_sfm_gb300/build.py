@@ -18,7 +18,8 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgba.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-UNITS = ["gba_kernels.cu", "gba_plan.cu", "gba_noalloc.cu", "gba_server.cu", "gba_triangulate.cu"]
+UNITS = ["gba_kernels.cu", "gba_plan.cu", "gba_noalloc.cu", "gba_server.cu", "gba_triangulate.cu",
+         "gba_calibrate.cu"]
 
 
 def nvcc() -> str:

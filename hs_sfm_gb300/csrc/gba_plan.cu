@@ -372,11 +372,18 @@ int validate(const gba_problem& p, bool pcg) {
     int64_t c = p.image_camera_map[i];
     if (c < 0 || c >= p.number_of_cameras) return GBA_ERR_BAD_INDEX;
   }
-  for (int64_t k = 0; k < p.number_of_keys; ++k) {
-    int64_t im = p.feature_maps[2 * k], pt = p.feature_maps[2 * k + 1];
-    if (im < 0 || im >= p.number_of_images || pt < 0 || pt >= p.number_of_points)
-      return GBA_ERR_BAD_INDEX;
-  }
+  // key indices, in parallel pieces for large problems
+  const int64_t nk = p.number_of_keys;
+  const int nth = nk > 200000 ? host_threads() : 1;
+  std::vector<char> bad(size_t(nth), 0);
+  host_parallel(nk, nth, [&](int64_t k0, int64_t k1, int t) {
+    for (int64_t k = k0; k < k1; ++k) {
+      const int64_t im = p.feature_maps[2 * k], pt = p.feature_maps[2 * k + 1];
+      if (im < 0 || im >= p.number_of_images || pt < 0 || pt >= p.number_of_points) bad[t] = 1;
+    }
+  });
+  for (char v : bad)
+    if (v) return GBA_ERR_BAD_INDEX;
   return GBA_OK;
 }
 

@@ -81,6 +81,7 @@ def lib():
     L.gba_estimate_device_bytes.argtypes = [P, C.c_int32]
     L.gba_triangulate.argtypes = [C.POINTER(abi.Triangulation), O, d, C.POINTER(C.c_int32)]
     L.gba_triangulate_last_kernel_ms.restype = C.c_double
+    L.gba_fma_peak.argtypes = [C.c_int32, C.c_int32, d]
     _lib = L
     return L
 
@@ -346,3 +347,10 @@ def triangulate(batch, options=None):
     _check(lib().gba_triangulate(ct.ref, C.byref(opt), abi.dptr(pts),
                                  st.ctypes.data_as(C.POINTER(C.c_int32))), "gba_triangulate")
     return pts, st
+
+
+def fma_peak(precision=abi.PRECISION_MIXED, device=0):
+    """FP32 (PRECISION_MIXED) or FP64 FMA throughput of the device, TFLOP/s."""
+    out = C.c_double()
+    _check(lib().gba_fma_peak(precision, device, C.byref(out)), "gba_fma_peak")
+    return out.value

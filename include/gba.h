@@ -422,6 +422,11 @@ GBA_API int gba_triangulate(const gba_triangulation* problem, const gba_options*
  * that call had options->profile set; else 0. */
 GBA_API double gba_triangulate_last_kernel_ms(void);
 
+/* FMA throughput of the device at its current clocks (TFLOP/s; precision
+ * GBA_PRECISION_MIXED = FP32, GBA_PRECISION_FP64 = FP64): the compute roof
+ * of the kernels that run on the CUDA cores. */
+GBA_API int gba_fma_peak(int32_t precision, int32_t device, double* tflops);
+
 /* ---- library ------------------------------------------------------------ */
 GBA_API const char* gba_status_string(int status);
 GBA_API const char* gba_version(void);

@@ -447,7 +447,9 @@ def run_gba(args, ws, rank, local):
             "data": "synthetic (seeded grid scene, noise 1 px, float32-exact keys)",
             "config": {"workload": WORKLOAD, "points": P, "images": I, "keys": K, "pairs": pairs,
                        "precision": args.precision, "iterations_per_step": ITERS_PER_SOLVE,
-                       "linear_solver": "dense FP64 Cholesky (1,200 unknowns)",
+                       "linear_solver": ("dense Cholesky of the 1,200-unknown reduced system, "
+                                     + ("FP32 on the mixed path" if precision == abi.PRECISION_MIXED
+                                        else "FP64")),
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas{ws}"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
             "solve": {"initial_cost": rep.initial_cost, "final_cost": rep.final_cost,

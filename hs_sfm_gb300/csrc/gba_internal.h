@@ -195,6 +195,7 @@ struct DevPlan {
   const int* pt_rec_off;          // [P + 1] camera records of each point (indices >= K)
   const int2* rec_info;           // [R] (global camera, ext index)
   double* img_item_cam;           // [n_img_items * kImgCamVals] partial sums of image items
+  double* img_cam_sum;            // [I * kImgCamVals] the sums of each image's items
   double* Ei;                     // [60 I] J_i^T J_c per image (full columns)
   double* Uc;                     // [100 Ctot] camera normal block, cps x cps, row stride 10
   double* gc;                     // [10 Ctot]

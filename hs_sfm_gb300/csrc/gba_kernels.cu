@@ -737,9 +737,7 @@ __global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
         jc[m] = (l00 * a + l10 * b) * sw;
         jc[10 + m] = l11 * b * sw;
       }
-      T* out = tptr_mut<T>(d.JC) + 20LL * k;
-#pragma unroll
-      for (int m = 0; m < 20; ++m) out[m] = jc[m];
+      store_vec<20>(tptr_mut<T>(d.JC) + 20LL * k, jc);
     }
     if (d.key_wl) {
       const T l00 = T(__ldg(d.key_wl + 3LL * k)), l10 = T(__ldg(d.key_wl + 3LL * k + 1)),
@@ -952,7 +950,8 @@ __global__ void __launch_bounds__(256) k_image_finalize(DevPlan d) {
 // E = J_i^T J_c (6 x 10), the upper triangle of J_c^T J_c (55) and J_c^T r
 // (10) over its keys (camera_shared_normal_equation_builder.hpp:111-462 for
 // the camera blocks).  A CTA stages 32 keys' rows [J_i | J_c | r] in shared
-// memory; thread e owns sum e (Kahan in T, keys in order).
+// memory; thread e owns sum e (each batch in T, batches added in FP64, keys
+// in order).
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(128) k_image_cam_reduce(DevPlan d) {
@@ -980,58 +979,82 @@ __global__ void __launch_bounds__(128) k_image_cam_reduce(DevPlan d) {
     ca = 6 + (e - 115);
     cb = 16;
   }
-  T acc = T(0), cmp = T(0);
+  double acc = 0.0;
   for (int q0 = it.y; q0 < it.z; q0 += 32) {
     const int nq = min(32, it.z - q0);
-    for (int v = threadIdx.x; v < 64 * 17; v += 128) {
-      const int row = v / 17, col = v - 17 * (v / 17), kq = row >> 1, rr = row & 1;
-      T val = T(0);
+    if (threadIdx.x < 64) {   // thread r stages row r: key r/2, Jacobian row r%2
+      const int row = threadIdx.x, kq = row >> 1, rr = row & 1;
+      T v[17];
+#pragma unroll
+      for (int c = 0; c < 17; ++c) v[c] = T(0);
       if (kq < nq) {
         const long long k = __ldg(d.img_keys + q0 + kq);
-        if (col < 6) val = JR[kJRStride * k + 6 + 6 * rr + col];
-        else if (col < 16) val = JC[20 * k + 10 * rr + (col - 6)];
-        else val = JR[kJRStride * k + 18 + rr];
+        const T* jr = JR + kJRStride * k;
+        const T* jc = JC + 20 * k + 10 * rr;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v[c] = jr[6 + 6 * rr + c];
+#pragma unroll
+        for (int c = 0; c < 10; ++c) v[6 + c] = jc[c];
+        v[16] = jr[18 + rr];
       }
-      M[row][col] = val;
+#pragma unroll
+      for (int c = 0; c < 17; ++c) M[row][c] = v[c];
     }
     __syncthreads();
-    if (e < 125) {
-      for (int row = 0; row < 2 * nq; ++row) {
-        const T y = M[row][ca] * M[row][cb] - cmp;
-        const T t = acc + y;
-        cmp = (t - acc) - y;
-        acc = t;
-      }
+    if (e < 125) {   // 32 keys in T, then into the FP64 total in key order
+      T bs = T(0);
+      for (int row = 0; row < 2 * nq; ++row) bs = fma(M[row][ca], M[row][cb], bs);
+      acc += double(bs);
     }
     __syncthreads();
   }
-  d.img_item_cam[(long long)kImgCamVals * blockIdx.x + e] = e < 125 ? double(acc - cmp) : 0.0;
+  d.img_item_cam[(long long)kImgCamVals * blockIdx.x + e] = e < 125 ? acc : 0.0;
 }
 
-// Per free camera: E of each of its images (FP64 sums of the image's items),
-// then U_c and g_c over its images in order, compacted to the computed
+// Per image with a free camera: the FP64 sums of its work items' partials
+// (items in order); E_i also goes to its own array for the assembly.
+__global__ void __launch_bounds__(kImgCamVals) k_image_cam_finalize(DevPlan d) {
+  const int img = blockIdx.x;
+  const int4 ci = d.cam_info[d.img_cam[img]];
+  if (ci.x == 0) return;
+  const LMState& st = d.state[ci.z];
+  if (!st.relin || !st.active) return;
+  const int e = threadIdx.x;
+  double v = 0.0;
+  for (int t = d.img_item_off[img]; t < d.img_item_off[img + 1]; ++t)
+    v += d.img_item_cam[(long long)kImgCamVals * t + e];
+  d.img_cam_sum[(long long)kImgCamVals * img + e] = v;
+  if (e < 60) d.Ei[60LL * img + e] = v;
+}
+
+// Per free camera: U_c and g_c summed over its images in FP64 (kCamGroups
+// groups of kImgCamVals threads take every kCamGroups-th image in order, the
+// group sums are added in group order), compacted to the computed
 // parameters, with the camera's soft constraints
 // (camera_shared_normal_equation_builder.hpp:309-349,418-459).
-__global__ void __launch_bounds__(128) k_cam_finalize(DevPlan d) {
+constexpr int kCamGroups = 8;
+__global__ void __launch_bounds__(kImgCamVals * kCamGroups) k_cam_finalize(DevPlan d) {
+  __shared__ double part[kCamGroups][kImgCamVals];
   __shared__ double sh[kImgCamVals];
   const int c = blockIdx.x;
   const int4 ci = d.cam_info[c];
   if (ci.x == 0) return;
   const LMState& st = d.state[ci.z];
   if (!st.relin || !st.active) return;
-  const int e = threadIdx.x;
+  const int e = threadIdx.x % kImgCamVals, grp = threadIdx.x / kImgCamVals;
   double tot = 0.0;
-  for (int u = d.cam_img_off[c]; u < d.cam_img_off[c + 1]; ++u) {
-    const int img = d.cam_imgs[u];
-    double v = 0.0;
-    for (int t = d.img_item_off[img]; t < d.img_item_off[img + 1]; ++t)
-      v += d.img_item_cam[(long long)kImgCamVals * t + e];
-    if (e < 60) d.Ei[60LL * img + e] = v;
-    tot += v;
-  }
-  sh[e] = tot;
+  for (int u = d.cam_img_off[c] + grp; u < d.cam_img_off[c + 1]; u += kCamGroups)
+    tot += d.img_cam_sum[(long long)kImgCamVals * d.cam_imgs[u] + e];
+  part[grp][e] = tot;
   __syncthreads();
-  if (e != 0) return;
+  if (threadIdx.x < kImgCamVals) {
+    double v = 0.0;
+#pragma unroll
+    for (int g = 0; g < kCamGroups; ++g) v += part[g][e];
+    sh[e] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   const int cps = ci.x;
   const unsigned mask = unsigned(ci.y);
   double* U = d.Uc + 100LL * c;
@@ -1139,7 +1162,9 @@ __global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
 
 // Free cameras: per camera record r of a point (camera c, part h) the Z
 // record C_p^-1 W with W = sum over the point's keys seen through camera c
-// of J_p^T J_c[:, 6h .. 6h+5] (computed parameters; zero past them).
+// of J_p^T J_c[:, 6h .. 6h+5] (computed parameters; zero past them).  The
+// records of one camera are consecutive; one pass over the point's keys
+// builds all of them (W for up to 12 computed columns).
 template <typename T>
 __global__ void __launch_bounds__(kPointChunk) k_camrec_z(DevPlan d) {
   const Chunk ch = d.pt_chunks[blockIdx.x];
@@ -1155,39 +1180,54 @@ __global__ void __launch_bounds__(kPointChunk) k_camrec_z(DevPlan d) {
   load_vec<8>(tptr<T>(d.PS) + 12LL * pt, ps);
   const T i00 = ps[0], m10 = ps[1], i11 = ps[2], m20 = ps[3], m21 = ps[4], i22 = ps[5];
   const int kb = d.pt_key_off[pt], ke = d.pt_key_off[pt + 1];
-  for (int r = rb; r < re; ++r) {
-    const int2 ri = d.rec_info[r - d.K];
-    const int4 ci = d.cam_info[ri.x];
-    const int h = ri.y - ci.w;
-    int col[6];
+  for (int r = rb; r < re;) {
+    const int cam = d.rec_info[r - d.K].x;
+    const int4 ci = d.cam_info[cam];
+    const int nparts = (ci.x + 5) / 6;
+    // W (3 x 12): the full-column index of each computed parameter
+    T w[36];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) col[a] = 6 * h + a < ci.x ? cam_full_col(unsigned(ci.y), 6 * h + a) : -1;
-    T w[18];
-#pragma unroll
-    for (int e = 0; e < 18; ++e) w[e] = T(0);
+    for (int e = 0; e < 36; ++e) w[e] = T(0);
     for (int k = kb; k < ke; ++k) {
-      if (d.img_cam[d.key_img[k]] != ri.x) continue;
-      T jp[6];
+      if (__ldg(d.img_cam + __ldg(d.key_img + k)) != cam) continue;
+      T jp[8], jc[20];
+      load_vec<8>(JR + (long long)kJRStride * k, jp);
+      load_vec<20>(JC + 20LL * k, jc);
 #pragma unroll
-      for (int m = 0; m < 6; ++m) jp[m] = JR[(long long)kJRStride * k + m];
+      for (int m = 0; m < 12; ++m) {
+        if (m >= ci.x) break;
+        const int f = cam_full_col(unsigned(ci.y), m);
+        T j0 = T(0), j1 = T(0);
 #pragma unroll
-      for (int a = 0; a < 6; ++a) {
-        if (col[a] < 0) continue;
-        const T j0 = JC[20LL * k + col[a]], j1 = JC[20LL * k + 10 + col[a]];
+        for (int q = 0; q < 10; ++q)
+          if (q == f) {
+            j0 = jc[q];
+            j1 = jc[10 + q];
+          }
 #pragma unroll
-        for (int i = 0; i < 3; ++i) w[6 * i + a] += jp[i] * j0 + jp[3 + i] * j1;
+        for (int i = 0; i < 3; ++i) w[12 * i + m] += jp[i] * j0 + jp[3 + i] * j1;
       }
     }
-    T z[kZStride];
+    for (int h = 0; h < nparts; ++h, ++r) {
+      T z[kZStride];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) {
-      z[a] = i00 * w[a];
-      z[6 + a] = m10 * w[a] + i11 * w[6 + a];
-      z[12 + a] = m20 * w[a] + m21 * w[6 + a] + i22 * w[12 + a];
+      for (int a = 0; a < 6; ++a) {
+        T w0 = T(0), w1 = T(0), w2 = T(0);
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh)
+          if (hh == h) {
+            w0 = w[6 * hh + a];
+            w1 = w[12 + 6 * hh + a];
+            w2 = w[24 + 6 * hh + a];
+          }
+        z[a] = i00 * w0;
+        z[6 + a] = m10 * w0 + i11 * w1;
+        z[12 + a] = m20 * w0 + m21 * w1 + i22 * w2;
+      }
+      z[18] = T(0);
+      z[19] = T(0);
+      store_vec<kZStride>(tptr_mut<T>(d.Z) + (long long)kZStride * r, z);
     }
-    z[18] = T(0);
-    z[19] = T(0);
-    store_vec<kZStride>(tptr_mut<T>(d.Z) + (long long)kZStride * r, z);
   }
 }
 
@@ -1257,6 +1297,29 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
   if (lane < 10) out[32 + lane] = double(mine1);
 }
 
+// Sum of one entry over work items [ib, ie) (stride kItemStride): in order
+// for short lists; else items t = ib + 4u + r go to partial r and the
+// partials are added in order (four loads in flight).
+__device__ __forceinline__ double sum_items4(const double* base, int ib, int ie) {
+  if (ie - ib < 8) {   // the common short lists: in order
+    double v = 0.0;
+    for (int t = ib; t < ie; ++t) v += base[(long long)kItemStride * t];
+    return v;
+  }
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int t = ib;
+  for (; t + 4 <= ie; t += 4) {
+    s0 += base[(long long)kItemStride * t];
+    s1 += base[(long long)kItemStride * (t + 1)];
+    s2 += base[(long long)kItemStride * (t + 2)];
+    s3 += base[(long long)kItemStride * (t + 3)];
+  }
+  if (t < ie) s0 += base[(long long)kItemStride * t];
+  if (t + 1 < ie) s1 += base[(long long)kItemStride * (t + 1)];
+  if (t + 2 < ie) s2 += base[(long long)kItemStride * (t + 2)];
+  return (s0 + s1) + (s2 + s3);
+}
+
 // Dense reduced system (lower triangle) and rhs in precision T; the block
 // sums over work items are taken in FP64.  Rows and columns run over the
 // problem's reduced-system images: its images, then with free cameras nc
@@ -1278,11 +1341,9 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
   const int Ie = pi.num_ext, ni = pi.num_images;
   const int blk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)j * Ie + i);
   double v = 0.0, rv = 0.0;
-  if (blk >= 0) {
+  if (blk >= 0) {   // four interleaved partial sums (loads in flight together), then in order
     const int ib = __ldg(d.blk_item_off + blk), ie = __ldg(d.blk_item_off + blk + 1);
-    for (int t = ib; t < ie; ++t) {
-      v += d.item_partial[(long long)kItemStride * t + 6 * bcol + a];
-    }
+    v = sum_items4(d.item_partial + 6 * bcol + a, ib, ie);
   }
   double base = 0.0, g = 0.0;
   if (i < ni) {
@@ -1316,7 +1377,7 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
     rv = 0.0;
     if (dblk >= 0) {
       const int ib = __ldg(d.blk_item_off + dblk), ie = __ldg(d.blk_item_off + dblk + 1);
-      for (int t = ib; t < ie; ++t) rv += d.item_partial[(long long)kItemStride * t + 36 + a];
+      rv = sum_items4(d.item_partial + 36 + a, ib, ie);
     }
     tptr_mut<T>(d.b)[6LL * (pi.ext_begin + i) + a] = T(g - rv);
   }
@@ -2841,8 +2902,9 @@ int launch_image_reduce(const DevPlan& d, cudaStream_t s) {
   k_image_finalize<<<(d.I + 7) / 8, 256, 0, s>>>(d);
   if (!d.free_cams) return 2;
   GBA_DISPATCH(d, (k_image_cam_reduce<T><<<d.n_img_items, 128, 0, s>>>(d)));
-  k_cam_finalize<<<d.Ctot, 128, 0, s>>>(d);
-  return 4;
+  k_image_cam_finalize<<<d.I, kImgCamVals, 0, s>>>(d);
+  k_cam_finalize<<<d.Ctot, kImgCamVals * kCamGroups, 0, s>>>(d);
+  return 5;
 }
 
 int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s) {

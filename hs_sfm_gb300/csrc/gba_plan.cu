@@ -1030,6 +1030,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     D.rec_info = arena.upload(rec_info);
     D.img_item_cam = arena.alloc<double>(size_t(kImgCamVals) * std::max<size_t>(img_items.size(), 1));
     D.Ei = arena.alloc<double>(60 * I);
+    D.img_cam_sum = arena.alloc<double>(size_t(kImgCamVals) * std::max<int64_t>(I, 1));
     D.Uc = arena.alloc<double>(100 * C);
     D.gc = arena.alloc<double>(10 * C);
     D.cam_sum = arena.alloc<double>(3 * C);

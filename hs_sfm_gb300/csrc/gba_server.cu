@@ -235,17 +235,27 @@ int64_t gba_estimate_device_bytes(const gba_problem* p, int32_t precision) {
   const int64_t tsz = precision == GBA_PRECISION_MIXED ? 4 : 8;
   const int64_t K = p->number_of_keys, P = p->number_of_points, I = p->number_of_images;
   const int64_t C = p->number_of_cameras;
-  int64_t pairs = 0;
+  // free cameras: nc six-wide parts per camera in the reduced system and up
+  // to nc camera records per (point, camera seen)
+  const int64_t cps = ppc(p->intrinsic_computations_mask);
+  const bool free_cams = !(p->fix_mask & GBA_FIX_CAMERAS) && cps > 0 && C > 0;
+  const int64_t nc = free_cams ? (cps + 5) / 6 : 0;
+  int64_t pairs = 0, recs = 0;
   if (K > 0 && p->feature_maps) {
     std::vector<int32_t> cnt(size_t(std::max<int64_t>(P, 1)), 0);
     for (int64_t k = 0; k < K; ++k) {
       const int64_t pt = p->feature_maps[2 * k + 1];
       if (pt >= 0 && pt < P) cnt[size_t(pt)]++;
     }
-    for (int32_t c : cnt) pairs += int64_t(c) * (c + 1) / 2;
+    for (int32_t c : cnt) {
+      const int64_t r = free_cams ? std::min<int64_t>(c, C) * nc : 0;   // records, at most
+      pairs += (c + r) * (c + r + 1) / 2;
+      recs += r;
+    }
   }
-  const int64_t n = 6 * I, nt = (n + 31) / 32;
-  const int64_t blocks = I * (I + 1) / 2;
+  const int64_t Ie = I + C * nc;
+  const int64_t n = 6 * Ie, nt = (n + 31) / 32;
+  const int64_t blocks = Ie * (Ie + 1) / 2;
   const int64_t items = pairs / 1024 + blocks + 1;
   int64_t b = 0;
   b += K * (4 + 4 + 16 + 4 + 8 * tsz + 20 * tsz + 20 * tsz);   // indices, obs, RW, JR, Z
@@ -256,7 +266,14 @@ int64_t gba_estimate_device_bytes(const gba_problem* p, int32_t precision) {
   b += (K / 512 + 1) * (16 + 28 * 8);                         // image reduce items
   b += C * (80 + 40 + 80);
   b += n * n * tsz + nt * 1024 * tsz;                          // reduced system, tile inverses
-  b += pairs * 8 + items * (16 + 352) + blocks * 12 + I * I * 4;
+  b += pairs * 8 + items * (16 + 352) + blocks * 12 + Ie * Ie * 4;
+  if (free_cams) {
+    b += recs * (20 * tsz + 12) + P * 4;                        // camera Z records, offsets
+    b += K * 20 * tsz + (K / 512 + 1) * 128 * 8 + I * (60 * 8 + 128 * 8 + 4);   // J_c, sums, E, ext
+    b += C * (3 * 80 + 100 * 8 + 10 * 8 + 3 * 8 + 2 * (80 + 40 + 80) + 16 + 8) + I * 4;
+  }
+  const int64_t rows = gba_y_size(p) - 2 * K;                   // constraint and prior rows
+  if (rows > 0) b += rows * 32 + (P + I + 2) * 8 + p->number_of_point_priors * 96;
   return b + (1 << 20);                                        // bookkeeping slack
 }
 

@@ -114,9 +114,37 @@ def test_refuse_over_budget_and_poll():
 @pytest.mark.parametrize("precision", [abi.PRECISION_MIXED, abi.PRECISION_FP64])
 def test_estimate_bounds_plan_bytes(precision):
     from hs_sfm_gb300 import gba
-    for s in _requests(4, seed=13) + [synthetic.ring_scene(num_images=60, num_points=5000)]:
+    extra = [synthetic.ring_scene(num_images=60, num_points=5000),
+             synthetic.full_model_scene(seed=3, num_images=20, num_points=2000, num_cameras=2,
+                                        obs_per_point=4),               # free cameras
+             synthetic.full_model_scene(seed=4, num_images=12, num_points=1500, num_cameras=12,
+                                        obs_per_point=4),               # a camera per image
+             synthetic.gcp_scene(seed=5, num_images=20, num_points=3000, num_gcps=10)]
+    for s in _requests(4, seed=13) + extra:
         est = gba.estimate_device_bytes(s, precision)
         p = gba.Plan(s, abi.make_options(precision=precision, max_iterations=1))
         real = p.device_bytes()
         p.close()
         assert real <= est <= 3 * real + (2 << 20), (s.name, real, est)
+
+
+
+@pytest.mark.gpu
+def test_server_free_cameras_and_priors_match_alone():
+    # requests of the extended models through the server equal their solo solves
+    from hs_sfm_gb300 import gba
+    scenes = [synthetic.full_model_scene(seed=21, num_images=10, num_points=400, obs_per_point=4),
+              synthetic.gcp_scene(seed=22, num_images=10, num_points=500, num_gcps=6),
+              synthetic.full_model_scene(seed=23, num_images=8, num_points=300,
+                                         fix_mask=abi.FIX_CAMERAS, obs_per_point=4)]
+    cfg = gba.default_server_config(precision=abi.PRECISION_FP64)
+    cfg.solve.max_iterations = 8
+    cfg.solve.eps1 = 0.0
+    cfg.solve.eps2 = 0.0
+    with gba.Server(cfg) as srv:
+        tickets = [srv.submit(s) for s in scenes]
+        outs = [srv.wait(t) for t in tickets]
+    for s, (x, rep) in zip(scenes, outs):
+        x1, r1 = gba.solve(s, cfg.solve)
+        assert rep.status == abi.GBA_OK
+        assert rep.final_cost == r1.final_cost and np.array_equal(x, x1)

@@ -1886,9 +1886,15 @@ __global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
       int sel = -1, cnt = 0, mode = kIdle;
       for (int t = 0; t < nown; ++t) {
         if ((rd_s[t] & 0xff) > 0) {
+          const bool diag_at = pr_s[t] >= 0 && kt_s[pr_s[t]] == ti_s[t] - 1;
+          // the chain's subdiagonal tile keeps its last update for the fused
+          // task (below) until L_jj^-1 is out and its diagonal tile has all
+          // other updates: run alone it would split the chain into three
+          // tasks on the critical path (the inputs it waits for never
+          // depend on this tile)
+          if (pr_s[t] >= 0 && kt_s[t] == tj_s[t] - 1 && (!(rd_s[t] >> 8) || !diag_at)) continue;
           sel = t;
           cnt = rd_s[t] & 0xff;
-          const bool diag_at = pr_s[t] >= 0 && kt_s[pr_s[t]] == ti_s[t] - 1;
           mode = kt_s[t] < tj_s[t] ? kUpdate : kFinish;
           if (mode == kFinish && diag_at) mode = kChain;
           // the last update of a subdiagonal tile, its panel and the next

@@ -20,14 +20,23 @@
 //   k_assemble_items per block (i<=j) of the reduced system: -sum Z_a^T Z_b
 //                    over the points seen by both images, rhs terms
 //                    (normal_equation_solver.hpp:190-267,398-420)
-//   k_assemble_S     dense FP64 reduced system S and rhs b
-//   k_chol_*         tiled FP64 Cholesky with the forward solve folded in,
+//   k_assemble_S     dense reduced system S and rhs b (T), block sums in FP64
+//   k_chol_*         tiled Cholesky (T) with the forward solve folded in,
 //                    then the backward solve (normal_equation_solver.hpp:448-466)
-//   k_backsub        delta_p = C^-T (h_p - sum Z_a delta_i), x_new = x - delta
+//   k_backsub        delta_p = C^-T (h_p - sum Z_a delta_i), x_new = x - delta,
+//                    and the candidate's image rotations
 //                    (normal_equation_solver.hpp:468-538)
 //   k_ctrl_*         the LM decisions per problem on the device (Madsen,
 //                    Nielsen & Tingleff 2004, Alg. 3.16 as bound by
 //                    camera_shared_nllso_meta_levenberg_marquardt.hpp:33-106)
+//   free cameras:    k_cam_prep (camera arrays of x), J_c in k_linearize_keys,
+//                    k_image_cam_reduce / k_image_cam_finalize / k_cam_finalize
+//                    (E_i = J_i^T J_c, U_c, g_c), k_camrec_z (camera Z
+//                    records), camera parts in k_assemble_S, k_cam_backsub
+//                    (normal_equation_builder.hpp:157-205,309-349;
+//                     normal_equation_solver.hpp:270-392,422-443)
+//   PCG:             k_assemble_blocks, k_pcg_* (block-Jacobi PCG on the
+//                    explicit 6x6 blocks of S)
 #include "gba_internal.h"
 
 #include <cooperative_groups.h>
@@ -508,8 +517,8 @@ __device__ void image_prep_one(const DevPlan& d, int i, int par) {
 }
 
 // which = 0: the current x of active problems (at init); 1: the candidate of
-// problems whose step is evaluated (the back-substitution prepares it too,
-// so the solve loop does not launch this for the candidate).
+// problems whose step is evaluated.  The solve loop prepares the candidate in
+// k_backsub instead; which = 1 is kept for callers that move x themselves.
 template <typename T>
 __global__ void k_image_prep(DevPlan d, int which) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;

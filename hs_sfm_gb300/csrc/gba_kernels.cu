@@ -2623,6 +2623,25 @@ __device__ double prob_sum(const double* v, int stride, int off, const int* chun
   return block_sum(s, red);
 }
 
+// The first NF fields of a problem's chunk partials (stride fields per
+// chunk) summed in one pass: each thread walks its chunks with NF loads per
+// chunk, four chunks in flight, then fixed-shape trees.  Results in thread 0.
+template <int NF>
+__device__ void prob_sums(const double* v, int stride, const int* chunk_off, int p, double* red,
+                          double* out) {
+  double s[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) s[f] = 0.0;
+  const int c0 = chunk_off[p], c1 = chunk_off[p + 1];
+#pragma unroll 4
+  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) s[f] += v[(long long)stride * c + f];
+  }
+#pragma unroll
+  for (int f = 0; f < NF; ++f) out[f] = block_sum(s[f], red);
+}
+
 // LM control: one CTA per problem (kCtrlThreads), thread 0 decides.
 constexpr int kCtrlThreads = 256;
 
@@ -2631,9 +2650,11 @@ __global__ void __launch_bounds__(kCtrlThreads) k_ctrl_initial_cost(DevPlan d) {
   const int p = blockIdx.x;
   LMState& st = d.state[p];
   if (!st.active) return;
-  double F = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, red);
-  const double raw = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, red);
+  double fr[2];
+  prob_sums<2>(d.key_chunk_sum, 2, d.prob_key_chunk_off, p, red, fr);
   if (threadIdx.x != 0) return;
+  double F = fr[0];
+  const double raw = fr[1];
   if (d.cons_cost) F += d.cons_cost[p];
   st.F = F;
   st.raw = raw;
@@ -2676,18 +2697,20 @@ __global__ void __launch_bounds__(kCtrlThreads) k_ctrl_step(DevPlan d) {
   const bool failed = d.factor_flag[p] != 0;
   double dn2 = 0, xn2 = 0, gd = 0, er = 0;
   if (!failed) {
-    dn2 = prob_sum(d.pt_chunk_sum, 3, 0, d.prob_pt_chunk_off, p, red) +
-          prob_sum(d.img_chunk_sum, 3, 0, d.prob_img_chunk_off, p, red);
-    xn2 = prob_sum(d.pt_chunk_sum, 3, 1, d.prob_pt_chunk_off, p, red) +
-          prob_sum(d.img_chunk_sum, 3, 1, d.prob_img_chunk_off, p, red);
-    gd = prob_sum(d.pt_chunk_sum, 3, 2, d.prob_pt_chunk_off, p, red) +
-         prob_sum(d.img_chunk_sum, 3, 2, d.prob_img_chunk_off, p, red);
+    double sp[3], si[3];
+    prob_sums<3>(d.pt_chunk_sum, 3, d.prob_pt_chunk_off, p, red, sp);
+    prob_sums<3>(d.img_chunk_sum, 3, d.prob_img_chunk_off, p, red, si);
+    dn2 = sp[0] + si[0];
+    xn2 = sp[1] + si[1];
+    gd = sp[2] + si[2];
     // PCG leaves the image rows with residual r: the model decrease gains r^T delta_i
     if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_img_chunk_off, p, red);
     if (d.free_cams) {
-      dn2 += prob_sum(d.cam_sum, 3, 0, d.prob_cam_off, p, red);
-      xn2 += prob_sum(d.cam_sum, 3, 1, d.prob_cam_off, p, red);
-      gd += prob_sum(d.cam_sum, 3, 2, d.prob_cam_off, p, red);
+      double sc[3];
+      prob_sums<3>(d.cam_sum, 3, d.prob_cam_off, p, red, sc);
+      dn2 += sc[0];
+      xn2 += sc[1];
+      gd += sc[2];
     }
   }
   if (threadIdx.x != 0) return;
@@ -2723,9 +2746,11 @@ __global__ void __launch_bounds__(kCtrlThreads) k_ctrl_accept(DevPlan d) {
   const int p = blockIdx.x;
   LMState& st = d.state[p];
   if (!st.evaluate) return;
-  double Fn = prob_sum(d.key_chunk_sum, 2, 0, d.prob_key_chunk_off, p, red);
-  const double raw_n = prob_sum(d.key_chunk_sum, 2, 1, d.prob_key_chunk_off, p, red);
+  double fr[2];
+  prob_sums<2>(d.key_chunk_sum, 2, d.prob_key_chunk_off, p, red, fr);
   if (threadIdx.x != 0) return;
+  double Fn = fr[0];
+  const double raw_n = fr[1];
   if (d.cons_cost) Fn += d.cons_cost[p];
   st.evaluate = 0;
   st.F_new = Fn;

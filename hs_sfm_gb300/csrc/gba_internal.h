@@ -262,5 +262,9 @@ void count_launches(long long n);
 // key order (T precision), vector function (FP64).
 int launch_vector_function(const DevPlan& d, double* y_sorted, cudaStream_t s);
 int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, double* jc, cudaStream_t s);
+// The observed keys split into double-float pairs (mixed path) on the device.
+int launch_split_keys(const DevPlan& d, float2* out, cudaStream_t s);
+// Every problem's current x (x0 before a run) into out [3P + 6I + 10 Ctot (free cameras)].
+int launch_gather_x(const DevPlan& d, int ran, double* out, cudaStream_t s);
 
 }  // namespace gba

@@ -2780,6 +2780,34 @@ __global__ void __launch_bounds__(kCtrlThreads) k_ctrl_accept(DevPlan d) {
   }
 }
 
+// The observed keys as double-float pairs (hi = float(v), lo = float(v - hi)).
+__global__ void k_split_keys(DevPlan d, float2* out) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k >= d.K) return;
+  const double2 o = d.key_obs[k];
+  out[2 * k] = ff_split(o.x);
+  out[2 * k + 1] = ff_split(o.y);
+}
+
+// The current x of every problem (each in its own parity; x0 before a run)
+// gathered into out = [points 3P][images 6I][cameras 10 Ctot].
+__global__ void k_gather_x(DevPlan d, int ran, double* out) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long np = 3LL * d.P, ni = 6LL * d.I, nc = d.free_cams ? 10LL * d.Ctot : 0;
+  if (e < np) {
+    const int par = d.state[d.pt_prob[e / 3]].parity;
+    out[e] = ran ? d.x_pt[par][e] : d.x0_pt[e];
+  } else if (e < np + ni) {
+    const long long f = e - np;
+    const int par = d.state[d.img_prob[f / 6]].parity;
+    out[e] = ran ? d.x_img[par][f] : d.x0_img[f];
+  } else if (e < np + ni + nc) {
+    const long long f = e - np - ni;
+    const int par = d.state[d.cam_info[f / 10].z].parity;
+    out[e] = ran ? d.x_cam[par][f] : d.x0_cam[f];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // stage outputs for parity checks
 // ---------------------------------------------------------------------------
@@ -3123,6 +3151,19 @@ int launch_ctrl_accept(const DevPlan& d, cudaStream_t s) {
 int launch_vector_function(const DevPlan& d, double* y, cudaStream_t s) {
   if (d.K <= 0) return 0;
   k_vector_function<<<(d.K + 255) / 256, 256, 0, s>>>(d, y);
+  return 1;
+}
+
+int launch_split_keys(const DevPlan& d, float2* out, cudaStream_t s) {
+  if (d.K <= 0) return 0;
+  k_split_keys<<<unsigned((d.K + 255) / 256), 256, 0, s>>>(d, out);
+  return 1;
+}
+
+int launch_gather_x(const DevPlan& d, int ran, double* out, cudaStream_t s) {
+  const long long n = 3LL * d.P + 6LL * d.I + (d.free_cams ? 10LL * d.Ctot : 0);
+  if (n <= 0) return 0;
+  k_gather_x<<<unsigned((n + 255) / 256), 256, 0, s>>>(d, ran, out);
   return 1;
 }
 

@@ -320,7 +320,7 @@ namespace {
 // Validates a problem for the device path: points and images free, the
 // shared cameras fixed or (dense solver) free, soft constraints on any free
 // group.
-int validate(const gba_problem& p, bool pcg) {
+int validate(const gba_problem& p, bool pcg, int threads) {
   if (p.number_of_points < 0 || p.number_of_images < 0 || p.number_of_cameras < 0 ||
       p.number_of_keys < 0)
     return GBA_ERR_INVALID;
@@ -374,7 +374,7 @@ int validate(const gba_problem& p, bool pcg) {
   }
   // key indices, in parallel pieces for large problems
   const int64_t nk = p.number_of_keys;
-  const int nth = nk > 200000 ? host_threads() : 1;
+  const int nth = nk > 200000 ? threads : 1;
   std::vector<char> bad(size_t(nth), 0);
   host_parallel(nk, nth, [&](int64_t k0, int64_t k1, int t) {
     for (int64_t k = k0; k < k1; ++k) {
@@ -421,10 +421,20 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   const size_t tsz = mixed ? sizeof(float) : sizeof(double);
   const bool pcg = opt.linear_solver == GBA_LINEAR_PCG;
 
-  for (int q = 0; q < nprob; ++q) {
-    int err = validate(problems[q], pcg);
-    if (err) return err;
-    if (!near_ys || !near_ys[q]) return GBA_ERR_INVALID;
+  if (!near_ys) return GBA_ERR_INVALID;
+  for (int q = 0; q < nprob; ++q)
+    if (!near_ys[q]) return GBA_ERR_INVALID;
+  if (nprob == 1) {
+    if (int err = validate(problems[0], pcg, host_threads())) return err;
+  } else {   // problems in parallel; the first failing problem's status, as in order
+    std::vector<int> errs(nprob, GBA_OK);
+    const int nth = std::min(host_threads(), nprob);
+    std::atomic<int> next{0};
+    host_parallel(nth, nth, [&](int64_t, int64_t, int) {
+      for (int q = next++; q < nprob; q = next++) errs[q] = validate(problems[q], pcg, 1);
+    });
+    for (int e : errs)
+      if (e) return e;
   }
   phase("validate");
   // ---- global sizes
@@ -830,84 +840,168 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     if (pieces[q].err) return pieces[q].err;
   phase("problems");
 
-  // ---- concatenation in problem order
+  // ---- concatenation in problem order: a serial pass sizes every list and
+  // gives each problem its slices, then the problems fill them in parallel
+  // (the layout is exactly that of appending the problems one after another)
   // camera records are Z records K .. K+R-1, after the keys
-  std::vector<int> pt_rec_off;
-  std::vector<int2> rec_info;
-  if (any_free) pt_rec_off.assign(P + 1, int(K));
+  struct Bases {
+    long long img_items = 0, pairs = 0, recs = 0, blocks = 0, items = 0, blk_map = 0;
+    long long key_chunks = 0, pt_chunks = 0, img_chunks = 0, cons = 0, priors = 0;
+  };
+  std::vector<Bases> base(nprob + 1);
   for (int q = 0; q < nprob; ++q) {
+    const Piece& pc = pieces[q];
+    const gba_problem& p = problems[q];
+    const long long np = p.number_of_points, ni = p.number_of_images, nk = p.number_of_keys;
+    Bases b = base[q];
+    b.img_items += (long long)pc.img_items.size();
+    b.pairs += (long long)pc.pairs.size();
+    b.recs += (long long)pc.rec_ext.size();
+    const long long nblk = (long long)pc.blk_ij.size();
+    b.blocks += nblk;
+    for (long long t = 0; t < nblk; ++t) {
+      const long long cntp = pc.blk_off[t + 1] - pc.blk_off[t];
+      b.items += std::max<long long>(1, (cntp + kPairItem - 1) / kPairItem);
+    }
+    b.blk_map += (long long)pc.blk_map.size();
+    b.key_chunks += (nk + kKeyChunk - 1) / kKeyChunk;
+    b.pt_chunks += (np + kPointChunk - 1) / kPointChunk;
+    b.img_chunks += (ni + kImageChunk - 1) / kImageChunk;
+    b.cons += (long long)pc.cons.size();
+    b.priors += (long long)pc.prior_pt.size();
+    base[q + 1] = b;
+  }
+  const Bases& tot = base[nprob];
+  if (tot.pairs > INT32_MAX || (long long)K + tot.recs > INT32_MAX || tot.items > INT32_MAX)
+    return GBA_ERR_INVALID;
+  img_items.resize(tot.img_items);
+  img_item_off.assign(size_t(I) + 1, 0);
+  // the pair lists (the largest array): one problem's list moves into place;
+  // a batch's lists go straight from each problem to its slice on the device
+  int2* d_pairs = nprob > 1 ? arena.alloc<int2>(size_t(tot.pairs)) : nullptr;
+  std::atomic<int> pair_upload_failed{0};
+  std::vector<int> pt_rec_off;
+  std::vector<int2> rec_info(tot.recs);
+  if (any_free) pt_rec_off.assign(P + 1, int(K));
+  blk_ij.resize(tot.blocks);
+  blk_item_off.assign(size_t(tot.blocks) + 1, 0);
+  items.resize(tot.items);
+  if (!pcg) {
+    if (nprob == 1)
+      blk_map.swap(pieces[0].blk_map);
+    else
+      blk_map.resize(tot.blk_map);
+  }
+  key_chunks.resize(tot.key_chunks);
+  pt_chunks.resize(tot.pt_chunks);
+  img_chunks.resize(tot.img_chunks);
+  cons.resize(tot.cons);
+  cons_yw.resize(tot.cons);
+  prior_pt.resize(tot.priors);
+  prior_y.resize(3 * tot.priors);
+  prior_info.resize(9 * tot.priors);
+  prob_key_chunk_off.assign(nprob + 1, 0);
+  prob_pt_chunk_off.assign(nprob + 1, 0);
+  prob_img_chunk_off.assign(nprob + 1, 0);
+  prob_cons_off.assign(nprob + 1, 0);
+  prob_prior_off.assign(nprob + 1, 0);
+  for (int q = 0; q < nprob; ++q) {   // first entries (shared with the previous problem's last)
+    pt_key_off[pbase[q]] = int(kbase[q]);
+    img_key_off[ibase[q]] = int(kbase[q]);
+  }
+  for (int q = 0; q <= nprob; ++q) {
+    prob_key_chunk_off[q] = int(base[q].key_chunks);
+    prob_pt_chunk_off[q] = int(base[q].pt_chunks);
+    prob_img_chunk_off[q] = int(base[q].img_chunks);
+    prob_cons_off[q] = int(base[q].cons);
+    prob_prior_off[q] = int(base[q].priors);
+  }
+  auto fill_one = [&](int q) {
     Piece& pc = pieces[q];
     ProbInfo& pi = prob[q];
     const gba_problem& p = problems[q];
+    const Bases& b = base[q];
     const int np = int(p.number_of_points), ni = int(p.number_of_images), nk = int(p.number_of_keys);
     const int64_t pb = pbase[q], ib = ibase[q], kb = kbase[q];
-    pt_key_off[pb] = int(kb);
-    img_key_off[ib] = int(kb);
-    for (int i = 0, t = 0; i < ni; ++i) {
-      for (int u = 0; u < pc.img_item_cnt[i]; ++u) img_items.push_back(pc.img_items[t++]);
-      img_item_off.push_back(int(img_items.size()));
+    std::copy(pc.img_items.begin(), pc.img_items.end(), img_items.begin() + b.img_items);
+    for (int i = 0, acc = int(b.img_items); i < ni; ++i) {
+      acc += pc.img_item_cnt[i];
+      img_item_off[ib + i + 1] = acc;
     }
-    const int block_begin = int(blk_ij.size());
-    const long long pair_base = (long long)pairs.size();
-    if (pair_base + (long long)pc.pairs.size() > INT32_MAX) return GBA_ERR_INVALID;
-    const long long rec_base = (long long)K + (long long)rec_info.size();
-    if (rec_base + (long long)pc.rec_ext.size() > INT32_MAX) return GBA_ERR_INVALID;
+    const long long rec_base = (long long)K + b.recs;
     if (!pc.rec_ext.empty()) {
       for (int2& pr : pc.pairs) {   // camera records: -(local + 1) -> global record
         if (pr.x < 0) pr.x = int(rec_base - 1 - pr.x);
         if (pr.y < 0) pr.y = int(rec_base - 1 - pr.y);
       }
       for (int i = 0; i < np; ++i) pt_rec_off[pb + i] = int(rec_base + pc.pt_rec_off[i]);
-      for (int e : pc.rec_ext)
-        rec_info.push_back(make_int2(int(cbase[q]) + (e - ni) / pi.nc, pi.ext_begin + e));
+      for (size_t r = 0; r < pc.rec_ext.size(); ++r) {
+        const int e = pc.rec_ext[r];
+        rec_info[b.recs + r] = make_int2(int(cbase[q]) + (e - ni) / pi.nc, pi.ext_begin + e);
+      }
     } else if (any_free) {
       for (int i = 0; i < np; ++i) pt_rec_off[pb + i] = int(rec_base);
     }
-    if (pairs.empty())   // the first problem's list moves instead of copying
+    if (nprob == 1)
       pairs.swap(pc.pairs);
-    else
-      pairs.insert(pairs.end(), pc.pairs.begin(), pc.pairs.end());
-    blk_ij.insert(blk_ij.end(), pc.blk_ij.begin(), pc.blk_ij.end());
+    else if (!pc.pairs.empty() &&
+             cudaMemcpyAsync(d_pairs + b.pairs, pc.pairs.data(), sizeof(int2) * pc.pairs.size(),
+                             cudaMemcpyHostToDevice, stream) != cudaSuccess)
+      pair_upload_failed = 1;
+    const int block_begin = int(b.blocks);
+    std::copy(pc.blk_ij.begin(), pc.blk_ij.end(), blk_ij.begin() + b.blocks);
     const int nblk = int(pc.blk_ij.size());
     pi.block_begin = block_begin;
     pi.num_blocks = nblk;
-    pi.item_begin = int(items.size());
+    pi.item_begin = int(b.items);
+    long long it = b.items;
     for (int t = 0; t < nblk; ++t) {
-      const long long s0 = pair_base + pc.blk_off[t], s1 = pair_base + pc.blk_off[t + 1];
-      long long s = s0;
+      const long long s0 = b.pairs + pc.blk_off[t], s1 = b.pairs + pc.blk_off[t + 1];
+      long long s_ = s0;
       do {
-        long long e = std::min(s1, s + kPairItem);
-        items.push_back(make_int4(block_begin + t, int(s), int(e), q));
-        s = e;
-      } while (s < s1);
-      blk_item_off.push_back(int(items.size()));
+        const long long e = std::min(s1, s_ + kPairItem);
+        items[it++] = make_int4(block_begin + t, int(s_), int(e), q);
+        s_ = e;
+      } while (s_ < s1);
+      blk_item_off[block_begin + t + 1] = int(it);
     }
-    pi.num_items = int(items.size()) - pi.item_begin;
-    blk_map_off[q] = (long long)blk_map.size();
-    if (!pcg && blk_map.empty() && block_begin == 0)
-      blk_map.swap(pc.blk_map);
-    else if (!pcg)
-      for (int v : pc.blk_map) blk_map.push_back(v >= 0 ? v + block_begin : -1);
+    pi.num_items = int(it - b.items);
+    blk_map_off[q] = b.blk_map;
+    if (!pcg && nprob > 1)
+      for (size_t e = 0; e < pc.blk_map.size(); ++e)
+        blk_map[b.blk_map + e] = pc.blk_map[e] >= 0 ? pc.blk_map[e] + block_begin : -1;
     // work chunks
-    for (int s = 0; s < nk; s += kKeyChunk)
-      key_chunks.push_back(Chunk{q, int(kb + s), int(kb + std::min(nk, s + kKeyChunk)), 0});
-    prob_key_chunk_off.push_back(int(key_chunks.size()));
-    for (int s = 0; s < np; s += kPointChunk)
-      pt_chunks.push_back(Chunk{q, int(pb + s), int(pb + std::min(np, s + kPointChunk)), 0});
-    prob_pt_chunk_off.push_back(int(pt_chunks.size()));
-    for (int s = 0; s < ni; s += kImageChunk)
-      img_chunks.push_back(Chunk{q, int(ib + s), int(ib + std::min(ni, s + kImageChunk)), 0});
-    prob_img_chunk_off.push_back(int(img_chunks.size()));
-    cons.insert(cons.end(), pc.cons.begin(), pc.cons.end());
-    cons_yw.insert(cons_yw.end(), pc.cons_yw.begin(), pc.cons_yw.end());
-    prob_cons_off.push_back(int(cons.size()));
-    prior_pt.insert(prior_pt.end(), pc.prior_pt.begin(), pc.prior_pt.end());
-    prior_y.insert(prior_y.end(), pc.prior_y.begin(), pc.prior_y.end());
-    prior_info.insert(prior_info.end(), pc.prior_info.begin(), pc.prior_info.end());
-    prob_prior_off.push_back(int(prior_pt.size()));
+    long long c = b.key_chunks;
+    for (int s_ = 0; s_ < nk; s_ += kKeyChunk)
+      key_chunks[c++] = Chunk{q, int(kb + s_), int(kb + std::min(nk, s_ + kKeyChunk)), 0};
+    c = b.pt_chunks;
+    for (int s_ = 0; s_ < np; s_ += kPointChunk)
+      pt_chunks[c++] = Chunk{q, int(pb + s_), int(pb + std::min(np, s_ + kPointChunk)), 0};
+    c = b.img_chunks;
+    for (int s_ = 0; s_ < ni; s_ += kImageChunk)
+      img_chunks[c++] = Chunk{q, int(ib + s_), int(ib + std::min(ni, s_ + kImageChunk)), 0};
+    std::copy(pc.cons.begin(), pc.cons.end(), cons.begin() + b.cons);
+    std::copy(pc.cons_yw.begin(), pc.cons_yw.end(), cons_yw.begin() + b.cons);
+    std::copy(pc.prior_pt.begin(), pc.prior_pt.end(), prior_pt.begin() + b.priors);
+    std::copy(pc.prior_y.begin(), pc.prior_y.end(), prior_y.begin() + 3 * b.priors);
+    std::copy(pc.prior_info.begin(), pc.prior_info.end(), prior_info.begin() + 9 * b.priors);
     std::vector<int>().swap(pc.blk_map);   // release as we go
     std::vector<int2>().swap(pc.pairs);
+  };
+  if (nprob == 1) {
+    fill_one(0);
+  } else {
+    const int nth = std::min(host_threads(), nprob);
+    std::atomic<int> next{0};
+    host_parallel(nth, nth, [&](int64_t, int64_t, int) {
+      for (int q = next++; q < nprob; q = next++) fill_one(q);
+    });
   }
+  if (pair_upload_failed) {
+    cudaGetLastError();
+    throw CudaError{GBA_ERR_CUDA};
+  }
+  if (d_pairs) arena.uploaded += (long long)(sizeof(int2) * tot.pairs);
   pt_key_off[P] = int(K);
   img_key_off[I] = int(K);
   const int R = int(rec_info.size());
@@ -955,20 +1049,20 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.cam32[1] = any_free ? arena.upload(cam32) : D.cam32[0];
   D.cam_ff[0] = D.cam_ff[1] = nullptr;
   if (mixed) {
-    std::vector<float2> obs_ff(2 * K), cam_ff(10 * std::max<int64_t>(C, 1));
+    std::vector<float2> cam_ff(10 * std::max<int64_t>(C, 1));
     auto split = [](double v) {
       float hi = float(v);
       return make_float2(hi, float(v - double(hi)));
     };
-    for (int64_t k = 0; k < K; ++k) {
-      obs_ff[2 * k] = split(key_obs[k].x);
-      obs_ff[2 * k + 1] = split(key_obs[k].y);
-    }
     for (int64_t c = 0; c < C; ++c) {
       for (int j = 0; j < 9; ++j) cam_ff[10 * c + j] = split(cam64[10 * c + j]);
       cam_ff[10 * c + 9] = split(cam64[10 * c + 5] * cam64[10 * c + 9]);   // f * a
     }
-    D.key_obs_ff = arena.upload(obs_ff);
+    // the keys' double-float pairs are split on the device from key_obs
+    float2* obs_ff = arena.alloc<float2>(2 * K);
+    launch_split_keys(D, obs_ff, stream);
+    count_launches(1);
+    D.key_obs_ff = obs_ff;
     D.cam_ff[0] = arena.upload(cam_ff);
     D.cam_ff[1] = any_free ? arena.upload(cam_ff) : D.cam_ff[0];
   }
@@ -1110,7 +1204,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       }
     }
   }
-  D.pairs = arena.upload(pairs);
+  D.pairs = d_pairs ? d_pairs : arena.upload(pairs);
   D.items = arena.upload(items);
   D.blk_ij = arena.upload(blk_ij);
   D.blk_item_off = arena.upload(blk_item_off);
@@ -1360,6 +1454,31 @@ double bits_to_double(unsigned long long b) {
   return v;
 }
 
+// A problem's report from its LM state and the plan's timings.
+void fill_report(const gba::Plan& P, int q, const gba::LMState& st, gba_report* r) {
+  std::memset(r, 0, sizeof(*r));
+  r->status = st.status;
+  r->stop_reason = st.stop;
+  r->iterations = st.iter;
+  r->accepted = st.accepted;
+  r->rejected = st.rejected;
+  r->factor_failures = st.factor_fail;
+  r->pcg_iterations = st.pcg_iters;
+  r->initial_cost = st.initial_cost;
+  r->final_cost = st.F;
+  const int K = P.prob[q].num_keys;
+  r->final_rmse = K > 0 ? std::sqrt(std::max(st.raw, 0.0) / K) : 0.0;   // plain residuals
+  r->final_mu = st.mu;
+  r->final_gradient_inf_norm = bits_to_double(st.ginf_bits);
+  r->setup_ms = P.setup_ms;
+  float ms = 0;
+  if (P.ran) cudaEventElapsedTime(&ms, P.ev0, P.ev1);
+  r->solve_ms = ms;
+  for (int s = 0; s < GBA_NUM_STAGES; ++s) r->stage_ms[s] = P.stage_ms[s];
+  r->h2d_bytes = P.h2d_bytes + P.arena.uploaded;
+  r->d2h_bytes = P.d2h_bytes;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1552,31 +1671,93 @@ int gba_plan_get_report(gba_plan* p, int32_t q, gba_report* r) {
     gba::LMState st;
     GBA_CUDA(cudaStreamSynchronize(P.stream));
     GBA_CUDA(cudaMemcpy(&st, P.d.state + q, sizeof(st), cudaMemcpyDeviceToHost));
-    std::memset(r, 0, sizeof(*r));
-    r->status = st.status;
-    r->stop_reason = st.stop;
-    r->iterations = st.iter;
-    r->accepted = st.accepted;
-    r->rejected = st.rejected;
-    r->factor_failures = st.factor_fail;
-    r->pcg_iterations = st.pcg_iters;
-    r->initial_cost = st.initial_cost;
-    r->final_cost = st.F;
-    const int K = P.prob[q].num_keys;
-    r->final_rmse = K > 0 ? std::sqrt(std::max(st.raw, 0.0) / K) : 0.0;   // plain residuals
-    r->final_mu = st.mu;
-    r->final_gradient_inf_norm = bits_to_double(st.ginf_bits);
-    r->setup_ms = P.setup_ms;
-    float ms = 0;
-    if (P.ran) cudaEventElapsedTime(&ms, P.ev0, P.ev1);
-    r->solve_ms = ms;
-    for (int s = 0; s < GBA_NUM_STAGES; ++s) r->stage_ms[s] = P.stage_ms[s];
     P.d2h_bytes += (long long)sizeof(st);
-    r->h2d_bytes = P.h2d_bytes + P.arena.uploaded;
-    r->d2h_bytes = P.d2h_bytes;
+    fill_report(P, q, st, r);
     return GBA_OK;
   });
 }
+
+}  // extern "C"
+
+namespace {
+
+// Every problem's x and report in one device gather and a few copies (the
+// batch path of gba_solve_batch; the per-problem calls would synchronize the
+// stream once per problem).
+int get_all(gba::Plan& P, double* const* xs, gba_report* reports) {
+  return guarded([&] {
+    GBA_CUDA(cudaStreamSynchronize(P.stream));
+    std::vector<gba::LMState> st(P.B);
+    GBA_CUDA(cudaMemcpy(st.data(), P.d.state, sizeof(gba::LMState) * P.B, cudaMemcpyDeviceToHost));
+    const long long np = 3LL * P.d.P, ni = 6LL * P.d.I, nc = P.d.free_cams ? 10LL * P.d.Ctot : 0;
+    std::vector<double> h(size_t(np + ni + nc));
+    if (!h.empty()) {
+      double* dx = P.arena.alloc<double>(h.size());
+      gba::launch_gather_x(P.d, P.ran ? 1 : 0, dx, P.stream);
+      gba::count_launches(1);
+      GBA_CUDA(cudaMemcpyAsync(h.data(), dx, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, P.stream));
+      GBA_CUDA(cudaStreamSynchronize(P.stream));
+      GBA_CUDA(cudaGetLastError());
+    }
+    P.d2h_bytes += (long long)(sizeof(gba::LMState) * P.B + sizeof(double) * h.size());
+    const int nth = std::min(gba::host_threads(), P.B);
+    std::atomic<int> next{0};
+    gba::host_parallel(nth, nth, [&](int64_t, int64_t, int) {
+      for (int q = next++; q < P.B; q = next++) {
+        const gba::ProbInfo& pi = P.prob[q];
+        double* x = xs[q];
+        std::copy(h.begin() + 3LL * pi.point_begin, h.begin() + 3LL * (pi.point_begin + pi.num_points), x);
+        std::copy(h.begin() + np + 6LL * pi.image_begin,
+                  h.begin() + np + 6LL * (pi.image_begin + pi.num_images), x + 3LL * pi.num_points);
+        double* xc = x + 3LL * pi.num_points + 6LL * pi.num_images;
+        for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
+          std::copy(h.begin() + np + ni + 10LL * (pi.cam_begin + c),
+                    h.begin() + np + ni + 10LL * (pi.cam_begin + c) + pi.cps, xc + (size_t)pi.cps * c);
+        if (reports) fill_report(P, q, st[q], &reports[q]);
+      }
+    });
+    return GBA_OK;
+  });
+}
+
+// Every problem's x0 scattered on the host and uploaded in a few copies.
+int set_all_x0(gba::Plan& P, const double* const* xs) {
+  return guarded([&] {
+    const long long np = 3LL * P.d.P, ni = 6LL * P.d.I, nc = P.d.free_cams ? 10LL * P.d.Ctot : 0;
+    std::vector<double> h(size_t(np + ni + nc), 0.0);
+    const int nth = std::min(gba::host_threads(), P.B);
+    std::atomic<int> next{0};
+    gba::host_parallel(nth, nth, [&](int64_t, int64_t, int) {
+      for (int q = next++; q < P.B; q = next++) {
+        const gba::ProbInfo& pi = P.prob[q];
+        const double* x = xs[q];
+        std::copy(x, x + 3LL * pi.num_points, h.begin() + 3LL * pi.point_begin);
+        std::copy(x + 3LL * pi.num_points, x + 3LL * pi.num_points + 6LL * pi.num_images,
+                  h.begin() + np + 6LL * pi.image_begin);
+        const double* xc = x + 3LL * pi.num_points + 6LL * pi.num_images;
+        for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
+          std::copy(xc + (size_t)pi.cps * c, xc + (size_t)pi.cps * (c + 1),
+                    h.begin() + np + ni + 10LL * (pi.cam_begin + c));
+      }
+    });
+    if (np)
+      GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_pt), h.data(), sizeof(double) * np,
+                               cudaMemcpyHostToDevice, P.stream));
+    if (ni)
+      GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_img), h.data() + np, sizeof(double) * ni,
+                               cudaMemcpyHostToDevice, P.stream));
+    if (nc)
+      GBA_CUDA(cudaMemcpyAsync(P.d.x0_cam, h.data() + np + ni, sizeof(double) * nc, cudaMemcpyHostToDevice,
+                               P.stream));
+    GBA_CUDA(cudaStreamSynchronize(P.stream));
+    P.h2d_bytes += (long long)sizeof(double) * (long long)h.size();
+    return GBA_OK;
+  });
+}
+
+}  // namespace
+
+extern "C" {
 
 int gba_plan_query(gba_plan* p) {
   if (!p) return GBA_ERR_INVALID;
@@ -1630,13 +1811,12 @@ int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, i
   gba_plan* plan = nullptr;
   int err = gba_plan_create(problems, near_ys, n, &once, &plan);
   if (err) return err;
-  for (int q = 0; q < n && !err; ++q) err = gba_plan_set_initial_x(plan, q, x_inout[q]);
+  for (int q = 0; q < n && !err; ++q)
+    if (!x_inout[q]) err = GBA_ERR_INVALID;
+  if (!err) err = set_all_x0(plan->impl, x_inout);
   if (!err) err = gba_plan_run(plan);
   if (!err) err = gba_plan_synchronize(plan);
-  for (int q = 0; q < n && !err; ++q) {
-    err = gba_plan_get_x(plan, q, x_inout[q]);
-    if (!err && reports) err = gba_plan_get_report(plan, q, &reports[q]);
-  }
+  if (!err) err = get_all(plan->impl, x_inout, reports);
   int first_status = GBA_OK;
   if (!err && reports)
     for (int q = 0; q < n; ++q)

@@ -1801,6 +1801,20 @@ int gba_plan_device_bytes(gba_plan* p, int64_t* bytes) {
   return GBA_OK;
 }
 
+int gba_plan_set_initial_x_all(gba_plan* p, const double* const* x0s) {
+  if (!p || !x0s) return GBA_ERR_INVALID;
+  for (int q = 0; q < p->impl.B; ++q)
+    if (!x0s[q] && p->impl.x_size[q] > 0) return GBA_ERR_INVALID;
+  return set_all_x0(p->impl, x0s);
+}
+
+int gba_plan_get_all(gba_plan* p, double* const* xs, gba_report* reports) {
+  if (!p || !xs) return GBA_ERR_INVALID;
+  for (int q = 0; q < p->impl.B; ++q)
+    if (!xs[q] && p->impl.x_size[q] > 0) return GBA_ERR_INVALID;
+  return get_all(p->impl, xs, reports);
+}
+
 int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, int32_t n,
                     const gba_options* options, double* const* x_inout, gba_report* reports) {
   if (!x_inout || !options) return GBA_ERR_INVALID;
@@ -1812,7 +1826,7 @@ int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, i
   int err = gba_plan_create(problems, near_ys, n, &once, &plan);
   if (err) return err;
   for (int q = 0; q < n && !err; ++q)
-    if (!x_inout[q]) err = GBA_ERR_INVALID;
+    if (!x_inout[q] && plan->impl.x_size[q] > 0) err = GBA_ERR_INVALID;
   if (!err) err = set_all_x0(plan->impl, x_inout);
   if (!err) err = gba_plan_run(plan);
   if (!err) err = gba_plan_synchronize(plan);

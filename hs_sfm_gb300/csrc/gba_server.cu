@@ -111,7 +111,15 @@ struct gba_server {
   std::thread worker;
 
   void harvest_locked(Batch& b) {
-    const int qst = gba_plan_synchronize(b.plan);
+    int qst = gba_plan_synchronize(b.plan);
+    // every request's x and report in one gather
+    std::vector<double*> xs(b.reqs.size());
+    std::vector<gba_report> reps(b.reqs.size());
+    for (size_t q = 0; q < b.reqs.size(); ++q) {
+      b.reqs[q]->x.assign(size_t(b.reqs[q]->x_size), 0.0);
+      xs[q] = b.reqs[q]->x.data();
+    }
+    if (qst == GBA_OK) qst = gba_plan_get_all(b.plan, xs.data(), reps.data());
     for (size_t q = 0; q < b.reqs.size(); ++q) {
       Request* r = b.reqs[q];
       r->t_done = Clock::now();
@@ -120,11 +128,11 @@ struct gba_server {
         r->status = GBA_ERR_CANCELLED;
         continue;
       }
-      r->x.assign(size_t(r->x_size), 0.0);
       int st = qst;
-      if (st == GBA_OK) st = gba_plan_get_x(b.plan, int32_t(q), r->x.data());
-      if (st == GBA_OK) st = gba_plan_get_report(b.plan, int32_t(q), &r->report);
-      if (st == GBA_OK) st = r->report.status;
+      if (st == GBA_OK) {
+        r->report = reps[q];
+        st = r->report.status;
+      }
       r->report.queue_ms = ms_between(r->t_submit, r->t_admit);
       r->report.latency_ms = ms_between(r->t_submit, r->t_done);
       r->status = st;
@@ -182,8 +190,11 @@ struct gba_server {
           o.use_cuda_graph = 0;   // a micro-batch plan runs once
           o.shared_device = 1;    // several micro-batches run at the same time
           int st = gba_plan_create(probs.data(), ys.data(), int32_t(probs.size()), &o, &b.plan);
-          for (size_t q = 0; st == GBA_OK && q < b.reqs.size(); ++q)
-            st = gba_plan_set_initial_x(b.plan, int32_t(q), b.reqs[q]->x0.data());
+          if (st == GBA_OK) {
+            std::vector<const double*> x0s;
+            for (Request* r : b.reqs) x0s.push_back(r->x0.data());
+            st = gba_plan_set_initial_x_all(b.plan, x0s.data());
+          }
           if (st == GBA_OK) st = gba_plan_run(b.plan);
           lk.lock();
           if (st != GBA_OK) {

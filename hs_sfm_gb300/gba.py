@@ -58,6 +58,8 @@ def lib():
     L.gba_plan_synchronize.argtypes = [vp]
     L.gba_plan_get_x.argtypes = [vp, C.c_int32, d]
     L.gba_plan_get_report.argtypes = [vp, C.c_int32, R]
+    L.gba_plan_set_initial_x_all.argtypes = [vp, C.POINTER(d)]
+    L.gba_plan_get_all.argtypes = [vp, C.POINTER(d), R]
     L.gba_plan_last_run_ms.argtypes = [vp, d]
     L.gba_plan_kernel_stats.argtypes = [vp, C.c_int32, d, C.POINTER(C.c_int32)]
     L.gba_plan_last_run_launches.argtypes = [vp, C.POINTER(C.c_int64)]
@@ -140,8 +142,21 @@ class Plan:
         _check(L.gba_plan_create(self._arr, yp, len(self.scenes), C.byref(self.options),
                                  C.byref(h)), "gba_plan_create")
         self.h = h
-        for q, s in enumerate(self.scenes):
-            self.set_initial_x(q, s.x0)
+        self.set_initial_x_all([s.x0 for s in self.scenes])
+
+    def set_initial_x_all(self, x0s):
+        """Every problem's x0 in one upload (gba_plan_set_initial_x_all)."""
+        xs = [_f64(x) for x in x0s]
+        xp = (C.POINTER(C.c_double) * len(xs))(*[abi.dptr(x) for x in xs])
+        _check(lib().gba_plan_set_initial_x_all(self.h, xp), "set_initial_x_all")
+
+    def get_all(self):
+        """Every problem's (x, report) in one gather (gba_plan_get_all)."""
+        xs = [np.zeros(c.x_size) for c in self._cps]
+        xp = (C.POINTER(C.c_double) * len(xs))(*[abi.dptr(x) for x in xs])
+        reps = (abi.Report * len(xs))()
+        _check(lib().gba_plan_get_all(self.h, xp, reps), "get_all")
+        return xs, list(reps)
 
     def set_initial_x(self, q, x0):
         x0 = _f64(x0)

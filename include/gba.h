@@ -256,6 +256,11 @@ GBA_API int gba_plan_synchronize(gba_plan* plan);
  * device, GBA_ERR_BUSY while it is still running. */
 GBA_API int gba_plan_query(gba_plan* plan);
 GBA_API int gba_plan_get_x(gba_plan* plan, int32_t problem, double* x_out);
+/* Every problem at once (x0s / xs [number of problems] host pointers; reports
+ * may be NULL): one upload, one device gather and one copy instead of one
+ * synchronizing call per problem. */
+GBA_API int gba_plan_set_initial_x_all(gba_plan* plan, const double* const* x0s);
+GBA_API int gba_plan_get_all(gba_plan* plan, double* const* xs, gba_report* reports);
 GBA_API int gba_plan_get_report(gba_plan* plan, int32_t problem, gba_report* report);
 /* Device time of the last gba_plan_run in milliseconds (CUDA events on the
  * plan's stream), and the average duration of the named kernel's launches

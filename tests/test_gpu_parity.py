@@ -276,3 +276,24 @@ def test_nan_observation_reports_status(gba):
     with pytest.raises(gba.GbaError) as e:
         gba.solve(s)
     assert e.value.status == abi.GBA_ERR_NAN
+
+
+def test_plan_batched_x_and_reports_equal_per_problem_calls(gba):
+    # gba_plan_set_initial_x_all / gba_plan_get_all against the per-problem calls
+    scenes = synthetic.window_batch(num_windows=6, seed=31, images_range=(5, 12),
+                                    points_range=(200, 900))
+    scenes.append(synthetic.full_model_scene(seed=32, num_images=8, num_points=300,
+                                             obs_per_point=4))   # free cameras
+    plan = gba.Plan(scenes, abi.make_options(max_iterations=5, eps1=0.0, eps2=0.0))
+    xs0, reps0 = plan.get_all()            # before a run: x0
+    for q, s in enumerate(scenes):
+        np.testing.assert_array_equal(xs0[q], s.x0)
+    plan.run()
+    plan.synchronize()
+    xs, reps = plan.get_all()
+    for q in range(len(scenes)):
+        np.testing.assert_array_equal(xs[q], plan.x(q))
+        r = plan.report(q)
+        assert (reps[q].final_cost, reps[q].iterations, reps[q].status) == \
+            (r.final_cost, r.iterations, r.status)
+    plan.close()

@@ -297,3 +297,26 @@ def test_plan_batched_x_and_reports_equal_per_problem_calls(gba):
         assert (reps[q].final_cost, reps[q].iterations, reps[q].status) == \
             (r.final_cost, r.iterations, r.status)
     plan.close()
+
+
+def test_concurrent_solves_from_host_threads(gba):
+    # gba_solve is re-entrant: solves on several host threads at once (each
+    # plan has its own stream; ctypes releases the GIL) give the same bits as
+    # the same solves one after another
+    import threading
+    scenes = [synthetic.ring_scene(num_images=10 + 2 * i, num_points=1500, obs_per_point=5, seed=40 + i)
+              for i in range(6)]
+    opt = abi.make_options(max_iterations=10, eps1=0.0, eps2=0.0, precision=abi.PRECISION_MIXED)
+    alone = [gba.solve(s, opt) for s in scenes]
+    out = [None] * len(scenes)
+
+    def work(i):
+        out[i] = gba.solve(scenes[i], opt)
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(len(scenes))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for (x0, r0), (x1, r1) in zip(alone, out):
+        assert np.array_equal(x0, x1) and r0.final_cost == r1.final_cost

@@ -1815,6 +1815,26 @@ int gba_plan_get_all(gba_plan* p, double* const* xs, gba_report* reports) {
   return get_all(p->impl, xs, reports);
 }
 
+int gba_batch_create(const gba_problem* problems, const double* const* near_ys, int32_t n,
+                     const gba_options* options, gba_batch** batch) {
+  return gba_plan_create(problems, near_ys, n, options, batch);
+}
+
+int gba_batch_submit(gba_batch* b, const double* const* x0s) {
+  int err = gba_plan_set_initial_x_all(b, x0s);
+  return err ? err : gba_plan_run(b);
+}
+
+int gba_batch_poll(gba_batch* b, double* const* xs, gba_report* reports) {
+  if (!b) return GBA_ERR_INVALID;
+  const int st = gba_plan_query(b);
+  if (st != GBA_OK) return st;
+  int err = gba_plan_synchronize(b);   // the run is over: picks up its errors and profile
+  return err ? err : gba_plan_get_all(b, xs, reports);
+}
+
+int gba_batch_destroy(gba_batch* b) { return gba_plan_destroy(b); }
+
 int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, int32_t n,
                     const gba_options* options, double* const* x_inout, gba_report* reports) {
   if (!x_inout || !options) return GBA_ERR_INVALID;

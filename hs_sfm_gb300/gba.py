@@ -59,6 +59,10 @@ def lib():
     L.gba_plan_get_x.argtypes = [vp, C.c_int32, d]
     L.gba_plan_get_report.argtypes = [vp, C.c_int32, R]
     L.gba_plan_set_initial_x_all.argtypes = [vp, C.POINTER(d)]
+    L.gba_batch_create.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(vp)]
+    L.gba_batch_submit.argtypes = [vp, C.POINTER(d)]
+    L.gba_batch_poll.argtypes = [vp, C.POINTER(d), R]
+    L.gba_batch_destroy.argtypes = [vp]
     L.gba_plan_get_all.argtypes = [vp, C.POINTER(d), R]
     L.gba_plan_last_run_ms.argtypes = [vp, d]
     L.gba_plan_kernel_stats.argtypes = [vp, C.c_int32, d, C.POINTER(C.c_int32)]

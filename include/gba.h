@@ -261,6 +261,19 @@ GBA_API int gba_plan_get_x(gba_plan* plan, int32_t problem, double* x_out);
  * synchronizing call per problem. */
 GBA_API int gba_plan_set_initial_x_all(gba_plan* plan, const double* const* x0s);
 GBA_API int gba_plan_get_all(gba_plan* plan, double* const* xs, gba_report* reports);
+
+/* Batched form (create once, submit initial x, poll for the results): the
+ * asynchronous face of a plan.  submit uploads every problem's x0 and
+ * launches the solve without waiting; poll returns GBA_ERR_BUSY while the
+ * device is still solving, else fills xs / reports (as gba_plan_get_all) and
+ * returns GBA_OK.  A batch may be submitted again after a poll succeeded. */
+typedef struct gba_plan gba_batch;
+GBA_API int gba_batch_create(const gba_problem* problems, const double* const* near_ys,
+                             int32_t number_of_problems, const gba_options* options,
+                             gba_batch** batch);
+GBA_API int gba_batch_submit(gba_batch* batch, const double* const* x0s);
+GBA_API int gba_batch_poll(gba_batch* batch, double* const* xs, gba_report* reports);
+GBA_API int gba_batch_destroy(gba_batch* batch);
 GBA_API int gba_plan_get_report(gba_plan* plan, int32_t problem, gba_report* report);
 /* Device time of the last gba_plan_run in milliseconds (CUDA events on the
  * plan's stream), and the average duration of the named kernel's launches

@@ -320,3 +320,36 @@ def test_concurrent_solves_from_host_threads(gba):
         t.join()
     for (x0, r0), (x1, r1) in zip(alone, out):
         assert np.array_equal(x0, x1) and r0.final_cost == r1.final_cost
+
+
+def test_batch_create_submit_poll(gba):
+    # the asynchronous batch face (gba_batch_*): submit returns before the
+    # solve ends, poll answers BUSY until it has, then gives gba_solve_batch's bits
+    import ctypes as C
+    L = gba.lib()
+    scenes = synthetic.window_batch(num_windows=5, seed=51, images_range=(5, 12),
+                                    points_range=(300, 1200))
+    opt = abi.make_options(max_iterations=8, eps1=0.0, eps2=0.0, precision=abi.PRECISION_MIXED)
+    cps = [abi.CProblem(s) for s in scenes]
+    arr = (abi.Problem * len(cps))(*[c.problem for c in cps])
+    ys = [np.ascontiguousarray(s.near_y, dtype=np.float64) for s in scenes]
+    yp = (C.POINTER(C.c_double) * len(ys))(*[abi.dptr(y) for y in ys])
+    h = C.c_void_p()
+    assert L.gba_batch_create(arr, yp, len(scenes), C.byref(opt), C.byref(h)) == abi.GBA_OK
+    x0 = [np.ascontiguousarray(s.x0, dtype=np.float64) for s in scenes]
+    x0p = (C.POINTER(C.c_double) * len(x0))(*[abi.dptr(x) for x in x0])
+    xs = [np.zeros_like(x) for x in x0]
+    xp = (C.POINTER(C.c_double) * len(xs))(*[abi.dptr(x) for x in xs])
+    reps = (abi.Report * len(xs))()
+    for _ in range(2):   # a batch can be submitted again
+        assert L.gba_batch_submit(h, x0p) == abi.GBA_OK
+        for _ in range(200000):
+            st = L.gba_batch_poll(h, xp, reps)
+            if st != abi.GBA_ERR_BUSY:
+                break
+        assert st == abi.GBA_OK
+        ref_x, ref_r = gba.solve_batch(scenes, opt)
+        for q in range(len(scenes)):
+            np.testing.assert_array_equal(xs[q], ref_x[q])
+            assert reps[q].final_cost == ref_r[q].final_cost
+    assert L.gba_batch_destroy(h) == abi.GBA_OK

@@ -262,6 +262,17 @@ void count_launches(long long n);
 // key order (T precision), vector function (FP64).
 int launch_vector_function(const DevPlan& d, double* y_sorted, cudaStream_t s);
 int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, double* jc, cudaStream_t s);
+// The key pairs of a one-problem plan on the device: each point's pairs with
+// their block id (bid [Ie * Ie], point-major offsets pp_off [P + 1]), sorted
+// stably by block id; *out points at the sorted pairs (one of the two value
+// buffers).  d_hist / d_sums are sized by pairs_sort_scratch, which returns 0
+// when n is beyond the sort's single-CTA scan of chunk totals.  Returns the
+// number of launches.
+int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, const int* d_key_img,
+                          const long long* d_pp_off, const int* d_bid, long long n, int* d_keys0,
+                          int2* d_vals0, int* d_keys1, int2* d_vals1, int* d_hist, int* d_sums,
+                          int* d_bad, int2** out, cudaStream_t s);
+int pairs_sort_scratch(long long n, long long* hist_ints, int* scan_chunks);
 // The observed keys split into double-float pairs (mixed path) on the device.
 int launch_split_keys(const DevPlan& d, float2* out, cudaStream_t s);
 // Every problem's current x (x0 before a run) into out [3P + 6I + 10 Ctot (free cameras)].

@@ -3173,4 +3173,219 @@ int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, double* jc, cu
   return 1;
 }
 
+// ===========================================================================
+// Key pairs of the Schur complement built on the device (one-problem plans):
+// every point writes its pairs (a <= c over its keys, point-major) with the
+// block id of (image a, image c), then a stable LSD radix sort by block id
+// leaves each block's pairs in point order -- the same list, in the same
+// order, as the host build's placement.
+// ===========================================================================
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortPerThread = 8;
+constexpr int kSortTile = kSortThreads * kSortPerThread;   // elements per tile
+constexpr int kScanChunk = 4096;                             // per scan CTA (1024 x 4)
+
+__global__ void __launch_bounds__(128) k_enumerate_pairs(int P, int Ie, const int* __restrict__ pt_key_off,
+                                                         const int* __restrict__ key_img,
+                                                         const long long* __restrict__ pp_off,
+                                                         const int* __restrict__ bid, int* __restrict__ keys,
+                                                         int2* __restrict__ vals) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  const int k0 = pt_key_off[i], k1 = pt_key_off[i + 1];
+  long long pos = pp_off[i];
+  for (int a = k0; a < k1; ++a) {
+    const long long row = (long long)key_img[a] * Ie;
+    for (int c = a; c < k1; ++c, ++pos) {
+      keys[pos] = bid[row + key_img[c]];
+      // a pair of a diagonal block is a key with itself: carry its point instead
+      vals[pos] = make_int2(a, a == c ? i : c);
+    }
+  }
+}
+
+// Per tile, the count of each 8-bit digit of the keys (digit-major output).
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const int* __restrict__ keys, long long n, int shift,
+                                                               int ntiles, int* __restrict__ hist) {
+  __shared__ int h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long t0 = (long long)blockIdx.x * kSortTile;
+#pragma unroll
+  for (int j = 0; j < kSortPerThread; ++j) {
+    const long long e = t0 + (long long)j * kSortThreads + threadIdx.x;
+    if (e < n) atomicAdd(&h[(keys[e] >> shift) & 255], 1);
+  }
+  __syncthreads();
+  hist[(long long)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of v [n] in chunks of kScanChunk: each CTA scans its chunk
+// and writes the chunk total to sums.
+__global__ void __launch_bounds__(1024) k_scan_chunks(int* __restrict__ v, long long n, int* __restrict__ sums) {
+  __shared__ int wsum[32];
+  const long long base = (long long)blockIdx.x * kScanChunk + 4LL * threadIdx.x;
+  int x[4], t = 0;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    x[u] = base + u < n ? v[base + u] : 0;
+    t += x[u];
+  }
+  // inclusive scan of the thread totals across the CTA
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    int ws = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += y;
+    }
+    wsum[lane] = ws;   // inclusive over warps
+  }
+  __syncthreads();
+  int run = inc - t + (w > 0 ? wsum[w - 1] : 0);   // exclusive prefix of this thread
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    if (base + u < n) v[base + u] = run;
+    run += x[u];
+  }
+  if (threadIdx.x == 1023) sums[blockIdx.x] = run;
+}
+
+// Exclusive scan of the chunk totals (at most 8192) in one CTA.
+__global__ void __launch_bounds__(1024) k_scan_totals(int* __restrict__ sums, int m) {
+  __shared__ int part[1024];
+  const int per = (m + 1023) / 1024;
+  const int b = threadIdx.x * per;
+  int t = 0;
+  for (int u = 0; u < per; ++u)
+    if (b + u < m) t += sums[b + u];
+  part[threadIdx.x] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {   // 1024 values: serial in one thread, fixed order
+    int run = 0;
+    for (int u = 0; u < 1024; ++u) {
+      const int y = part[u];
+      part[u] = run;
+      run += y;
+    }
+  }
+  __syncthreads();
+  int run = part[threadIdx.x];
+  for (int u = 0; u < per; ++u)
+    if (b + u < m) {
+      const int y = sums[b + u];
+      sums[b + u] = run;
+      run += y;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_add(int* __restrict__ v, long long n, const int* __restrict__ sums) {
+  const long long base = (long long)blockIdx.x * kScanChunk + 4LL * threadIdx.x;
+  const int add = sums[blockIdx.x];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    if (base + u < n) v[base + u] += add;
+}
+
+// Stable scatter of one tile by the digit at `shift`: elements are ranked in
+// tile order (256 at a time, warp by warp, lane by lane).  A position outside
+// [0, n) is not written and raises *bad.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const int* __restrict__ keys,
+                                                                  const int2* __restrict__ vals, long long n,
+                                                                  int shift, int ntiles,
+                                                                  const int* __restrict__ offs,
+                                                                  int* __restrict__ okeys,
+                                                                  int2* __restrict__ ovals, int* bad) {
+  __shared__ int base[256], run[256], wc[kSortThreads / 32][256];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  base[t] = offs[(long long)t * ntiles + blockIdx.x];
+  run[t] = 0;
+  const long long t0 = (long long)blockIdx.x * kSortTile;
+  for (int j = 0; j < kSortPerThread; ++j) {
+#pragma unroll
+    for (int ww = 0; ww < kSortThreads / 32; ++ww) wc[ww][t] = 0;
+    __syncthreads();
+    const long long e = t0 + (long long)j * kSortThreads + t;
+    const bool valid = e < n;
+    const int key = valid ? keys[e] : 0;
+    const int dgt = valid ? (key >> shift) & 255 : 256;
+    const unsigned peers = __match_any_sync(0xffffffffu, dgt);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank == 0) wc[w][dgt] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      int pos = base[dgt] + run[dgt] + rank;
+      for (int ww = 0; ww < w; ++ww) pos += wc[ww][dgt];
+      if (pos >= 0 && (long long)pos < n) {
+        okeys[pos] = key;
+        ovals[pos] = vals[e];
+      } else {
+        atomicExch(bad, 1);
+      }
+    }
+    __syncthreads();
+    int add = 0;
+#pragma unroll
+    for (int ww = 0; ww < kSortThreads / 32; ++ww) add += wc[ww][t];
+    run[t] += add;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, const int* d_key_img,
+                          const long long* d_pp_off, const int* d_bid, long long n, int* d_keys0,
+                          int2* d_vals0, int* d_keys1, int2* d_vals1, int* d_hist, int* d_sums,
+                          int* d_bad, int2** out, cudaStream_t s) {
+  int launches = 0;
+  if (P > 0) {
+    k_enumerate_pairs<<<unsigned((P + 127) / 128), 128, 0, s>>>(P, Ie, d_pt_key_off, d_key_img, d_pp_off,
+                                                                  d_bid, d_keys0, d_vals0);
+    ++launches;
+  }
+  int bits = 1;
+  while (bits < 31 && (1LL << bits) < nblocks) ++bits;
+  const int passes = (bits + 7) / 8;
+  const int ntiles = int((n + kSortTile - 1) / kSortTile);
+  const long long L = 256LL * ntiles;
+  const int nchunks = int((L + kScanChunk - 1) / kScanChunk);
+  int* kin = d_keys0;
+  int2* vin = d_vals0;
+  int* kout = d_keys1;
+  int2* vout = d_vals1;
+  for (int pass = 0; pass < passes && n > 0; ++pass) {
+    const int shift = 8 * pass;
+    k_radix_hist<<<unsigned(ntiles), kSortThreads, 0, s>>>(kin, n, shift, ntiles, d_hist);
+    k_scan_chunks<<<unsigned(nchunks), 1024, 0, s>>>(d_hist, L, d_sums);
+    k_scan_totals<<<1, 1024, 0, s>>>(d_sums, nchunks);
+    k_scan_add<<<unsigned(nchunks), 1024, 0, s>>>(d_hist, L, d_sums);
+    k_radix_scatter<<<unsigned(ntiles), kSortThreads, 0, s>>>(kin, vin, n, shift, ntiles, d_hist, kout, vout,
+                                                              d_bad);
+    launches += 5;
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  *out = vin;
+  return launches;
+}
+
+int pairs_sort_scratch(long long n, long long* hist_ints, int* scan_chunks) {
+  const long long ntiles = (n + kSortTile - 1) / kSortTile;
+  *hist_ints = 256LL * std::max<long long>(ntiles, 1);
+  *scan_chunks = int((*hist_ints + kScanChunk - 1) / kScanChunk);
+  return *scan_chunks <= 8192 ? 1 : 0;
+}
+
 }  // namespace gba

@@ -535,7 +535,12 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     std::vector<int> rec_ext;          // local reduced-system image of each camera record
     std::vector<int> prior_pt;         // point priors: global point, observed y, information
     std::vector<double> prior_y, prior_info;
+    bool pairs_on_device = false;      // the pair list is built by the device (below)
+    std::vector<int> bid;              // the dense block map kept for it (PCG plans)
   };
+  // one-problem plans without free cameras place their key pairs on the
+  // device (GBA_HOST_PAIRS=1 keeps the host placement, for comparison)
+  const bool device_pairs = nprob == 1 && !any_free && std::getenv("GBA_HOST_PAIRS") == nullptr;
   std::vector<Piece> pieces(nprob);
   // fine phases of a single problem's build (GBA_BUILD_TIMING)
   auto sub = [&](const char* name) {
@@ -735,47 +740,59 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         out.err = GBA_ERR_INVALID;
         return;
       }
-      // cnt_t[t][e] becomes piece t's first slot in block e
-      for (size_t e = 0; e < nn; ++e) {
-        if (bid[e] < 0) continue;
-        long long o = out.blk_off[bid[e]];
-        for (int t = 0; t < nth; ++t) {
-          const int c_ = cnt_t[t][e];
-          cnt_t[t][e] = int(o);
-          o += c_;
-        }
+      long long hist_ints = 0;
+      int scan_chunks = 0;
+      if (device_pairs && !fc && pairs_sort_scratch(acc, &hist_ints, &scan_chunks)) {
+        out.pairs_on_device = true;   // the device enumerates and sorts (device allocations)
+        if (pcg)
+          out.bid.swap(bid);
+        else
+          out.blk_map.swap(bid);
+        sub("  pair counts");
       }
-    sub("  pair counts");
-      out.pairs.resize(acc);
-      host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
-        int* slot = cnt_t[t].data();
-        std::vector<int2> rec;
-        for (int64_t i = i0; i < i1; ++i) {
-          if (!fc) {
-            const int b0 = cnt[i], b1 = cnt[i + 1];
-            for (int a = b0; a < b1; ++a) {
-              const size_t row = (size_t)(key_img[kb + a] - int(ib)) * Ie;
-              for (int c = a; c < b1; ++c)
-                out.pairs[slot[row + key_img[kb + c] - int(ib)]++] =
-                    make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
-            }
-            continue;
-          }
-          point_records(i, rec);
-          const int nr = int(rec.size());
-          for (int a = 0; a < nr; ++a) {
-            const size_t row = (size_t)rec[a].x * Ie;
-            for (int c = a; c < nr; ++c) {
-              // a pair of a diagonal block is a record with itself: carry its point instead
-              out.pairs[slot[row + rec[c].x]++] =
-                  make_int2(rec[a].y, a == c ? int(pb + i) : rec[c].y);
-            }
+      if (!out.pairs_on_device) {
+        // cnt_t[t][e] becomes piece t's first slot in block e
+        for (size_t e = 0; e < nn; ++e) {
+          if (bid[e] < 0) continue;
+          long long o = out.blk_off[bid[e]];
+          for (int t = 0; t < nth; ++t) {
+            const int c_ = cnt_t[t][e];
+            cnt_t[t][e] = int(o);
+            o += c_;
           }
         }
-      }, &cuts);
-    sub("  pairs placed");
+        sub("  pair counts");
+        out.pairs.resize(acc);
+        host_parallel(np, nth, [&](int64_t i0, int64_t i1, int t) {
+          int* slot = cnt_t[t].data();
+          std::vector<int2> rec;
+          for (int64_t i = i0; i < i1; ++i) {
+            if (!fc) {
+              const int b0 = cnt[i], b1 = cnt[i + 1];
+              for (int a = b0; a < b1; ++a) {
+                const size_t row = (size_t)(key_img[kb + a] - int(ib)) * Ie;
+                for (int c = a; c < b1; ++c)
+                  out.pairs[slot[row + key_img[kb + c] - int(ib)]++] =
+                      make_int2(int(kb + a), a == c ? int(pb + i) : int(kb + c));
+              }
+              continue;
+            }
+            point_records(i, rec);
+            const int nr = int(rec.size());
+            for (int a = 0; a < nr; ++a) {
+              const size_t row = (size_t)rec[a].x * Ie;
+              for (int c = a; c < nr; ++c) {
+                // a pair of a diagonal block is a record with itself: carry its point instead
+                out.pairs[slot[row + rec[c].x]++] =
+                    make_int2(rec[a].y, a == c ? int(pb + i) : rec[c].y);
+              }
+            }
+          }
+        }, &cuts);
+        sub("  pairs placed");
+      }
       // dense map for the assembly of the lower triangle: map[j*Ie + i], j <= i
-      if (!pcg) out.blk_map.swap(bid);
+      if (!pcg && !out.pairs_on_device) out.blk_map.swap(bid);
     }
     // soft constraints in y order (camera_shared_vector_function.hpp:483-629):
     // the rows after the keys, each a copy of one parameter with its own
@@ -855,7 +872,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     const long long np = p.number_of_points, ni = p.number_of_images, nk = p.number_of_keys;
     Bases b = base[q];
     b.img_items += (long long)pc.img_items.size();
-    b.pairs += (long long)pc.pairs.size();
+    b.pairs += pc.blk_off.empty() ? 0 : pc.blk_off.back();   // on the host or (below) the device
     b.recs += (long long)pc.rec_ext.size();
     const long long nblk = (long long)pc.blk_ij.size();
     b.blocks += nblk;
@@ -1204,13 +1221,46 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       }
     }
   }
-  D.pairs = d_pairs ? d_pairs : arena.upload(pairs);
+  D.blk_map = arena.upload(blk_map);
+  int dev_pair_bad = 0;
+  int* d_pair_bad = nullptr;
+  if (nprob == 1 && pieces[0].pairs_on_device) {
+    // enumerate every point's pairs with their block ids and sort them by
+    // block (stable) on the device: the host's placement, without its
+    // scattered writes and the copy of the list
+    std::vector<long long> pp_off(size_t(P) + 1, 0);
+    for (int64_t i = 0; i < P; ++i) {
+      const long long k = pt_key_off[i + 1] - pt_key_off[i];
+      pp_off[i + 1] = pp_off[i] + k * (k + 1) / 2;
+    }
+    const long long n = tot.pairs;
+    if (pp_off[P] != n) return GBA_ERR;   // the counts disagree: never expected
+    long long hist_ints = 0;
+    int scan_chunks = 0;
+    pairs_sort_scratch(n, &hist_ints, &scan_chunks);
+    const int* d_bid = pcg ? arena.upload(pieces[0].bid) : D.blk_map;
+    int* k0 = arena.alloc<int>(size_t(n));
+    int* k1 = arena.alloc<int>(size_t(n));
+    int2* v0 = arena.alloc<int2>(size_t(n));
+    int2* v1 = arena.alloc<int2>(size_t(n));
+    int* hist = arena.alloc<int>(size_t(hist_ints));
+    int* sums = arena.alloc<int>(size_t(scan_chunks));
+    d_pair_bad = arena.alloc<int>(1);
+    GBA_CUDA(cudaMemsetAsync(d_pair_bad, 0, sizeof(int), stream));
+    int2* sorted = nullptr;
+    count_launches(build_pairs_on_device(int(P), prob[0].num_ext, int(blk_ij.size()), D.pt_key_off,
+                                         D.key_img, arena.upload(pp_off), d_bid, n, k0, v0, k1, v1,
+                                         hist, sums, d_pair_bad, &sorted, stream));
+    GBA_CUDA(cudaGetLastError());
+    D.pairs = sorted;
+  } else {
+    D.pairs = d_pairs ? d_pairs : arena.upload(pairs);
+  }
   D.items = arena.upload(items);
   D.blk_ij = arena.upload(blk_ij);
   D.blk_item_off = arena.upload(blk_item_off);
   D.n_items = int(items.size());
   D.n_blocks = int(blk_ij.size());
-  D.blk_map = arena.upload(blk_map);
   D.blk_map_off = arena.upload(blk_map_off);
   D.item_partial = arena.alloc<double>(size_t(kItemStride) * std::max<size_t>(items.size(), 1));
   D.n_key_chunks = int(key_chunks.size());
@@ -1273,6 +1323,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   GBA_CUDA(cudaMemsetAsync(D.state, 0, sizeof(LMState) * nprob, stream));
   phase("uploads issued");
   GBA_CUDA(cudaStreamSynchronize(stream));
+  if (d_pair_bad) {   // a sorted position outside the list: never expected
+    GBA_CUDA(cudaMemcpy(&dev_pair_bad, d_pair_bad, sizeof(int), cudaMemcpyDeviceToHost));
+    if (dev_pair_bad) return GBA_ERR;
+  }
   phase("uploads done");
   setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (timing) {

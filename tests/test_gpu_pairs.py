@@ -1,0 +1,71 @@
+"""The device's pair placement (enumeration + stable radix sort by block)
+against the host's: a single-problem plan builds its key-pair list on the
+device unless GBA_HOST_PAIRS is set, and both lists must give the same
+solve, bit for bit -- one radix pass (fewer than 256 blocks), two and three
+passes (more than 65,536 blocks), the dense and the PCG solver, FP64 and
+mixed, single-key points and keyless images."""
+import numpy as np
+import pytest
+
+from hs_sfm_gb300 import abi, synthetic
+
+pytestmark = pytest.mark.gpu
+
+OPT = dict(max_iterations=4, eps1=0.0, eps2=0.0)
+
+
+@pytest.fixture(scope="module")
+def gba():
+    from hs_sfm_gb300 import gba as g
+    g.lib()
+    return g
+
+
+def both(gba, monkeypatch, scene, opt):
+    monkeypatch.delenv("GBA_HOST_PAIRS", raising=False)
+    x_dev, r_dev = gba.solve(scene, opt)
+    monkeypatch.setenv("GBA_HOST_PAIRS", "1")
+    x_host, r_host = gba.solve(scene, opt)
+    monkeypatch.delenv("GBA_HOST_PAIRS", raising=False)
+    assert r_dev.status == abi.GBA_OK and r_host.status == abi.GBA_OK
+    np.testing.assert_array_equal(x_dev, x_host)
+    assert r_dev.final_cost == r_host.final_cost
+    assert r_dev.iterations == r_host.iterations
+    return r_dev
+
+
+@pytest.mark.parametrize("prec", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_one_pass_dense(gba, monkeypatch, prec):
+    s = synthetic.ring_scene(num_images=12, num_points=2000, obs_per_point=5, seed=21)
+    r = both(gba, monkeypatch, s, abi.make_options(precision=prec, **OPT))
+    assert r.final_cost < r.initial_cost
+
+
+@pytest.mark.parametrize("solver", [abi.LINEAR_DENSE_CHOLESKY, abi.LINEAR_PCG])
+def test_two_passes_grid(gba, monkeypatch, solver):
+    s = synthetic.grid_scene(num_images=120, num_points=20_000, seed=22)
+    both(gba, monkeypatch, s, abi.make_options(precision=abi.PRECISION_MIXED,
+                                                 linear_solver=solver, **OPT))
+
+
+def test_three_passes_walk(gba, monkeypatch):
+    # long tracks over 2,000 images: about 60 neighbours per image, more than
+    # 65,536 blocks, so the block ids need three 8-bit digits
+    s = synthetic.walk_scene(num_images=2000, num_points=60_000, mean_obs=20.0, seed=23)
+    both(gba, monkeypatch, s, abi.make_options(precision=abi.PRECISION_MIXED,
+                                                 linear_solver=abi.LINEAR_PCG,
+                                                 max_iterations=2, eps1=0.0, eps2=0.0))
+
+
+def test_single_key_points_and_keyless_images(gba, monkeypatch):
+    s = synthetic.ring_scene(num_images=9, num_points=600, obs_per_point=3, seed=24)
+    fm = s.feature_maps
+    keep = fm[:, 0] != 4
+    first = np.r_[True, fm[1:, 1] != fm[:-1, 1]]
+    keep &= ~np.isin(fm[:, 1], np.arange(0, 600, 5)) | first
+    t = synthetic.Scene(**{**s.__dict__})
+    t.feature_maps = fm[keep]
+    K = s.number_of_keys
+    y = s.near_y[:2 * K].reshape(-1, 2)[keep].reshape(-1)
+    t.near_y = np.concatenate([y, s.near_y[2 * K:]])
+    both(gba, monkeypatch, t, abi.make_options(**OPT))

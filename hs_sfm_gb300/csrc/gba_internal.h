@@ -273,6 +273,17 @@ int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, c
                           int2* d_vals0, int* d_keys1, int2* d_vals1, int* d_hist, int* d_sums,
                           int* d_bad, int2** out, cudaStream_t s);
 int pairs_sort_scratch(long long n, long long* hist_ints, int* scan_chunks);
+// The longest array the device's exclusive scan takes (8,192 chunks of 4,096).
+constexpr long long kDeviceScanMax = 8192LL * 4096;
+// Pairs per image pair of a one-problem plan, on the device: counts by
+// atomics, block ids (bid [Ie * Ie], -1 where no block; every diagonal
+// present) and the block list in (i, j) order: blk_code = i * Ie + j,
+// blk_first = its first pair; info = (blocks, pairs).  Scratch: cnt, off
+// [Ie * Ie], sums [Ie * Ie / 4096 + 1]; blk_code / blk_first hold
+// Ie * (Ie + 1) / 2.  Returns the launch count, -1 if Ie * Ie is too long.
+int count_blocks_on_device(int P, int Ie, const int* d_pt_key_off, const int* d_key_img, int* d_cnt, int* d_bid,
+                           int* d_off, int* d_sums, int* d_blk_code, int* d_blk_first, int* d_info,
+                           cudaStream_t s);
 // The observed keys split into double-float pairs (mixed path) on the device.
 int launch_split_keys(const DevPlan& d, float2* out, cudaStream_t s);
 // Every problem's current x (x0 before a run) into out [3P + 6I + 10 Ctot (free cameras)].

@@ -1249,8 +1249,13 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
   const int lane = threadIdx.x & 31;
   if (wid >= n_items) return;
   const int4 it = __ldg(d.items + wid);
-  if (!d.state[it.w].active) return;
+  // the problem's state, the block and the first pair are independent
+  // loads: all three are issued before the first of them is used
+  const int active = d.state[it.w].active;
   const int2 ij = __ldg(d.blk_ij + it.x);
+  int q = it.y + lane;
+  int2 pr = q < it.z ? __ldg(d.pairs + q) : make_int2(0, 0);
+  if (!active) return;
   const bool diag = ij.x == ij.y;
   const T* __restrict__ Z = tptr<T>(d.Z);
   const T* __restrict__ PS = tptr<T>(d.PS);
@@ -1261,8 +1266,6 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
   for (int e = 0; e < 6; ++e) racc[e] = T(0);
   // the next pair's key indices are fetched one iteration ahead, so each
   // iteration waits on a single round trip (the Z records)
-  int q = it.y + lane;
-  int2 pr = q < it.z ? __ldg(d.pairs + q) : make_int2(0, 0);
   for (; q < it.z; q += 32) {
     const int qn = q + 32;
     const int2 prn = qn < it.z ? __ldg(d.pairs + qn) : pr;
@@ -3343,6 +3346,69 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const int* __res
   }
 }
 
+// Pairs per image pair (a, c), a <= c: one thread per point, one atomic per
+// key pair (keys of a point are in image order).
+__global__ void __launch_bounds__(128) k_count_pairs(int P, int Ie, const int* __restrict__ pt_key_off,
+                                                     const int* __restrict__ key_img, int* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  const int k0 = pt_key_off[i], k1 = pt_key_off[i + 1];
+  for (int a = k0; a < k1; ++a) {
+    int* row = cnt + (long long)key_img[a] * Ie;
+    for (int c = a; c < k1; ++c) atomicAdd(row + key_img[c], 1);
+  }
+}
+
+// A block for every image pair a < c with pairs and for every diagonal
+// (a == c, even without keys): mark[e] = 1, e = a * Ie + c; off[e] = the
+// pair count, scanned next into the block's first pair.
+__device__ __forceinline__ bool block_present(long long e, int Ie, int count) {
+  const int a = int(e / Ie), c = int(e % Ie);
+  return a == c || (c > a && count > 0);
+}
+
+__global__ void __launch_bounds__(256) k_block_marks(long long L, int Ie, const int* __restrict__ cnt,
+                                                     int* __restrict__ mark, int* __restrict__ off) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= L) return;
+  const int v = cnt[e];
+  mark[e] = block_present(e, Ie, v) ? 1 : 0;
+  off[e] = v;
+}
+
+// After the scans: bid[e] = the block id (or -1), the block list (code,
+// first pair) in block order, and info = (blocks, pairs) from the last
+// entry (the diagonal block (Ie-1, Ie-1), always present).
+__global__ void __launch_bounds__(256) k_block_lists(long long L, int Ie, const int* __restrict__ cnt,
+                                                     int* __restrict__ bid, const int* __restrict__ off,
+                                                     int* __restrict__ blk_code, int* __restrict__ blk_first,
+                                                     int* __restrict__ info) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= L) return;
+  const int v = cnt[e];
+  const bool m = block_present(e, Ie, v);
+  const int b = bid[e];
+  if (m) {
+    blk_code[b] = int(e);
+    blk_first[b] = off[e];
+  }
+  bid[e] = m ? b : -1;
+  if (e == L - 1) {
+    info[0] = b + 1;
+    info[1] = off[e] + v;
+  }
+}
+
+// Exclusive scan of v [L] (L <= kDeviceScanMax) in place; sums: the chunk totals.
+int scan_exclusive(int* v, long long L, int* sums, cudaStream_t s) {
+  if (L <= 0) return 0;
+  const int nchunks = int((L + kScanChunk - 1) / kScanChunk);
+  k_scan_chunks<<<unsigned(nchunks), 1024, 0, s>>>(v, L, sums);
+  k_scan_totals<<<1, 1024, 0, s>>>(sums, nchunks);
+  k_scan_add<<<unsigned(nchunks), 1024, 0, s>>>(v, L, sums);
+  return 3;
+}
+
 }  // namespace
 
 int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, const int* d_key_img,
@@ -3360,7 +3426,6 @@ int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, c
   const int passes = (bits + 7) / 8;
   const int ntiles = int((n + kSortTile - 1) / kSortTile);
   const long long L = 256LL * ntiles;
-  const int nchunks = int((L + kScanChunk - 1) / kScanChunk);
   int* kin = d_keys0;
   int2* vin = d_vals0;
   int* kout = d_keys1;
@@ -3368,9 +3433,7 @@ int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, c
   for (int pass = 0; pass < passes && n > 0; ++pass) {
     const int shift = 8 * pass;
     k_radix_hist<<<unsigned(ntiles), kSortThreads, 0, s>>>(kin, n, shift, ntiles, d_hist);
-    k_scan_chunks<<<unsigned(nchunks), 1024, 0, s>>>(d_hist, L, d_sums);
-    k_scan_totals<<<1, 1024, 0, s>>>(d_sums, nchunks);
-    k_scan_add<<<unsigned(nchunks), 1024, 0, s>>>(d_hist, L, d_sums);
+    scan_exclusive(d_hist, L, d_sums, s);
     k_radix_scatter<<<unsigned(ntiles), kSortThreads, 0, s>>>(kin, vin, n, shift, ntiles, d_hist, kout, vout,
                                                               d_bad);
     launches += 5;
@@ -3379,6 +3442,24 @@ int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, c
   }
   *out = vin;
   return launches;
+}
+
+int count_blocks_on_device(int P, int Ie, const int* d_pt_key_off, const int* d_key_img, int* d_cnt, int* d_bid,
+                           int* d_off, int* d_sums, int* d_blk_code, int* d_blk_first, int* d_info,
+                           cudaStream_t s) {
+  const long long L = (long long)Ie * Ie;
+  int launches = 0;
+  if (L <= 0 || L > kDeviceScanMax) return -1;
+  if (cudaMemsetAsync(d_cnt, 0, sizeof(int) * size_t(L), s) != cudaSuccess) return -1;
+  if (P > 0) {
+    k_count_pairs<<<unsigned((P + 127) / 128), 128, 0, s>>>(P, Ie, d_pt_key_off, d_key_img, d_cnt);
+    ++launches;
+  }
+  const unsigned g = unsigned((L + 255) / 256);
+  k_block_marks<<<g, 256, 0, s>>>(L, Ie, d_cnt, d_bid, d_off);
+  launches += 1 + scan_exclusive(d_bid, L, d_sums, s) + scan_exclusive(d_off, L, d_sums, s);
+  k_block_lists<<<g, 256, 0, s>>>(L, Ie, d_cnt, d_bid, d_off, d_blk_code, d_blk_first, d_info);
+  return launches + 1;
 }
 
 int pairs_sort_scratch(long long n, long long* hist_ints, int* scan_chunks) {

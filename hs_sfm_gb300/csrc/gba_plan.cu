@@ -537,6 +537,11 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     std::vector<double> prior_y, prior_info;
     bool pairs_on_device = false;      // the pair list is built by the device (below)
     std::vector<int> bid;              // the dense block map kept for it (PCG plans)
+    // blocks counted on the device: its block map and the uploads it used
+    int* d_bid = nullptr;
+    int* d_key_img = nullptr;
+    int* d_pt_key_off = nullptr;
+    std::vector<long long> pp_off;     // [np + 1] first pair of each point, point-major
   };
   // one-problem plans without free cameras place their key pairs on the
   // device (GBA_HOST_PAIRS=1 keeps the host placement, for comparison)
@@ -570,9 +575,37 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     // point-major order: counting sort by point, then image within point
     const int nth0 = nk > 200000 ? inner : 1;
     std::vector<int> cnt, order;
-    counting_sort(nk, np, nth0, [&](int64_t k) { return int(p.feature_maps[2 * k + 1]); }, cnt,
-                  order);
-    {
+    // keys that already come point-major (by point, then image, no repeats --
+    // the usual track layout) need no sort: the order is the identity and
+    // each point's first key is found where the point id steps
+    const int64_t* fm = p.feature_maps;
+    std::vector<char> unsorted(nth0, 0);
+    host_parallel(nk, nth0, [&](int64_t k0, int64_t k1, int t) {
+      for (int64_t k = std::max<int64_t>(k0, 1); k < k1; ++k) {
+        const int64_t dp = fm[2 * k + 1] - fm[2 * k - 1];
+        if (dp < 0 || (dp == 0 && fm[2 * k] <= fm[2 * k - 2])) {
+          unsorted[t] = 1;
+          break;
+        }
+      }
+    });
+    const bool presorted = std::find(unsorted.begin(), unsorted.end(), char(1)) == unsorted.end();
+    if (presorted) {
+      cnt.assign(size_t(np) + 1, nk);
+      order.resize(size_t(nk));
+      host_parallel(nk, nth0, [&](int64_t k0, int64_t k1, int) {
+        for (int64_t k = k0; k < k1; ++k) {
+          order[k] = int(k);
+          // points prev+1 .. this one start at key k (points without keys too)
+          const int64_t prev = k == 0 ? -1 : fm[2 * k - 1];
+          for (int64_t i = prev + 1; i <= fm[2 * k + 1]; ++i) cnt[i] = int(k);
+        }
+      });
+    } else {
+      counting_sort(nk, np, nth0, [&](int64_t k) { return int(p.feature_maps[2 * k + 1]); }, cnt,
+                    order);
+    }
+    if (!presorted) {
       std::vector<char> dup(nth0, 0);
       host_parallel(np, nth0, [&](int64_t i0, int64_t i1, int t) {
         for (int64_t i = i0; i < i1; ++i) {
@@ -685,12 +718,74 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
           rec.push_back(make_int2(out.rec_ext[r], -(r + 1)));
     };
     sub("  records");
+    // One problem with keys only: the device counts the pairs of every image
+    // pair (atomics over the key pairs), numbers the blocks in the order of
+    // the host's count below ((i, j) lexicographic, every diagonal present)
+    // and returns the block list; it places the pairs later, so the block
+    // list, the pair list and the dense block map are the host's.
+    bool dev_counted = false;
+    if (device_pairs && !fc && ni > 0 && (long long)Ie * Ie <= kDeviceScanMax) {
+      out.pp_off.assign(size_t(np) + 1, 0);
+      for (int i = 0; i < np; ++i) {
+        const long long k = cnt[i + 1] - cnt[i];
+        out.pp_off[i + 1] = out.pp_off[i] + k * (k + 1) / 2;
+      }
+      const long long total = out.pp_off[np];
+      if (total > INT32_MAX) {
+        out.err = GBA_ERR_INVALID;
+        return;
+      }
+      long long hist_ints = 0;
+      int scan_chunks = 0;
+      if (pairs_sort_scratch(total, &hist_ints, &scan_chunks)) {
+        const long long L = (long long)Ie * Ie, ub = (long long)Ie * (Ie + 1) / 2;
+        out.d_key_img = arena.upload(key_img);
+        out.d_pt_key_off = arena.upload(pt_key_off);
+        int* d_cnt = arena.alloc<int>(size_t(L));
+        int* d_off = arena.alloc<int>(size_t(L));
+        out.d_bid = arena.alloc<int>(size_t(L));
+        int* d_sums = arena.alloc<int>(size_t(L / 4096 + 1));
+        int* d_code = arena.alloc<int>(size_t(ub));
+        int* d_first = arena.alloc<int>(size_t(ub));
+        int* d_info = arena.alloc<int>(2);
+        const int nl = count_blocks_on_device(np, Ie, out.d_pt_key_off, out.d_key_img, d_cnt, out.d_bid, d_off,
+                                              d_sums, d_code, d_first, d_info, stream);
+        if (nl < 0) {
+          out.err = GBA_ERR;
+          return;
+        }
+        count_launches(nl);
+        GBA_CUDA(cudaGetLastError());
+        int info[2] = {0, 0};
+        GBA_CUDA(cudaMemcpyAsync(info, d_info, sizeof(info), cudaMemcpyDeviceToHost, stream));
+        GBA_CUDA(cudaStreamSynchronize(stream));
+        const int nb = info[0];
+        if (info[1] != total || nb < ni || nb > ub) {   // the counts disagree: never expected
+          out.err = GBA_ERR;
+          return;
+        }
+        std::vector<int> code(nb), first(nb);
+        GBA_CUDA(cudaMemcpyAsync(code.data(), d_code, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream));
+        GBA_CUDA(cudaMemcpyAsync(first.data(), d_first, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream));
+        GBA_CUDA(cudaStreamSynchronize(stream));
+        out.blk_ij.resize(nb);
+        out.blk_off.resize(size_t(nb) + 1);
+        for (int b = 0; b < nb; ++b) {
+          out.blk_ij[b] = make_int2(code[b] / Ie, code[b] % Ie);
+          out.blk_off[b] = first[b];
+        }
+        out.blk_off[nb] = total;
+        out.pairs_on_device = true;
+        dev_counted = true;
+        sub("  pair counts (device)");
+      }
+    }
     // reduced-system blocks: (i <= j) with their record pairs, point order.
     // Pairs are counted and placed by point ranges in parallel: each piece
     // counts its pairs per image pair, a piece's pairs of a block follow
     // those of the pieces before it, so every block lists its pairs in
     // point order whatever the number of pieces.
-    {
+    if (!dev_counted) {
       const size_t nn = (size_t)Ie * Ie;
       int nth = nth0;
       while (nth > 1 && nn * size_t(nth) * sizeof(int) > (size_t(256) << 20)) --nth;
@@ -1042,12 +1137,12 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.prob = arena.upload(prob);
   D.state = arena.alloc<LMState>(nprob);
   D.K = int(K);
-  D.key_img = arena.upload(key_img);
+  D.key_img = nprob == 1 && pieces[0].d_key_img ? pieces[0].d_key_img : arena.upload(key_img);
   D.key_pt = arena.upload(key_pt);
   D.key_obs = arena.upload(key_obs);
   D.key_wl = any_weights ? arena.upload(key_wl) : nullptr;
   D.P = int(P);
-  D.pt_key_off = arena.upload(pt_key_off);
+  D.pt_key_off = nprob == 1 && pieces[0].d_pt_key_off ? pieces[0].d_pt_key_off : arena.upload(pt_key_off);
   D.pt_prob = arena.upload(pt_prob);
   D.I = int(I);
   D.img_key_off = arena.upload(img_key_off);
@@ -1221,24 +1316,29 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       }
     }
   }
-  D.blk_map = arena.upload(blk_map);
+  D.blk_map = nprob == 1 && pieces[0].d_bid && !pcg ? pieces[0].d_bid : arena.upload(blk_map);
   int dev_pair_bad = 0;
   int* d_pair_bad = nullptr;
   if (nprob == 1 && pieces[0].pairs_on_device) {
     // enumerate every point's pairs with their block ids and sort them by
     // block (stable) on the device: the host's placement, without its
     // scattered writes and the copy of the list
-    std::vector<long long> pp_off(size_t(P) + 1, 0);
-    for (int64_t i = 0; i < P; ++i) {
-      const long long k = pt_key_off[i + 1] - pt_key_off[i];
-      pp_off[i + 1] = pp_off[i] + k * (k + 1) / 2;
+    std::vector<long long> pp_off;
+    if (!pieces[0].pp_off.empty()) {
+      pp_off.swap(pieces[0].pp_off);
+    } else {
+      pp_off.assign(size_t(P) + 1, 0);
+      for (int64_t i = 0; i < P; ++i) {
+        const long long k = pt_key_off[i + 1] - pt_key_off[i];
+        pp_off[i + 1] = pp_off[i] + k * (k + 1) / 2;
+      }
     }
     const long long n = tot.pairs;
     if (pp_off[P] != n) return GBA_ERR;   // the counts disagree: never expected
     long long hist_ints = 0;
     int scan_chunks = 0;
     pairs_sort_scratch(n, &hist_ints, &scan_chunks);
-    const int* d_bid = pcg ? arena.upload(pieces[0].bid) : D.blk_map;
+    const int* d_bid = pieces[0].d_bid ? pieces[0].d_bid : pcg ? arena.upload(pieces[0].bid) : D.blk_map;
     int* k0 = arena.alloc<int>(size_t(n));
     int* k1 = arena.alloc<int>(size_t(n));
     int2* v0 = arena.alloc<int2>(size_t(n));

@@ -69,3 +69,22 @@ def test_single_key_points_and_keyless_images(gba, monkeypatch):
     y = s.near_y[:2 * K].reshape(-1, 2)[keep].reshape(-1)
     t.near_y = np.concatenate([y, s.near_y[2 * K:]])
     both(gba, monkeypatch, t, abi.make_options(**OPT))
+
+
+def test_presorted_keys_take_the_same_path(gba):
+    # keys already by point then image skip the host sort; any other order
+    # is sorted into the same layout, so the solves agree bit for bit
+    s = synthetic.grid_scene(num_images=40, num_points=5000, seed=25)
+    fm = s.feature_maps
+    assert np.all(np.diff(fm[:, 1]) >= 0)
+    perm = np.random.default_rng(25).permutation(len(fm))
+    t = synthetic.Scene(**{**s.__dict__})
+    t.feature_maps = fm[perm]
+    K = s.number_of_keys
+    y = s.near_y[:2 * K].reshape(-1, 2)[perm].reshape(-1)
+    t.near_y = np.concatenate([y, s.near_y[2 * K:]])
+    opt = abi.make_options(precision=abi.PRECISION_MIXED, **OPT)
+    x0, r0 = gba.solve(s, opt)
+    x1, r1 = gba.solve(t, opt)
+    np.testing.assert_array_equal(x0, x1)
+    assert r0.final_cost == r1.final_cost

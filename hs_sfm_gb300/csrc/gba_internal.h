@@ -262,28 +262,31 @@ void count_launches(long long n);
 // key order (T precision), vector function (FP64).
 int launch_vector_function(const DevPlan& d, double* y_sorted, cudaStream_t s);
 int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, double* jc, cudaStream_t s);
-// The key pairs of a one-problem plan on the device: each point's pairs with
-// their block id (bid [Ie * Ie], point-major offsets pp_off [P + 1]), sorted
-// stably by block id; *out points at the sorted pairs (one of the two value
-// buffers).  d_hist / d_sums are sized by pairs_sort_scratch, which returns 0
-// when n is beyond the sort's single-CTA scan of chunk totals.  Returns the
-// number of launches.
-int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, const int* d_key_img,
-                          const long long* d_pp_off, const int* d_bid, long long n, int* d_keys0,
-                          int2* d_vals0, int* d_keys1, int2* d_vals1, int* d_hist, int* d_sums,
-                          int* d_bad, int2** out, cudaStream_t s);
-int pairs_sort_scratch(long long n, long long* hist_ints, int* scan_chunks);
-// The longest array the device's exclusive scan takes (8,192 chunks of 4,096).
-constexpr long long kDeviceScanMax = 8192LL * 4096;
-// Pairs per image pair of a one-problem plan, on the device: counts by
-// atomics, block ids (bid [Ie * Ie], -1 where no block; every diagonal
-// present) and the block list in (i, j) order: blk_code = i * Ie + j,
-// blk_first = its first pair; info = (blocks, pairs).  Scratch: cnt, off
-// [Ie * Ie], sums [Ie * Ie / 4096 + 1]; blk_code / blk_first hold
-// Ie * (Ie + 1) / 2.  Returns the launch count, -1 if Ie * Ie is too long.
-int count_blocks_on_device(int P, int Ie, const int* d_pt_key_off, const int* d_key_img, int* d_cnt, int* d_bid,
-                           int* d_off, int* d_sums, int* d_blk_code, int* d_blk_first, int* d_info,
-                           cudaStream_t s);
+// Key pairs of the reduced system on the device (plans without free
+// cameras).  pinfo[q] = (first image, Ie, first code, 0): problem q's image
+// pairs (a, c) have the codes first code + a * Ie + c (L codes in all, the
+// problems' ranges in order).  count_blocks_on_device counts the pairs per
+// code (cnt), numbers the blocks -- the codes with pairs and every
+// diagonal, in code order -- into bid [L] (-1 where no block) and returns
+// the block list (blk_code = a * Ie + c within the problem, blk_first = its
+// first pair; both hold up to the sum of Ie (Ie + 1) / 2), each problem's
+// first block (prob_block) and info = (blocks, pairs); qlast is the last
+// problem with images, max_ie the largest Ie; off [L] is scratch.
+// build_pairs_on_device writes the pairs of every point (pp [P + 1]
+// scratch) with their block ids and sorts them stably by block: *out points
+// at the sorted pairs (one of the two value buffers).  pairs_sort_scratch
+// sizes hist and scratch; scratch for count_blocks_on_device holds
+// scan_scratch_ints(L).  Both return the launch count (-1: bad arguments).
+long long scan_scratch_ints(long long L);
+int count_blocks_on_device(int nprob, int qlast, int max_ie, int P, const int4* d_pinfo, const int* d_pt_key_off,
+                           const int* d_key_img, const int* d_pt_prob, long long L, int* d_cnt, int* d_bid,
+                           int* d_off, int* d_scratch, int* d_blk_code, int* d_blk_first, int* d_prob_block,
+                           int* d_info, cudaStream_t s);
+int build_pairs_on_device(int P, int nblocks, const int4* d_pinfo, const int* d_pt_key_off, const int* d_key_img,
+                          const int* d_pt_prob, int* d_pp, const int* d_bid, long long n, int* d_keys0,
+                          int2* d_vals0, int* d_keys1, int2* d_vals1, int* d_hist, int* d_scratch, int* d_bad,
+                          int2** out, cudaStream_t s);
+void pairs_sort_scratch(long long n, int P, long long* hist_ints, long long* scratch_ints);
 // The observed keys split into double-float pairs (mixed path) on the device.
 int launch_split_keys(const DevPlan& d, float2* out, cudaStream_t s);
 // Every problem's current x (x0 before a run) into out [3P + 6I + 10 Ctot (free cameras)].

@@ -3177,11 +3177,17 @@ int launch_jacobian_out(const DevPlan& d, double* jp, double* ji, double* jc, cu
 }
 
 // ===========================================================================
-// Key pairs of the Schur complement built on the device (one-problem plans):
-// every point writes its pairs (a <= c over its keys, point-major) with the
-// block id of (image a, image c), then a stable LSD radix sort by block id
-// leaves each block's pairs in point order -- the same list, in the same
-// order, as the host build's placement.
+// Key pairs of the Schur complement built on the device (plans without free
+// cameras).  Problem q's image pairs (a, c), a <= c local images, have the
+// codes first_code(q) + a * Ie + c; the problems' code ranges follow each
+// other, so code order is the host's block order of the concatenated plan.
+// The device counts the pairs of every code (atomics), marks the blocks
+// (codes with pairs, and every diagonal), numbers them and their first pairs
+// by exclusive scans, and returns the block list.  Every point then writes
+// its pairs (a <= c over its keys, point-major) with their block id, and a
+// stable LSD radix sort by block id leaves each block's pairs in point order
+// -- the same list, in the same order, as the host build's placement.
+// Problem records pinfo[q] = (first image, Ie, first code, 0).
 // ===========================================================================
 namespace {
 
@@ -3189,20 +3195,102 @@ constexpr int kSortThreads = 256;
 constexpr int kSortPerThread = 8;
 constexpr int kSortTile = kSortThreads * kSortPerThread;   // elements per tile
 constexpr int kScanChunk = 4096;                             // per scan CTA (1024 x 4)
+constexpr int kScanTop = 8192;                               // chunk totals one CTA scans
 
-__global__ void __launch_bounds__(128) k_enumerate_pairs(int P, int Ie, const int* __restrict__ pt_key_off,
+// Pairs per code: one thread per point, one atomic per key pair (keys of a
+// point are in image order).
+__global__ void __launch_bounds__(128) k_count_pairs(int P, const int* __restrict__ pt_key_off,
+                                                     const int* __restrict__ key_img,
+                                                     const int* __restrict__ pt_prob,
+                                                     const int4* __restrict__ pinfo, int* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  const int4 pq = pinfo[pt_prob[i]];
+  const int k0 = pt_key_off[i], k1 = pt_key_off[i + 1];
+  for (int a = k0; a < k1; ++a) {
+    const long long row = pq.z + (long long)(key_img[a] - pq.x) * pq.y;
+    for (int c = a; c < k1; ++c) atomicAdd(cnt + row + (key_img[c] - pq.x), 1);
+  }
+}
+
+// Pairs of each point, k (k + 1) / 2; entry P is 0 (the scan makes it the total).
+__global__ void __launch_bounds__(256) k_point_pairs(int P, const int* __restrict__ pt_key_off,
+                                                     int* __restrict__ pp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > P) return;
+  int v = 0;
+  if (i < P) {
+    const int k = pt_key_off[i + 1] - pt_key_off[i];
+    v = k * (k + 1) / 2;
+  }
+  pp[i] = v;
+}
+
+// A block for every image pair a < c with pairs and for every diagonal
+// (a == c, even without keys).
+__device__ __forceinline__ bool block_present(int local, int Ie, int count) {
+  const int a = local / Ie, c = local - a * Ie;
+  return a == c || (c > a && count > 0);
+}
+
+// grid (codes of the largest problem / 256, problems)
+__global__ void __launch_bounds__(256) k_block_marks(const int4* __restrict__ pinfo, const int* __restrict__ cnt,
+                                                     int* __restrict__ mark, int* __restrict__ off) {
+  const int4 pq = pinfo[blockIdx.y];
+  const int local = blockIdx.x * blockDim.x + threadIdx.x;
+  if (local >= pq.y * pq.y) return;
+  const int e = pq.z + local;
+  const int v = cnt[e];
+  mark[e] = block_present(local, pq.y, v) ? 1 : 0;
+  off[e] = v;
+}
+
+// After the scans: bid[e] = the block id (or -1); the block list (local
+// code, first pair) in block order; each problem's first block (its block
+// (0, 0) is always present); info = (blocks, pairs) from the last code of
+// problem qlast (the last with images: its block (Ie-1, Ie-1)).
+__global__ void __launch_bounds__(256) k_block_lists(const int4* __restrict__ pinfo, int qlast,
+                                                     const int* __restrict__ cnt, int* __restrict__ bid,
+                                                     const int* __restrict__ off, int* __restrict__ blk_code,
+                                                     int* __restrict__ blk_first, int* __restrict__ prob_block,
+                                                     int* __restrict__ info) {
+  const int q = blockIdx.y;
+  const int4 pq = pinfo[q];
+  const int local = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = pq.y * pq.y;
+  if (local >= L) return;
+  const int e = pq.z + local;
+  const int v = cnt[e];
+  const bool m = block_present(local, pq.y, v);
+  const int b = bid[e];
+  if (m) {
+    blk_code[b] = local;
+    blk_first[b] = off[e];
+  }
+  bid[e] = m ? b : -1;
+  if (local == 0) prob_block[q] = b;
+  if (q == qlast && local == L - 1) {
+    info[0] = b + 1;
+    info[1] = off[e] + v;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_enumerate_pairs(int P, const int* __restrict__ pt_key_off,
                                                          const int* __restrict__ key_img,
-                                                         const long long* __restrict__ pp_off,
+                                                         const int* __restrict__ pt_prob,
+                                                         const int4* __restrict__ pinfo,
+                                                         const int* __restrict__ pp_off,
                                                          const int* __restrict__ bid, int* __restrict__ keys,
                                                          int2* __restrict__ vals) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
+  const int4 pq = pinfo[pt_prob[i]];
   const int k0 = pt_key_off[i], k1 = pt_key_off[i + 1];
-  long long pos = pp_off[i];
+  int pos = pp_off[i];
   for (int a = k0; a < k1; ++a) {
-    const long long row = (long long)key_img[a] * Ie;
+    const long long row = pq.z + (long long)(key_img[a] - pq.x) * pq.y;
     for (int c = a; c < k1; ++c, ++pos) {
-      keys[pos] = bid[row + key_img[c]];
+      keys[pos] = bid[row + (key_img[c] - pq.x)];
       // a pair of a diagonal block is a key with itself: carry its point instead
       vals[pos] = make_int2(a, a == c ? i : c);
     }
@@ -3346,79 +3434,66 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const int* __res
   }
 }
 
-// Pairs per image pair (a, c), a <= c: one thread per point, one atomic per
-// key pair (keys of a point are in image order).
-__global__ void __launch_bounds__(128) k_count_pairs(int P, int Ie, const int* __restrict__ pt_key_off,
-                                                     const int* __restrict__ key_img, int* __restrict__ cnt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P) return;
-  const int k0 = pt_key_off[i], k1 = pt_key_off[i + 1];
-  for (int a = k0; a < k1; ++a) {
-    int* row = cnt + (long long)key_img[a] * Ie;
-    for (int c = a; c < k1; ++c) atomicAdd(row + key_img[c], 1);
-  }
-}
-
-// A block for every image pair a < c with pairs and for every diagonal
-// (a == c, even without keys): mark[e] = 1, e = a * Ie + c; off[e] = the
-// pair count, scanned next into the block's first pair.
-__device__ __forceinline__ bool block_present(long long e, int Ie, int count) {
-  const int a = int(e / Ie), c = int(e % Ie);
-  return a == c || (c > a && count > 0);
-}
-
-__global__ void __launch_bounds__(256) k_block_marks(long long L, int Ie, const int* __restrict__ cnt,
-                                                     int* __restrict__ mark, int* __restrict__ off) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= L) return;
-  const int v = cnt[e];
-  mark[e] = block_present(e, Ie, v) ? 1 : 0;
-  off[e] = v;
-}
-
-// After the scans: bid[e] = the block id (or -1), the block list (code,
-// first pair) in block order, and info = (blocks, pairs) from the last
-// entry (the diagonal block (Ie-1, Ie-1), always present).
-__global__ void __launch_bounds__(256) k_block_lists(long long L, int Ie, const int* __restrict__ cnt,
-                                                     int* __restrict__ bid, const int* __restrict__ off,
-                                                     int* __restrict__ blk_code, int* __restrict__ blk_first,
-                                                     int* __restrict__ info) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= L) return;
-  const int v = cnt[e];
-  const bool m = block_present(e, Ie, v);
-  const int b = bid[e];
-  if (m) {
-    blk_code[b] = int(e);
-    blk_first[b] = off[e];
-  }
-  bid[e] = m ? b : -1;
-  if (e == L - 1) {
-    info[0] = b + 1;
-    info[1] = off[e] + v;
-  }
-}
-
-// Exclusive scan of v [L] (L <= kDeviceScanMax) in place; sums: the chunk totals.
-int scan_exclusive(int* v, long long L, int* sums, cudaStream_t s) {
+// Exclusive scan of v [L] in place: chunks of kScanChunk, their totals
+// scanned the same way (one CTA once there are at most kScanTop of them).
+// scratch holds scan_scratch_ints(L) ints.
+int scan_exclusive(int* v, long long L, int* scratch, cudaStream_t s) {
   if (L <= 0) return 0;
-  const int nchunks = int((L + kScanChunk - 1) / kScanChunk);
-  k_scan_chunks<<<unsigned(nchunks), 1024, 0, s>>>(v, L, sums);
-  k_scan_totals<<<1, 1024, 0, s>>>(sums, nchunks);
-  k_scan_add<<<unsigned(nchunks), 1024, 0, s>>>(v, L, sums);
-  return 3;
+  const long long nchunks = (L + kScanChunk - 1) / kScanChunk;
+  k_scan_chunks<<<unsigned(nchunks), 1024, 0, s>>>(v, L, scratch);
+  int n = 1;
+  if (nchunks <= kScanTop) {
+    k_scan_totals<<<1, 1024, 0, s>>>(scratch, int(nchunks));
+    ++n;
+  } else {
+    n += scan_exclusive(scratch, nchunks, scratch + nchunks, s);
+  }
+  k_scan_add<<<unsigned(nchunks), 1024, 0, s>>>(v, L, scratch);
+  return n + 1;
 }
 
 }  // namespace
 
-int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, const int* d_key_img,
-                          const long long* d_pp_off, const int* d_bid, long long n, int* d_keys0,
-                          int2* d_vals0, int* d_keys1, int2* d_vals1, int* d_hist, int* d_sums,
-                          int* d_bad, int2** out, cudaStream_t s) {
+long long scan_scratch_ints(long long L) {
+  long long t = 0;
+  while (L > 0) {
+    const long long c = (L + kScanChunk - 1) / kScanChunk;
+    t += c;
+    if (c <= kScanTop) break;
+    L = c;
+  }
+  return std::max<long long>(t, 1);
+}
+
+int count_blocks_on_device(int nprob, int qlast, int max_ie, int P, const int4* d_pinfo, const int* d_pt_key_off,
+                           const int* d_key_img, const int* d_pt_prob, long long L, int* d_cnt, int* d_bid,
+                           int* d_off, int* d_scratch, int* d_blk_code, int* d_blk_first, int* d_prob_block,
+                           int* d_info, cudaStream_t s) {
+  int launches = 0;
+  if (L <= 0 || nprob <= 0 || nprob > 65535) return -1;
+  if (cudaMemsetAsync(d_cnt, 0, sizeof(int) * size_t(L), s) != cudaSuccess) return -1;
+  if (P > 0) {
+    k_count_pairs<<<unsigned((P + 127) / 128), 128, 0, s>>>(P, d_pt_key_off, d_key_img, d_pt_prob, d_pinfo, d_cnt);
+    ++launches;
+  }
+  const dim3 g(unsigned(((long long)max_ie * max_ie + 255) / 256), unsigned(nprob));
+  k_block_marks<<<g, 256, 0, s>>>(d_pinfo, d_cnt, d_bid, d_off);
+  launches += 1 + scan_exclusive(d_bid, L, d_scratch, s) + scan_exclusive(d_off, L, d_scratch, s);
+  k_block_lists<<<g, 256, 0, s>>>(d_pinfo, qlast, d_cnt, d_bid, d_off, d_blk_code, d_blk_first, d_prob_block,
+                                  d_info);
+  return launches + 1;
+}
+
+int build_pairs_on_device(int P, int nblocks, const int4* d_pinfo, const int* d_pt_key_off, const int* d_key_img,
+                          const int* d_pt_prob, int* d_pp, const int* d_bid, long long n, int* d_keys0,
+                          int2* d_vals0, int* d_keys1, int2* d_vals1, int* d_hist, int* d_scratch, int* d_bad,
+                          int2** out, cudaStream_t s) {
   int launches = 0;
   if (P > 0) {
-    k_enumerate_pairs<<<unsigned((P + 127) / 128), 128, 0, s>>>(P, Ie, d_pt_key_off, d_key_img, d_pp_off,
-                                                                  d_bid, d_keys0, d_vals0);
+    k_point_pairs<<<unsigned((P + 256) / 256), 256, 0, s>>>(P, d_pt_key_off, d_pp);
+    launches += 1 + scan_exclusive(d_pp, (long long)P + 1, d_scratch, s);
+    k_enumerate_pairs<<<unsigned((P + 127) / 128), 128, 0, s>>>(P, d_pt_key_off, d_key_img, d_pt_prob, d_pinfo,
+                                                                  d_pp, d_bid, d_keys0, d_vals0);
     ++launches;
   }
   int bits = 1;
@@ -3433,10 +3508,9 @@ int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, c
   for (int pass = 0; pass < passes && n > 0; ++pass) {
     const int shift = 8 * pass;
     k_radix_hist<<<unsigned(ntiles), kSortThreads, 0, s>>>(kin, n, shift, ntiles, d_hist);
-    scan_exclusive(d_hist, L, d_sums, s);
+    launches += 2 + scan_exclusive(d_hist, L, d_scratch, s);
     k_radix_scatter<<<unsigned(ntiles), kSortThreads, 0, s>>>(kin, vin, n, shift, ntiles, d_hist, kout, vout,
                                                               d_bad);
-    launches += 5;
     std::swap(kin, kout);
     std::swap(vin, vout);
   }
@@ -3444,29 +3518,10 @@ int build_pairs_on_device(int P, int Ie, int nblocks, const int* d_pt_key_off, c
   return launches;
 }
 
-int count_blocks_on_device(int P, int Ie, const int* d_pt_key_off, const int* d_key_img, int* d_cnt, int* d_bid,
-                           int* d_off, int* d_sums, int* d_blk_code, int* d_blk_first, int* d_info,
-                           cudaStream_t s) {
-  const long long L = (long long)Ie * Ie;
-  int launches = 0;
-  if (L <= 0 || L > kDeviceScanMax) return -1;
-  if (cudaMemsetAsync(d_cnt, 0, sizeof(int) * size_t(L), s) != cudaSuccess) return -1;
-  if (P > 0) {
-    k_count_pairs<<<unsigned((P + 127) / 128), 128, 0, s>>>(P, Ie, d_pt_key_off, d_key_img, d_cnt);
-    ++launches;
-  }
-  const unsigned g = unsigned((L + 255) / 256);
-  k_block_marks<<<g, 256, 0, s>>>(L, Ie, d_cnt, d_bid, d_off);
-  launches += 1 + scan_exclusive(d_bid, L, d_sums, s) + scan_exclusive(d_off, L, d_sums, s);
-  k_block_lists<<<g, 256, 0, s>>>(L, Ie, d_cnt, d_bid, d_off, d_blk_code, d_blk_first, d_info);
-  return launches + 1;
-}
-
-int pairs_sort_scratch(long long n, long long* hist_ints, int* scan_chunks) {
+void pairs_sort_scratch(long long n, int P, long long* hist_ints, long long* scratch_ints) {
   const long long ntiles = (n + kSortTile - 1) / kSortTile;
   *hist_ints = 256LL * std::max<long long>(ntiles, 1);
-  *scan_chunks = int((*hist_ints + kScanChunk - 1) / kScanChunk);
-  return *scan_chunks <= 8192 ? 1 : 0;
+  *scratch_ints = std::max(scan_scratch_ints(*hist_ints), scan_scratch_ints((long long)P + 1));
 }
 
 }  // namespace gba

@@ -535,17 +535,15 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     std::vector<int> rec_ext;          // local reduced-system image of each camera record
     std::vector<int> prior_pt;         // point priors: global point, observed y, information
     std::vector<double> prior_y, prior_info;
-    bool pairs_on_device = false;      // the pair list is built by the device (below)
-    std::vector<int> bid;              // the dense block map kept for it (PCG plans)
-    // blocks counted on the device: its block map and the uploads it used
-    int* d_bid = nullptr;
-    int* d_key_img = nullptr;
-    int* d_pt_key_off = nullptr;
-    std::vector<long long> pp_off;     // [np + 1] first pair of each point, point-major
+    long long n_pairs = 0;             // key pairs (blocks built on the device)
   };
-  // one-problem plans without free cameras place their key pairs on the
-  // device (GBA_HOST_PAIRS=1 keeps the host placement, for comparison)
-  const bool device_pairs = nprob == 1 && !any_free && std::getenv("GBA_HOST_PAIRS") == nullptr;
+  // plans without free cameras count, number and place their key pairs on
+  // the device (GBA_HOST_PAIRS=1 keeps the host build, for comparison); the
+  // per-code tables take 12 bytes per (image, image) entry of every problem
+  long long codes = 0;
+  for (int q = 0; q < nprob; ++q) codes += (long long)prob[q].num_ext * prob[q].num_ext;
+  const bool dev_blocks = !any_free && nprob <= 65535 && codes <= (1LL << 26) &&
+                          std::getenv("GBA_HOST_PAIRS") == nullptr;
   std::vector<Piece> pieces(nprob);
   // fine phases of a single problem's build (GBA_BUILD_TIMING)
   auto sub = [&](const char* name) {
@@ -718,74 +716,22 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
           rec.push_back(make_int2(out.rec_ext[r], -(r + 1)));
     };
     sub("  records");
-    // One problem with keys only: the device counts the pairs of every image
-    // pair (atomics over the key pairs), numbers the blocks in the order of
-    // the host's count below ((i, j) lexicographic, every diagonal present)
-    // and returns the block list; it places the pairs later, so the block
-    // list, the pair list and the dense block map are the host's.
-    bool dev_counted = false;
-    if (device_pairs && !fc && ni > 0 && (long long)Ie * Ie <= kDeviceScanMax) {
-      out.pp_off.assign(size_t(np) + 1, 0);
+    // plans that build their blocks on the device (after this phase) only
+    // need the pair count here
+    if (dev_blocks) {
+      long long t = 0;
       for (int i = 0; i < np; ++i) {
         const long long k = cnt[i + 1] - cnt[i];
-        out.pp_off[i + 1] = out.pp_off[i] + k * (k + 1) / 2;
+        t += k * (k + 1) / 2;
       }
-      const long long total = out.pp_off[np];
-      if (total > INT32_MAX) {
-        out.err = GBA_ERR_INVALID;
-        return;
-      }
-      long long hist_ints = 0;
-      int scan_chunks = 0;
-      if (pairs_sort_scratch(total, &hist_ints, &scan_chunks)) {
-        const long long L = (long long)Ie * Ie, ub = (long long)Ie * (Ie + 1) / 2;
-        out.d_key_img = arena.upload(key_img);
-        out.d_pt_key_off = arena.upload(pt_key_off);
-        int* d_cnt = arena.alloc<int>(size_t(L));
-        int* d_off = arena.alloc<int>(size_t(L));
-        out.d_bid = arena.alloc<int>(size_t(L));
-        int* d_sums = arena.alloc<int>(size_t(L / 4096 + 1));
-        int* d_code = arena.alloc<int>(size_t(ub));
-        int* d_first = arena.alloc<int>(size_t(ub));
-        int* d_info = arena.alloc<int>(2);
-        const int nl = count_blocks_on_device(np, Ie, out.d_pt_key_off, out.d_key_img, d_cnt, out.d_bid, d_off,
-                                              d_sums, d_code, d_first, d_info, stream);
-        if (nl < 0) {
-          out.err = GBA_ERR;
-          return;
-        }
-        count_launches(nl);
-        GBA_CUDA(cudaGetLastError());
-        int info[2] = {0, 0};
-        GBA_CUDA(cudaMemcpyAsync(info, d_info, sizeof(info), cudaMemcpyDeviceToHost, stream));
-        GBA_CUDA(cudaStreamSynchronize(stream));
-        const int nb = info[0];
-        if (info[1] != total || nb < ni || nb > ub) {   // the counts disagree: never expected
-          out.err = GBA_ERR;
-          return;
-        }
-        std::vector<int> code(nb), first(nb);
-        GBA_CUDA(cudaMemcpyAsync(code.data(), d_code, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream));
-        GBA_CUDA(cudaMemcpyAsync(first.data(), d_first, sizeof(int) * nb, cudaMemcpyDeviceToHost, stream));
-        GBA_CUDA(cudaStreamSynchronize(stream));
-        out.blk_ij.resize(nb);
-        out.blk_off.resize(size_t(nb) + 1);
-        for (int b = 0; b < nb; ++b) {
-          out.blk_ij[b] = make_int2(code[b] / Ie, code[b] % Ie);
-          out.blk_off[b] = first[b];
-        }
-        out.blk_off[nb] = total;
-        out.pairs_on_device = true;
-        dev_counted = true;
-        sub("  pair counts (device)");
-      }
+      out.n_pairs = t;
     }
     // reduced-system blocks: (i <= j) with their record pairs, point order.
     // Pairs are counted and placed by point ranges in parallel: each piece
     // counts its pairs per image pair, a piece's pairs of a block follow
     // those of the pieces before it, so every block lists its pairs in
     // point order whatever the number of pieces.
-    if (!dev_counted) {
+    if (!dev_blocks) {
       const size_t nn = (size_t)Ie * Ie;
       int nth = nth0;
       while (nth > 1 && nn * size_t(nth) * sizeof(int) > (size_t(256) << 20)) --nth;
@@ -835,17 +781,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         out.err = GBA_ERR_INVALID;
         return;
       }
-      long long hist_ints = 0;
-      int scan_chunks = 0;
-      if (device_pairs && !fc && pairs_sort_scratch(acc, &hist_ints, &scan_chunks)) {
-        out.pairs_on_device = true;   // the device enumerates and sorts (device allocations)
-        if (pcg)
-          out.bid.swap(bid);
-        else
-          out.blk_map.swap(bid);
-        sub("  pair counts");
-      }
-      if (!out.pairs_on_device) {
+      {
         // cnt_t[t][e] becomes piece t's first slot in block e
         for (size_t e = 0; e < nn; ++e) {
           if (bid[e] < 0) continue;
@@ -887,7 +823,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         sub("  pairs placed");
       }
       // dense map for the assembly of the lower triangle: map[j*Ie + i], j <= i
-      if (!pcg && !out.pairs_on_device) out.blk_map.swap(bid);
+      if (!pcg) out.blk_map.swap(bid);
     }
     // soft constraints in y order (camera_shared_vector_function.hpp:483-629):
     // the rows after the keys, each a copy of one parameter with its own
@@ -952,6 +888,99 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     if (pieces[q].err) return pieces[q].err;
   phase("problems");
 
+  // ---- blocks on the device: the keys go up now, the device counts the
+  // pairs of every code and returns the block list, which is split into the
+  // problems' pieces (the layout of the host's count, block for block)
+  int* dv_key_img = nullptr;
+  int* dv_pt_key_off = nullptr;
+  int* dv_pt_prob = nullptr;
+  int* dv_bid = nullptr;
+  int4* dv_pinfo = nullptr;
+  int dv_blocks = 0;
+  std::vector<int> code_base(nprob, 0);
+  if (dev_blocks) {
+    for (int q = 0; q < nprob; ++q) pt_key_off[pbase[q]] = int(kbase[q]);
+    pt_key_off[P] = int(K);
+    std::vector<int4> pinfo(nprob);
+    long long L = 0, ub = 0, total = 0, min_blocks = 0;
+    int qlast = -1, max_ie = 0;
+    for (int q = 0; q < nprob; ++q) {
+      const int n = prob[q].num_ext;   // the images (no free cameras)
+      pinfo[q] = make_int4(int(ibase[q]), n, int(L), 0);
+      code_base[q] = int(L);
+      L += (long long)n * n;
+      ub += (long long)n * (n + 1) / 2;
+      min_blocks += n;
+      if (n > 0) qlast = q;
+      max_ie = std::max(max_ie, n);
+      total += pieces[q].n_pairs;
+    }
+    if (total > INT32_MAX) return GBA_ERR_INVALID;
+    dv_key_img = arena.upload(key_img);
+    dv_pt_key_off = arena.upload(pt_key_off);
+    dv_pt_prob = arena.upload(pt_prob);
+    dv_pinfo = arena.upload(pinfo);
+    std::vector<int> code, first, pblk(nprob, 0);
+    if (qlast >= 0) {
+      int* d_cnt = arena.alloc<int>(size_t(L));
+      int* d_off = arena.alloc<int>(size_t(L));
+      dv_bid = arena.alloc<int>(size_t(L));
+      int* d_scratch = arena.alloc<int>(size_t(scan_scratch_ints(L)));
+      int* d_code = arena.alloc<int>(size_t(ub));
+      int* d_first = arena.alloc<int>(size_t(ub));
+      int* d_pblk = arena.alloc<int>(size_t(nprob));
+      int* d_info = arena.alloc<int>(2);
+      const int nl = count_blocks_on_device(nprob, qlast, max_ie, int(P), dv_pinfo, dv_pt_key_off, dv_key_img,
+                                            dv_pt_prob, L, d_cnt, dv_bid, d_off, d_scratch, d_code, d_first,
+                                            d_pblk, d_info, stream);
+      if (nl < 0) return GBA_ERR;
+      count_launches(nl);
+      GBA_CUDA(cudaGetLastError());
+      int info[2] = {0, 0};
+      GBA_CUDA(cudaMemcpyAsync(info, d_info, sizeof(info), cudaMemcpyDeviceToHost, stream));
+      GBA_CUDA(cudaStreamSynchronize(stream));
+      dv_blocks = info[0];
+      if (info[1] != total || dv_blocks < min_blocks || dv_blocks > ub) return GBA_ERR;   // never expected
+      code.resize(dv_blocks);
+      first.resize(dv_blocks);
+      GBA_CUDA(cudaMemcpyAsync(code.data(), d_code, sizeof(int) * code.size(), cudaMemcpyDeviceToHost, stream));
+      GBA_CUDA(cudaMemcpyAsync(first.data(), d_first, sizeof(int) * first.size(), cudaMemcpyDeviceToHost, stream));
+      GBA_CUDA(cudaMemcpyAsync(pblk.data(), d_pblk, sizeof(int) * nprob, cudaMemcpyDeviceToHost, stream));
+      GBA_CUDA(cudaStreamSynchronize(stream));
+    }
+    // problem q's blocks run from its first block to the next problem's with images
+    std::vector<int> pend(nprob, dv_blocks);
+    for (int q = nprob - 2, nxt = dv_blocks; q >= 0; --q) {
+      if (prob[q + 1].num_ext > 0) nxt = pblk[q + 1];
+      pend[q] = nxt;
+    }
+    bool bad = false;
+    long long pair_base = 0;
+    for (int q = 0; q < nprob; ++q) {
+      Piece& pc = pieces[q];
+      const int n = prob[q].num_ext;
+      pc.blk_ij.clear();
+      pc.blk_off.assign(1, 0);
+      if (n > 0) {
+        const int b0 = pblk[q], b1 = pend[q];
+        if (b0 < 0 || b1 < b0 || b1 > dv_blocks || first[b0] != pair_base) {
+          bad = true;
+          break;
+        }
+        pc.blk_ij.resize(b1 - b0);
+        pc.blk_off.resize(size_t(b1 - b0) + 1);
+        for (int t = b0; t < b1; ++t) {
+          pc.blk_ij[t - b0] = make_int2(code[t] / n, code[t] % n);
+          pc.blk_off[t - b0] = first[t] - pair_base;
+        }
+        pc.blk_off[b1 - b0] = pc.n_pairs;
+      }
+      pair_base += pc.n_pairs;
+    }
+    if (bad) return GBA_ERR;   // the device's blocks disagree with the counts: never expected
+    phase("blocks (device)");
+  }
+
   // ---- concatenation in problem order: a serial pass sizes every list and
   // gives each problem its slices, then the problems fill them in parallel
   // (the layout is exactly that of appending the problems one after another)
@@ -990,7 +1019,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   img_item_off.assign(size_t(I) + 1, 0);
   // the pair lists (the largest array): one problem's list moves into place;
   // a batch's lists go straight from each problem to its slice on the device
-  int2* d_pairs = nprob > 1 ? arena.alloc<int2>(size_t(tot.pairs)) : nullptr;
+  int2* d_pairs = nprob > 1 && !dev_blocks ? arena.alloc<int2>(size_t(tot.pairs)) : nullptr;
   std::atomic<int> pair_upload_failed{0};
   std::vector<int> pt_rec_off;
   std::vector<int2> rec_info(tot.recs);
@@ -1078,7 +1107,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       blk_item_off[block_begin + t + 1] = int(it);
     }
     pi.num_items = int(it - b.items);
-    blk_map_off[q] = b.blk_map;
+    blk_map_off[q] = dev_blocks ? code_base[q] : b.blk_map;
     if (!pcg && nprob > 1)
       for (size_t e = 0; e < pc.blk_map.size(); ++e)
         blk_map[b.blk_map + e] = pc.blk_map[e] >= 0 ? pc.blk_map[e] + block_begin : -1;
@@ -1137,13 +1166,13 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.prob = arena.upload(prob);
   D.state = arena.alloc<LMState>(nprob);
   D.K = int(K);
-  D.key_img = nprob == 1 && pieces[0].d_key_img ? pieces[0].d_key_img : arena.upload(key_img);
+  D.key_img = dv_key_img ? dv_key_img : arena.upload(key_img);
   D.key_pt = arena.upload(key_pt);
   D.key_obs = arena.upload(key_obs);
   D.key_wl = any_weights ? arena.upload(key_wl) : nullptr;
   D.P = int(P);
-  D.pt_key_off = nprob == 1 && pieces[0].d_pt_key_off ? pieces[0].d_pt_key_off : arena.upload(pt_key_off);
-  D.pt_prob = arena.upload(pt_prob);
+  D.pt_key_off = dv_pt_key_off ? dv_pt_key_off : arena.upload(pt_key_off);
+  D.pt_prob = dv_pt_prob ? dv_pt_prob : arena.upload(pt_prob);
   D.I = int(I);
   D.img_key_off = arena.upload(img_key_off);
   D.img_keys = arena.upload(img_keys);
@@ -1316,41 +1345,28 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       }
     }
   }
-  D.blk_map = nprob == 1 && pieces[0].d_bid && !pcg ? pieces[0].d_bid : arena.upload(blk_map);
+  D.blk_map = dev_blocks && !pcg ? dv_bid : arena.upload(blk_map);
   int dev_pair_bad = 0;
   int* d_pair_bad = nullptr;
-  if (nprob == 1 && pieces[0].pairs_on_device) {
-    // enumerate every point's pairs with their block ids and sort them by
-    // block (stable) on the device: the host's placement, without its
-    // scattered writes and the copy of the list
-    std::vector<long long> pp_off;
-    if (!pieces[0].pp_off.empty()) {
-      pp_off.swap(pieces[0].pp_off);
-    } else {
-      pp_off.assign(size_t(P) + 1, 0);
-      for (int64_t i = 0; i < P; ++i) {
-        const long long k = pt_key_off[i + 1] - pt_key_off[i];
-        pp_off[i + 1] = pp_off[i] + k * (k + 1) / 2;
-      }
-    }
+  if (dev_blocks) {
+    // every point's pairs with their block ids, sorted stably by block on
+    // the device: the host's placement, without its scattered writes and the
+    // copy of the list
     const long long n = tot.pairs;
-    if (pp_off[P] != n) return GBA_ERR;   // the counts disagree: never expected
-    long long hist_ints = 0;
-    int scan_chunks = 0;
-    pairs_sort_scratch(n, &hist_ints, &scan_chunks);
-    const int* d_bid = pieces[0].d_bid ? pieces[0].d_bid : pcg ? arena.upload(pieces[0].bid) : D.blk_map;
+    long long hist_ints = 0, scratch_ints = 0;
+    pairs_sort_scratch(n, int(P), &hist_ints, &scratch_ints);
     int* k0 = arena.alloc<int>(size_t(n));
     int* k1 = arena.alloc<int>(size_t(n));
     int2* v0 = arena.alloc<int2>(size_t(n));
     int2* v1 = arena.alloc<int2>(size_t(n));
     int* hist = arena.alloc<int>(size_t(hist_ints));
-    int* sums = arena.alloc<int>(size_t(scan_chunks));
+    int* scratch = arena.alloc<int>(size_t(scratch_ints));
+    int* pp = arena.alloc<int>(size_t(P) + 1);
     d_pair_bad = arena.alloc<int>(1);
     GBA_CUDA(cudaMemsetAsync(d_pair_bad, 0, sizeof(int), stream));
     int2* sorted = nullptr;
-    count_launches(build_pairs_on_device(int(P), prob[0].num_ext, int(blk_ij.size()), D.pt_key_off,
-                                         D.key_img, arena.upload(pp_off), d_bid, n, k0, v0, k1, v1,
-                                         hist, sums, d_pair_bad, &sorted, stream));
+    count_launches(build_pairs_on_device(int(P), dv_blocks, dv_pinfo, dv_pt_key_off, dv_key_img, dv_pt_prob, pp,
+                                         dv_bid, n, k0, v0, k1, v1, hist, scratch, d_pair_bad, &sorted, stream));
     GBA_CUDA(cudaGetLastError());
     D.pairs = sorted;
   } else {

@@ -1,9 +1,10 @@
-"""The device's pair placement (enumeration + stable radix sort by block)
-against the host's: a single-problem plan builds its key-pair list on the
-device unless GBA_HOST_PAIRS is set, and both lists must give the same
-solve, bit for bit -- one radix pass (fewer than 256 blocks), two and three
-passes (more than 65,536 blocks), the dense and the PCG solver, FP64 and
-mixed, single-key points and keyless images."""
+"""The device's block and pair build (pair counts per image pair, block
+numbering, enumeration and a stable radix sort by block) against the
+host's: plans without free cameras build their blocks and key-pair list on
+the device unless GBA_HOST_PAIRS is set, and both must give the same solve,
+bit for bit -- one radix pass (fewer than 256 blocks), two and three passes
+(more than 65,536 blocks), the dense and the PCG solver, FP64 and mixed,
+single-key points, keyless images, ragged batches with empty problems."""
 import numpy as np
 import pytest
 
@@ -88,3 +89,27 @@ def test_presorted_keys_take_the_same_path(gba):
     x1, r1 = gba.solve(t, opt)
     np.testing.assert_array_equal(x0, x1)
     assert r0.final_cost == r1.final_cost
+
+
+@pytest.mark.parametrize("solver", [abi.LINEAR_DENSE_CHOLESKY, abi.LINEAR_PCG])
+def test_batch_blocks_on_device(gba, monkeypatch, solver):
+    # a ragged batch (empty, tiny and larger problems): the problems' code
+    # ranges follow each other, the device's blocks and pairs are the host's
+    s0 = synthetic.ring_scene(num_images=3, num_points=20, obs_per_point=2, seed=26)
+    empty = synthetic.Scene(**{**s0.__dict__})
+    empty.feature_maps = s0.feature_maps[:0]
+    empty.near_y = s0.near_y[2 * s0.number_of_keys:]
+    scenes = [synthetic.ring_scene(num_images=2, num_points=5, obs_per_point=2, seed=27), empty,
+              synthetic.ring_scene(num_images=30, num_points=3000, obs_range=(3, 8), seed=28),
+              synthetic.grid_scene(num_images=40, num_points=4000, seed=29), empty,
+              synthetic.ring_scene(num_images=12, num_points=800, obs_per_point=5, seed=30)]
+    opt = abi.make_options(precision=abi.PRECISION_MIXED, linear_solver=solver, **OPT)
+    monkeypatch.delenv("GBA_HOST_PAIRS", raising=False)
+    xs_dev, reps_dev = gba.solve_batch(scenes, opt)
+    monkeypatch.setenv("GBA_HOST_PAIRS", "1")
+    xs_host, reps_host = gba.solve_batch(scenes, opt)
+    monkeypatch.delenv("GBA_HOST_PAIRS", raising=False)
+    for xd, xh, rd, rh in zip(xs_dev, xs_host, reps_dev, reps_host):
+        assert rd.status == abi.GBA_OK and rh.status == abi.GBA_OK
+        np.testing.assert_array_equal(xd, xh)
+        assert rd.final_cost == rh.final_cost

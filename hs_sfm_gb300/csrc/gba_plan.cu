@@ -1854,35 +1854,96 @@ namespace {
 // Every problem's x and report in one device gather and a few copies (the
 // batch path of gba_solve_batch; the per-problem calls would synchronize the
 // stream once per problem).
+// Page-locked host staging for the x copies.  Page-locking memory is costly,
+// so released buffers are kept (up to kPinnedKeep) and reused by later
+// calls; a pageable buffer stands in when page-locked memory is refused.
+class PinnedStage {
+ public:
+  explicit PinnedStage(size_t n) : n_(std::max<size_t>(n, 1)) {
+    {
+      std::lock_guard<std::mutex> g(mu());
+      auto& fl = free_list();
+      for (size_t i = 0; i < fl.size(); ++i)
+        if (fl[i].second >= n_) {
+          p_ = fl[i].first;
+          cap_ = fl[i].second;
+          fl.erase(fl.begin() + long(i));
+          return;
+        }
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, n_ * sizeof(double), cudaHostAllocPortable) == cudaSuccess) {
+      p_ = static_cast<double*>(p);
+      cap_ = n_;
+    } else {
+      cudaGetLastError();
+      fallback_.resize(n_);
+    }
+  }
+  ~PinnedStage() {
+    if (!p_) return;
+    std::lock_guard<std::mutex> g(mu());
+    auto& fl = free_list();
+    fl.emplace_back(p_, cap_);
+    if (fl.size() > kPinnedKeep) {   // drop the smallest
+      size_t m = 0;
+      for (size_t i = 1; i < fl.size(); ++i)
+        if (fl[i].second < fl[m].second) m = i;
+      cudaFreeHost(fl[m].first);
+      fl.erase(fl.begin() + long(m));
+    }
+  }
+  PinnedStage(const PinnedStage&) = delete;
+  PinnedStage& operator=(const PinnedStage&) = delete;
+  double* data() { return p_ ? p_ : fallback_.data(); }
+
+ private:
+  static constexpr size_t kPinnedKeep = 4;
+  static std::mutex& mu() {
+    static std::mutex m;
+    return m;
+  }
+  static std::vector<std::pair<double*, size_t>>& free_list() {
+    static auto* fl = new std::vector<std::pair<double*, size_t>>();   // outlives static destruction
+    return *fl;
+  }
+  size_t n_;
+  double* p_ = nullptr;
+  size_t cap_ = 0;
+  std::vector<double> fallback_;
+};
+
 int get_all(gba::Plan& P, double* const* xs, gba_report* reports) {
   return guarded([&] {
     GBA_CUDA(cudaStreamSynchronize(P.stream));
     std::vector<gba::LMState> st(P.B);
     GBA_CUDA(cudaMemcpy(st.data(), P.d.state, sizeof(gba::LMState) * P.B, cudaMemcpyDeviceToHost));
     const long long np = 3LL * P.d.P, ni = 6LL * P.d.I, nc = P.d.free_cams ? 10LL * P.d.Ctot : 0;
-    std::vector<double> h(size_t(np + ni + nc));
-    if (!h.empty()) {
-      double* dx = P.arena.alloc<double>(h.size());
+    const size_t nx = size_t(np + ni + nc);
+    PinnedStage stage(nx);
+    double* const h = stage.data();
+    if (nx) {
+      double* dx = P.arena.alloc<double>(nx);
       gba::launch_gather_x(P.d, P.ran ? 1 : 0, dx, P.stream);
       gba::count_launches(1);
-      GBA_CUDA(cudaMemcpyAsync(h.data(), dx, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, P.stream));
+      GBA_CUDA(cudaMemcpyAsync(h, dx, sizeof(double) * nx, cudaMemcpyDeviceToHost, P.stream));
       GBA_CUDA(cudaStreamSynchronize(P.stream));
       GBA_CUDA(cudaGetLastError());
     }
-    P.d2h_bytes += (long long)(sizeof(gba::LMState) * P.B + sizeof(double) * h.size());
+    P.d2h_bytes += (long long)(sizeof(gba::LMState) * P.B + sizeof(double) * nx);
     const int nth = std::min(gba::host_threads(), P.B);
     std::atomic<int> next{0};
     gba::host_parallel(nth, nth, [&](int64_t, int64_t, int) {
       for (int q = next++; q < P.B; q = next++) {
         const gba::ProbInfo& pi = P.prob[q];
         double* x = xs[q];
-        std::copy(h.begin() + 3LL * pi.point_begin, h.begin() + 3LL * (pi.point_begin + pi.num_points), x);
-        std::copy(h.begin() + np + 6LL * pi.image_begin,
-                  h.begin() + np + 6LL * (pi.image_begin + pi.num_images), x + 3LL * pi.num_points);
+        std::copy(h + 3LL * pi.point_begin, h + 3LL * (pi.point_begin + pi.num_points), x);
+        std::copy(h + np + 6LL * pi.image_begin, h + np + 6LL * (pi.image_begin + pi.num_images),
+                  x + 3LL * pi.num_points);
         double* xc = x + 3LL * pi.num_points + 6LL * pi.num_images;
         for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
-          std::copy(h.begin() + np + ni + 10LL * (pi.cam_begin + c),
-                    h.begin() + np + ni + 10LL * (pi.cam_begin + c) + pi.cps, xc + (size_t)pi.cps * c);
+          std::copy(h + np + ni + 10LL * (pi.cam_begin + c), h + np + ni + 10LL * (pi.cam_begin + c) + pi.cps,
+                    xc + (size_t)pi.cps * c);
         if (reports) fill_report(P, q, st[q], &reports[q]);
       }
     });
@@ -1894,33 +1955,34 @@ int get_all(gba::Plan& P, double* const* xs, gba_report* reports) {
 int set_all_x0(gba::Plan& P, const double* const* xs) {
   return guarded([&] {
     const long long np = 3LL * P.d.P, ni = 6LL * P.d.I, nc = P.d.free_cams ? 10LL * P.d.Ctot : 0;
-    std::vector<double> h(size_t(np + ni + nc), 0.0);
+    const size_t nx = size_t(np + ni + nc);
+    PinnedStage stage(nx);
+    double* const h = stage.data();
+    std::fill(h + np + ni, h + nx, 0.0);   // the camera slots past each camera's parameters
     const int nth = std::min(gba::host_threads(), P.B);
     std::atomic<int> next{0};
     gba::host_parallel(nth, nth, [&](int64_t, int64_t, int) {
       for (int q = next++; q < P.B; q = next++) {
         const gba::ProbInfo& pi = P.prob[q];
         const double* x = xs[q];
-        std::copy(x, x + 3LL * pi.num_points, h.begin() + 3LL * pi.point_begin);
+        std::copy(x, x + 3LL * pi.num_points, h + 3LL * pi.point_begin);
         std::copy(x + 3LL * pi.num_points, x + 3LL * pi.num_points + 6LL * pi.num_images,
-                  h.begin() + np + 6LL * pi.image_begin);
+                  h + np + 6LL * pi.image_begin);
         const double* xc = x + 3LL * pi.num_points + 6LL * pi.num_images;
         for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
-          std::copy(xc + (size_t)pi.cps * c, xc + (size_t)pi.cps * (c + 1),
-                    h.begin() + np + ni + 10LL * (pi.cam_begin + c));
+          std::copy(xc + (size_t)pi.cps * c, xc + (size_t)pi.cps * (c + 1), h + np + ni + 10LL * (pi.cam_begin + c));
       }
     });
     if (np)
-      GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_pt), h.data(), sizeof(double) * np,
-                               cudaMemcpyHostToDevice, P.stream));
+      GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_pt), h, sizeof(double) * np, cudaMemcpyHostToDevice,
+                               P.stream));
     if (ni)
-      GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_img), h.data() + np, sizeof(double) * ni,
+      GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_img), h + np, sizeof(double) * ni,
                                cudaMemcpyHostToDevice, P.stream));
     if (nc)
-      GBA_CUDA(cudaMemcpyAsync(P.d.x0_cam, h.data() + np + ni, sizeof(double) * nc, cudaMemcpyHostToDevice,
-                               P.stream));
+      GBA_CUDA(cudaMemcpyAsync(P.d.x0_cam, h + np + ni, sizeof(double) * nc, cudaMemcpyHostToDevice, P.stream));
     GBA_CUDA(cudaStreamSynchronize(P.stream));
-    P.h2d_bytes += (long long)sizeof(double) * (long long)h.size();
+    P.h2d_bytes += (long long)(sizeof(double) * nx);
     return GBA_OK;
   });
 }
@@ -2012,20 +2074,34 @@ int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, i
   // CUDA graph would cost more than it saves, so it is launched directly.
   gba_options once = *options;
   once.use_cuda_graph = 0;
+  // GBA_BUILD_TIMING=1 prints the phases of the call to stderr
+  const bool timing = std::getenv("GBA_BUILD_TIMING") != nullptr;
+  const auto t0 = std::chrono::steady_clock::now();
+  auto phase = [&](const char* name) {
+    if (!timing) return;
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    std::fprintf(stderr, "gba solve: %-16s %8.2f ms\n", name, ms);
+  };
   gba_plan* plan = nullptr;
   int err = gba_plan_create(problems, near_ys, n, &once, &plan);
   if (err) return err;
+  phase("plan built");
   for (int q = 0; q < n && !err; ++q)
     if (!x_inout[q] && plan->impl.x_size[q] > 0) err = GBA_ERR_INVALID;
   if (!err) err = set_all_x0(plan->impl, x_inout);
+  phase("x0 uploaded");
   if (!err) err = gba_plan_run(plan);
+  phase("launched");
   if (!err) err = gba_plan_synchronize(plan);
+  phase("solved");
   if (!err) err = get_all(plan->impl, x_inout, reports);
+  phase("x read back");
   int first_status = GBA_OK;
   if (!err && reports)
     for (int q = 0; q < n; ++q)
       if (reports[q].status != GBA_OK) { first_status = reports[q].status; break; }
   gba_plan_destroy(plan);
+  phase("plan destroyed");
   return err ? err : first_status;
 }
 

@@ -217,6 +217,25 @@ NCU_DRAM_BYTES = {
 }
 
 
+def iteration_roofline(K, P, I, pairs, t_iter_ms, hbm_gbs, ffma_tflops, tsz):
+    """The whole LM iteration against its speed of light: algorithmic bytes
+    B = 40 K + 168 P + 120 I + (6I)^2 (tsz for the reduced system's write,
+    2 tsz for the factorization's read and write) and FLOPs
+    F = 216 K + sum_p [45 + 108 k + 216 k (k + 1) / 2 + 36 k] + (6I)^3 / 3
+    (k keys of point p); the iteration cannot take less than
+    max(B / HBM peak, F / FMA peak)."""
+    n = 6 * I
+    b = 40.0 * K + 168.0 * P + 120.0 * I + 3.0 * tsz * n * n
+    f = 216.0 * K + 45.0 * P + 144.0 * K + 216.0 * pairs + n ** 3 / 3.0
+    t_hbm = b / (hbm_gbs * 1e9)
+    t_fma = f / (ffma_tflops * 1e12) if ffma_tflops else 0.0
+    t_sol = max(t_hbm, t_fma)
+    return {"bound": "fp32" if t_fma >= t_hbm else "hbm", "algorithmic_bytes": b,
+            "algorithmic_flops": f, "speed_of_light_us": 1e6 * t_sol,
+            "measured_us": 1e3 * t_iter_ms, "frac": t_sol / (t_iter_ms / 1e3),
+            "peaks": {"hbm_gbs": hbm_gbs, "fp32_fma_tflops": ffma_tflops}}
+
+
 def pair_count(scene):
     fm = scene.feature_maps
     k = np.bincount(fm[:, 1], minlength=scene.number_of_points)
@@ -378,6 +397,7 @@ def run_gba(args, ws, rank, local):
                          "frac": roofline["achieved"] / ffma,
                          "peak_kind": "measured live (gba_fma_peak, FP32 FMA, this run)",
                          "fp64_fma_tflops": dfma}
+    roofline_iteration = iteration_roofline(K, P, I, pairs, total_ms / iters, peak, ffma, tsz)
     roofline_hbm = None
     if hbm_stages:
         dom = max(hbm_stages, key=lambda k: hbm_stages[k]["ms_per_iteration"])
@@ -460,6 +480,7 @@ def run_gba(args, ws, rank, local):
             "roofline": roofline,
             "roofline_fp32": roofline_fp32,
             "roofline_hbm": roofline_hbm,
+            "roofline_iteration": roofline_iteration,
             "stages": stages,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms))},

@@ -212,6 +212,23 @@ bool cameras_free(const gba_problem& p) {
          params_per_camera(p.intrinsic_computations_mask) > 0;
 }
 
+// A host array whose elements start uninitialized: the builders write every
+// entry, so the pages are first touched by their parallel loops instead of
+// by a serial zero fill.
+template <typename T>
+struct HostBuf {
+  std::unique_ptr<T[]> p;
+  size_t n = 0;
+  HostBuf() = default;
+  explicit HostBuf(size_t count) : p(count ? new T[count] : nullptr), n(count) {}
+  T& operator[](size_t i) { return p[i]; }
+  const T& operator[](size_t i) const { return p[i]; }
+  T* data() { return p.get(); }
+  const T* data() const { return p.get(); }
+  size_t size() const { return n; }
+  bool empty() const { return n == 0; }
+};
+
 // Device buffer registry.  Allocations are stream-ordered on the plan's
 // stream (cudaMallocAsync / cudaFreeAsync from the device's default pool), so
 // creating or destroying a plan never synchronizes other plans' streams.
@@ -230,12 +247,19 @@ struct DeviceArena {
     return static_cast<T*>(p);
   }
   template <typename T>
-  T* upload(const std::vector<T>& h) {
-    T* p = alloc<T>(h.size());
-    if (!h.empty())
-      GBA_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
-    uploaded += (long long)(h.size() * sizeof(T));
+  T* upload(const T* h, size_t n) {
+    T* p = alloc<T>(n);
+    if (n) GBA_CUDA(cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+    uploaded += (long long)(n * sizeof(T));
     return p;
+  }
+  template <typename T>
+  T* upload(const std::vector<T>& h) {
+    return upload(h.data(), h.size());
+  }
+  template <typename T>
+  T* upload(const HostBuf<T>& h) {
+    return upload(h.data(), h.size());
   }
   void release() {
     for (void* p : ptrs) cudaFreeAsync(p, stream);
@@ -447,14 +471,12 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   }
   if (P > INT32_MAX / 4 || K > INT32_MAX / 4 || I > INT32_MAX / 64) return GBA_ERR_INVALID;
 
-  std::vector<int> key_img(K), key_pt(K);
-  std::vector<double2> key_obs(K);
-  std::vector<double> key_wl;
+  HostBuf<int> key_img(K), key_pt(K), img_keys(K);
+  HostBuf<double2> key_obs(K);
   bool any_weights = false;
   for (int q = 0; q < nprob; ++q) any_weights |= problems[q].key_covariance_inverse != nullptr;
-  if (any_weights) key_wl.assign(3 * K, 0.0);
-  std::vector<int> pt_key_off(P + 1, 0), pt_prob(P), img_key_off(I + 1, 0), img_keys(K),
-      img_prob(I), img_cam(I);
+  HostBuf<double> key_wl(any_weights ? 3 * K : 0);
+  std::vector<int> pt_key_off(P + 1, 0), pt_prob(P), img_key_off(I + 1, 0), img_prob(I), img_cam(I);
   std::vector<double> cam64(10 * std::max<int64_t>(C, 1), 0.0);
   std::vector<float> cam32(cam64.size(), 0.0f);
   std::vector<int2> pairs;
@@ -606,12 +628,34 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     if (!presorted) {
       std::vector<char> dup(nth0, 0);
       host_parallel(np, nth0, [&](int64_t i0, int64_t i1, int t) {
+        constexpr int kShort = 32;   // tracks this long sort in registers
+        int64_t im[kShort];
+        int ix[kShort];
         for (int64_t i = i0; i < i1; ++i) {
-          std::sort(order.begin() + cnt[i], order.begin() + cnt[i + 1], [&](int a, int b) {
-            return p.feature_maps[2 * a] < p.feature_maps[2 * b];
-          });
-          for (int u = cnt[i] + 1; u < cnt[i + 1]; ++u)
-            if (p.feature_maps[2 * order[u]] == p.feature_maps[2 * order[u - 1]]) dup[t] = 1;
+          const int b0 = cnt[i], n = cnt[i + 1] - b0;
+          if (n <= 1) continue;
+          if (n <= kShort) {   // insertion sort of (image, key) (a repeated image is an error)
+            for (int u = 0; u < n; ++u) {
+              const int k = order[b0 + u];
+              const int64_t v = fm[2 * k];
+              int j = u - 1;
+              while (j >= 0 && im[j] > v) {
+                im[j + 1] = im[j];
+                ix[j + 1] = ix[j];
+                --j;
+              }
+              im[j + 1] = v;
+              ix[j + 1] = k;
+            }
+            for (int u = 0; u < n; ++u) {
+              order[b0 + u] = ix[u];
+              if (u && im[u] == im[u - 1]) dup[t] = 1;
+            }
+            continue;
+          }
+          std::sort(order.begin() + b0, order.begin() + b0 + n, [&](int a, int b) { return fm[2 * a] < fm[2 * b]; });
+          for (int u = b0 + 1; u < b0 + n; ++u)
+            if (fm[2 * order[u]] == fm[2 * order[u - 1]]) dup[t] = 1;
         }
       });
       for (char v : dup)

@@ -1534,61 +1534,92 @@ __device__ __forceinline__ void tile_sub_xyt(Tile<T>& A, const Tile<T>& X, const
   }
 }
 
-// Factor the SPD tile D (lower triangle used; identity-padded) in one warp and
-// write L^-1 to Dinv (D is left as it is).  Lane i keeps row i of the tile
-// in registers, and column i of L^-1 (forward substitution against L).
-// Columns are factored two at a time: every lane forms the 2x2 pivot block
-// from three shuffles (both reciprocal square roots issued together: the
-// second pivot is det / p0), then its own entries of both columns, which
-// are broadcast through shared memory (col: two buffers of two columns) for
-// the trailing update of the tile and of the inverse columns.  No
-// divisions.  Returns false when a pivot was not positive.
+// Factor the SPD tile D (lower triangle used; identity-padded) and write
+// L^-1 to Dinv (D is left as it is), in two warps of the CTA: lane i of warp
+// 0 keeps row i of the tile in registers, lane i of warp 1 column i of L^-1
+// (forward substitution against L).  Columns are factored two at a time:
+// every lane of warp 0 forms the 2x2 pivot block from three shuffles (both
+// reciprocal square roots issued together: the second pivot is det / p0),
+// then its own entries of both columns, which go to shared memory (col: two
+// buffers of two columns, piv: two buffers of the pivot block's r0, l10,
+// r1) for the trailing updates -- of the tile's rows in warp 0, of the
+// inverse's columns in warp 1, after one 64-thread named barrier per column
+// pair.  A buffer is rewritten two column pairs later, after warp 1 has
+// passed the next barrier, so one barrier per pair suffices.  No divisions.
+// Returns false (in warp 0) when a pivot was not positive.
+constexpr int kPotrfBarrier = 1;   // named barrier id (0 is __syncthreads)
+
+__device__ __forceinline__ void potrf_pair_sync() {
+  asm volatile("bar.sync %0, 64;\n" ::"n"(kPotrfBarrier) : "memory");
+}
+
 template <typename T>
-__device__ bool warp_potrf_inverse(const Tile<T>& D, Tile<T>& Dinv, T* col, int lane) {
+__device__ bool pair_potrf_inverse(const Tile<T>& D, Tile<T>& Dinv, T* col, T* piv, int warp, int lane) {
   using V = Vec16<T>;
   constexpr int N = V::N;
   constexpr unsigned FULL = 0xffffffffu;
-  T a[kTile], x[kTile];
-#pragma unroll
-  for (int q = 0; q < kTile; q += N) V::unpack(*reinterpret_cast<const typename V::V*>(&D[lane][q]), a + q);
-#pragma unroll
-  for (int r = 0; r < kTile; ++r) x[r] = (r == lane) ? T(1) : T(0);
   bool ok = true;
-  // j is a compile-time constant in every step, so a[] and x[] stay in registers
-  static_for<0, kTile, 2>([&](auto jc) {
-    constexpr int j = decltype(jc)::value;
-    const T p0 = __shfl_sync(FULL, a[j], j);
-    const T p1 = __shfl_sync(FULL, a[j], j + 1);
-    const T p2 = __shfl_sync(FULL, a[j + 1], j + 1);
-    const T det = fma(p0, p2, -(p1 * p1));
-    const T r0 = rsqrt(p0);
-    const T rd = rsqrt(det);
-    const T l00 = p0 * r0;             // sqrt(p0)
-    const T l10 = p1 * r0;
-    const T r1 = l00 * rd;             // 1 / sqrt(det / p0)
-    const T l11 = det * rd * r0;       // sqrt(det / p0)
-    ok = ok && (p0 > T(0)) && (det > T(0));
-    const T li0 = (lane > j) ? a[j] * r0 : ((lane == j) ? l00 : T(0));
-    const T li1 = (lane > j + 1) ? fma(-li0, l10, a[j + 1]) * r1 : ((lane == j + 1) ? l11 : T(0));
-    a[j] = li0;
-    a[j + 1] = li1;
-    T* cb = col + ((j >> 1) & 1) * 2 * kTile;
-    cb[lane] = li0;
-    cb[kTile + lane] = li1;
-    x[j] *= r0;
-    x[j + 1] = fma(-l10, x[j], x[j + 1]) * r1;
-    __syncwarp();
+  if (warp == 0) {
+    T a[kTile];
 #pragma unroll
-    for (int l = j + 2; l < kTile; ++l) {
-      const T c0 = cb[l], c1 = cb[kTile + l];
-      a[l] = fma(-li0, c0, a[l]);
-      a[l] = fma(-li1, c1, a[l]);
-      x[l] = fma(-c0, x[j], x[l]);
-      x[l] = fma(-c1, x[j + 1], x[l]);
-    }
-  });
+    for (int q = 0; q < kTile; q += N) V::unpack(*reinterpret_cast<const typename V::V*>(&D[lane][q]), a + q);
+    // j is a compile-time constant in every step, so a[] stays in registers
+    static_for<0, kTile, 2>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      const T p0 = __shfl_sync(FULL, a[j], j);
+      const T p1 = __shfl_sync(FULL, a[j], j + 1);
+      const T p2 = __shfl_sync(FULL, a[j + 1], j + 1);
+      const T det = fma(p0, p2, -(p1 * p1));
+      const T r0 = rsqrt(p0);
+      const T rd = rsqrt(det);
+      const T l00 = p0 * r0;             // sqrt(p0)
+      const T l10 = p1 * r0;
+      const T r1 = l00 * rd;             // 1 / sqrt(det / p0)
+      const T l11 = det * rd * r0;       // sqrt(det / p0)
+      ok = ok && (p0 > T(0)) && (det > T(0));
+      const T li0 = (lane > j) ? a[j] * r0 : ((lane == j) ? l00 : T(0));
+      const T li1 = (lane > j + 1) ? fma(-li0, l10, a[j + 1]) * r1 : ((lane == j + 1) ? l11 : T(0));
+      a[j] = li0;
+      a[j + 1] = li1;
+      const int buf = (j >> 1) & 1;
+      T* cb = col + buf * 2 * kTile;
+      cb[lane] = li0;
+      cb[kTile + lane] = li1;
+      if (lane == 0) {
+        piv[4 * buf] = r0;
+        piv[4 * buf + 1] = l10;
+        piv[4 * buf + 2] = r1;
+      }
+      potrf_pair_sync();
 #pragma unroll
-  for (int r = 0; r < kTile; ++r) Dinv[r][lane] = x[r];
+      for (int l = j + 2; l < kTile; ++l) {
+        const T c0 = cb[l], c1 = cb[kTile + l];
+        a[l] = fma(-li0, c0, a[l]);
+        a[l] = fma(-li1, c1, a[l]);
+      }
+    });
+  } else {
+    T x[kTile];
+#pragma unroll
+    for (int r = 0; r < kTile; ++r) x[r] = (r == lane) ? T(1) : T(0);
+    static_for<0, kTile, 2>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      potrf_pair_sync();
+      const int buf = (j >> 1) & 1;
+      const T* cb = col + buf * 2 * kTile;
+      const T r0 = piv[4 * buf], l10 = piv[4 * buf + 1], r1 = piv[4 * buf + 2];
+      x[j] *= r0;
+      x[j + 1] = fma(-l10, x[j], x[j + 1]) * r1;
+#pragma unroll
+      for (int l = j + 2; l < kTile; ++l) {
+        const T c0 = cb[l], c1 = cb[kTile + l];
+        x[l] = fma(-c0, x[j], x[l]);
+        x[l] = fma(-c1, x[j + 1], x[l]);
+      }
+    });
+#pragma unroll
+    for (int r = 0; r < kTile; ++r) Dinv[r][lane] = x[r];
+  }
   return ok;
 }
 
@@ -1665,10 +1696,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_chol_step(DevPl
   }
   // column c: factor the diagonal tile (own tile when i == c)
   __shared__ int ok_s;
-  __shared__ T colbuf[4 * kTile];
-  if (warp == 0) {
-    const bool ok = warp_potrf_inverse<T>(i == c ? A : D, Dinv, colbuf, lane);
-    if (lane == 0) ok_s = ok ? 1 : 0;
+  __shared__ T colbuf[4 * kTile + 8];
+  if (warp < 2) {
+    const bool ok = pair_potrf_inverse<T>(i == c ? A : D, Dinv, colbuf, colbuf + 4 * kTile, warp, lane);
+    if (warp == 0 && lane == 0) ok_s = ok ? 1 : 0;
   }
   __syncthreads();
   if (!ok_s) {
@@ -1768,7 +1799,7 @@ __global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
   constexpr int NB = df_batch<T>();
   enum { kIdle = 0, kUpdate = 1, kFinish = 2, kChain = 3, kExit = 4, kChain2 = 5 };
   extern __shared__ __align__(16) unsigned char df_raw[];
-  __shared__ T yv[NB][kTile], colbuf[4 * kTile];
+  __shared__ T yv[NB][kTile], colbuf[4 * kTile + 8];
   __shared__ int s_sel, s_cnt, s_mode, s_ok;
   const int p = 0;
   const ProbInfo pi = d.prob[p];
@@ -1794,9 +1825,9 @@ __global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
   // factor the diagonal tile A[t] of row i in warp 0 and publish L_ii^-1 and
   // y_i = L_ii^-1 b_i; false (after raising the abort word) on a bad pivot
   auto finish_diag = [&](int t, int i) -> bool {
-    if (warp == 0) {
-      const bool ok = warp_potrf_inverse<T>(A[t], Dinv, colbuf, lane);
-      if (lane == 0) s_ok = ok ? 1 : 0;
+    if (warp < 2) {
+      const bool ok = pair_potrf_inverse<T>(A[t], Dinv, colbuf, colbuf + 4 * kTile, warp, lane);
+      if (warp == 0 && lane == 0) s_ok = ok ? 1 : 0;
     }
     __syncthreads();
     if (!s_ok) {

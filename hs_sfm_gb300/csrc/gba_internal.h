@@ -247,6 +247,9 @@ int launch_pcg_setup(const DevPlan& d, cudaStream_t s);
 int launch_pcg_iterations(const DevPlan& d, cudaStream_t s);
 int launch_cholesky_factor(const DevPlan& d, cudaStream_t s);
 int launch_cholesky_solve(const DevPlan& d, cudaStream_t s);
+// Raises the backward solve's shared-memory limit for systems of up to
+// max_nt tile rows (before a graph capture); a GBA_* status.
+int prepare_cholesky_solve(int max_nt, int precision);
 // Tile ownership of the dataflow factorization of an nt-tile system for this
 // device, or false when it does not fit in shared memory.
 bool dataflow_layout(int nt, bool mixed, int device, int* grid, int* max_own,

@@ -2226,10 +2226,174 @@ __device__ __forceinline__ void chol_solve_body(const DevPlan& d, int q) {
   }
 }
 
+// The cluster backward solve without a cluster-wide barrier per step.
+// Rank q of the cluster owns the tile rows t = q (mod R) of y (local row
+// lt = t / R) and warp w of the rank the local rows lt = w (mod 8).  Every
+// rank keeps a slot per step j for delta_j and an mbarrier per step that
+// completes once the 32 entries of delta_j have landed in the slot.  Step j
+// (nt-1 down to 0): the warp owning row j forms delta_j = L_jj^-T y_j as
+// soon as y_j is final (its last update, from step j+1, was this warp's
+// own), and each of its lanes stores its entry into slot j of every rank
+// with st.async, which counts the bytes against that rank's mbarrier j (no
+// fence, no separate arrival).  Every warp waits on its own rank's
+// mbarrier j (acquire), then subtracts L_ji^T delta_j from its rows i < j,
+// the highest one (the next diagonal step's row when this warp owns it)
+// from registers loaded one step ahead.  The per-row arithmetic is that of the single-CTA body.
+// Slots are not reused within a launch; waits are bounded (a warp that
+// gives up records a timeout in the problem's factor flag and stops), and a
+// cluster barrier before the exit keeps every rank alive until the others
+// are done with its shared memory.
+constexpr long long kSolveSpin = 1LL << 22;
+
+template <typename T>
+__host__ __device__ constexpr size_t solve_smem_bytes(int max_nt) {
+  return size_t(max_nt) * 8 + size_t(max_nt) * kTile * sizeof(T) +
+         size_t((max_nt + kSolveRanks - 1) / kSolveRanks) * kTile * sizeof(T);
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+// An asynchronous store of v into rank `rank`'s copy of *dst that counts
+// its bytes against that rank's copy of the mbarrier b (complete_tx): a
+// waiter that sees the phase complete (acquire) sees the value.
+template <typename T>
+__device__ __forceinline__ void st_async_rank(T* dst, unsigned long long* b, int rank, T v) {
+  unsigned ra, rb;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(ra) : "r"(smem_addr(dst)), "r"(rank));
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(rb) : "r"(smem_addr(b)), "r"(rank));
+  if constexpr (sizeof(T) == 4)
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];\n" ::"r"(ra),
+                 "r"(__float_as_uint(v)), "r"(rb)
+                 : "memory");
+  else
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];\n" ::"r"(ra),
+                 "l"(__double_as_longlong(v)), "r"(rb)
+                 : "memory");
+}
+// This thread's arrival on b, announcing `bytes` of asynchronous stores.
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(b)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cluster(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void cluster_sync_acq_rel() {
+  asm volatile("barrier.cluster.arrive.aligned;\nbarrier.cluster.wait.aligned;\n" ::: "memory");
+}
+
 template <typename T>
 __global__ void __cluster_dims__(kSolveRanks, 1, 1) __launch_bounds__(256)
 k_chol_solve(DevPlan d) {
-  chol_solve_body<T, kSolveRanks>(d, int(cg::this_cluster().block_rank()));
+  constexpr int R = kSolveRanks;
+  extern __shared__ __align__(16) unsigned char solve_raw[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = int(cluster.block_rank());
+  const int p = blockIdx.y;
+  const LMState& st = d.state[p];
+  if (!st.active || d.factor_flag[p]) return;   // the same for every rank
+  const ProbInfo pi = d.prob[p];
+  const int nt = pi.nt, n = pi.n, mt = d.max_nt;
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(solve_raw);   // [mt]
+  T* xs = reinterpret_cast<T*>(bar + mt);                                         // [mt][kTile]
+  T* ys = xs + size_t(mt) * kTile;                                                // [rows][kTile]
+  const T* S = tptr<T>(d.S) + pi.s_off;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.ext_begin;
+  const T* Linv = tptr<T>(d.Linv) + (long long)p * d.max_nt * kTile * kTile;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nown = nt > q ? (nt - q + R - 1) / R : 0;
+  for (int e = tid; e < nown * kTile; e += blockDim.x) {
+    const int lt = e / kTile, r = e % kTile, t = q + R * lt;
+    ys[e] = (kTile * t + r < n) ? b[kTile * t + r] : T(0);
+  }
+  // barrier j completes when the owner's 32 stores of delta_j have landed
+  for (int j = tid; j < nt; j += blockDim.x) {
+    mbar_init(bar + j, 1);
+    mbar_arrive_expect_tx(bar + j, unsigned(kTile * sizeof(T)));
+  }
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  __syncthreads();
+  cluster_sync_acq_rel();   // every rank's barriers exist before anyone arrives on them
+  // the warp's rows, highest first: lt = lt_top, lt_top - 8, ...
+  const int lt_top = warp < nown ? warp + 8 * ((nown - 1 - warp) / 8) : -1;
+  // column `lane` of L_jj^-1 for the warp's next diagonal row
+  T lv[kTile];
+  auto fetch_linv = [&](int lt) {
+    if (lt < 0) return;
+    const T* Lv = Linv + (long long)(q + R * lt) * kTile * kTile + lane;
+#pragma unroll
+    for (int r = 0; r < kTile; ++r) lv[r] = r >= lane ? Lv[r * kTile] : T(0);
+  };
+  // L_ji (column `lane`) of the warp's highest row below j, loaded a step ahead
+  T cur[kTile];
+  int cur_lt = -1;
+  auto fetch_cur = [&](int jj) {
+    cur_lt = -1;
+    if (jj < 0 || lt_top < 0) return;
+    int lt = lt_top;
+    while (lt >= 0 && q + R * lt >= jj) lt -= 8;
+    if (lt < 0) return;
+    cur_lt = lt;
+    const int mj = tile_rows(n, jj);
+    const T* row = S + (long long)kTile * jj * n + kTile * (q + R * lt) + lane;
+#pragma unroll
+    for (int r = 0; r < kTile; ++r) cur[r] = r < mj ? row[(long long)r * n] : T(0);
+  };
+  fetch_linv(lt_top);
+  fetch_cur(nt - 1);
+  int next_diag = lt_top;   // the warp's next diagonal row (local index)
+  bool ok = true;
+  for (int j = nt - 1; j >= 0; --j) {
+    if (next_diag >= 0 && q + R * next_diag == j) {
+      __syncwarp();   // y_j's entries are this warp's own, written in step j+1
+      const T* y = ys + next_diag * kTile;
+      T sj = T(0);
+#pragma unroll
+      for (int r = 0; r < kTile; ++r) sj += lv[r] * y[r];
+      for (int rk = 0; rk < R; ++rk) st_async_rank(xs + (size_t)j * kTile + lane, bar + j, rk, sj);
+      if (kTile * j + lane < n) b[kTile * j + lane] = sj;
+      next_diag -= 8;
+      fetch_linv(next_diag);
+    }
+    long long spin = 0;
+    while (!mbar_try_wait_cluster(bar + j, 0u))
+      if (++spin > kSolveSpin) break;
+    if (spin > kSolveSpin) {   // delta_j never came
+      if (lane == 0) d.factor_flag[p] = 2;
+      ok = false;
+      break;
+    }
+    const T* xj = xs + (size_t)j * kTile;
+    if (cur_lt >= 0) {
+      T acc = T(0);
+#pragma unroll
+      for (int r = 0; r < kTile; ++r) acc += cur[r] * xj[r];
+      ys[cur_lt * kTile + lane] -= acc;
+      for (int lt = cur_lt - 8; lt >= 0; lt -= 8) {   // the warp's other rows below j
+        const int mj = tile_rows(n, j);
+        const T* row = S + (long long)kTile * j * n + kTile * (q + R * lt) + lane;
+        T a2 = T(0);
+        for (int r = 0; r < mj; ++r) a2 += row[(long long)r * n] * xj[r];
+        ys[lt * kTile + lane] -= a2;
+      }
+    }
+    fetch_cur(j - 1);
+  }
+  (void)ok;
+  __syncthreads();
+  cluster_sync_acq_rel();   // no rank leaves while another may still write into it
 }
 
 template <typename T>
@@ -2917,7 +3081,7 @@ int run_cholesky_solve(const DevPlan& d, cudaStream_t s) {
   if (d.max_nt <= kSolveSmallTiles)
     k_chol_solve_small<T><<<dim3(1u, unsigned(d.B)), 256, 0, s>>>(d);
   else
-    k_chol_solve<T><<<dim3(unsigned(kSolveRanks), unsigned(d.B)), 256, 0, s>>>(d);
+    k_chol_solve<T><<<dim3(unsigned(kSolveRanks), unsigned(d.B)), 256, solve_smem_bytes<T>(d.max_nt), s>>>(d);
   return 1;
 }
 
@@ -3053,6 +3217,20 @@ int launch_cholesky_factor(const DevPlan& d, cudaStream_t s) {
   int n = 0;
   GBA_DISPATCH(d, n = run_cholesky_factor<T>(d, s));
   return n;
+}
+
+int prepare_cholesky_solve(int max_nt, int precision) {
+  if (max_nt <= kSolveSmallTiles) return GBA_OK;
+  const bool mixed = precision == GBA_PRECISION_MIXED;
+  const size_t bytes = mixed ? solve_smem_bytes<float>(max_nt) : solve_smem_bytes<double>(max_nt);
+  if (bytes <= 48 * 1024) return GBA_OK;
+  const void* f = mixed ? reinterpret_cast<const void*>(&k_chol_solve<float>)
+                        : reinterpret_cast<const void*>(&k_chol_solve<double>);
+  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)) != cudaSuccess) {
+    cudaGetLastError();
+    return GBA_ERR_UNSUPPORTED;
+  }
+  return GBA_OK;
 }
 
 int launch_cholesky_solve(const DevPlan& d, cudaStream_t s) {

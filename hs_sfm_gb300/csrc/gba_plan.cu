@@ -1362,6 +1362,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     D.pcg_part = arena.alloc<double>(kPcgSlots * std::max<size_t>(img_chunks.size(), 1));
     D.pcg_done = arena.alloc<int>(nprob);
   }
+  if (!pcg)
+    if (int e = prepare_cholesky_solve(max_nt, opt.precision)) return e;
   if (!pcg && nprob == 1 && !opt.shared_device && max_nt >= 2) {
     int grid = 0, mo = 0;
     std::vector<int> own_off;

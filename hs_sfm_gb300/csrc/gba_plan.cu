@@ -212,21 +212,99 @@ bool cameras_free(const gba_problem& p) {
          params_per_camera(p.intrinsic_computations_mask) > 0;
 }
 
+// Page-locked host memory, pooled.  Page-locking is costly, so released
+// buffers are kept (at most kPinnedKeepBuffers of them and kPinnedKeepBytes
+// in all, the smallest dropped first) and handed to later requests that
+// fit; a request that cannot be page-locked gets nullptr (the caller then
+// uses pageable memory).
+class PinnedPool {
+ public:
+  static void* take(size_t bytes, size_t* cap) {
+    {
+      std::lock_guard<std::mutex> g(mu());
+      auto& fl = list();
+      size_t best = fl.size();
+      for (size_t i = 0; i < fl.size(); ++i)   // the smallest buffer that fits
+        if (fl[i].second >= bytes && (best == fl.size() || fl[i].second < fl[best].second)) best = i;
+      if (best < fl.size()) {
+        void* p = fl[best].first;
+        *cap = fl[best].second;
+        fl.erase(fl.begin() + long(best));
+        return p;
+      }
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    *cap = bytes;
+    return p;
+  }
+  static void give(void* p, size_t cap) {
+    if (!p) return;
+    std::lock_guard<std::mutex> g(mu());
+    auto& fl = list();
+    fl.emplace_back(p, cap);
+    for (;;) {
+      size_t total = 0, m = 0;
+      for (size_t i = 0; i < fl.size(); ++i) {
+        total += fl[i].second;
+        if (fl[i].second < fl[m].second) m = i;
+      }
+      if (fl.size() <= kPinnedKeepBuffers && total <= kPinnedKeepBytes) break;
+      cudaFreeHost(fl[m].first);
+      fl.erase(fl.begin() + long(m));
+    }
+  }
+
+ private:
+  static constexpr size_t kPinnedKeepBuffers = 16;
+  static constexpr size_t kPinnedKeepBytes = size_t(4) << 30;
+  static std::mutex& mu() {
+    static std::mutex m;
+    return m;
+  }
+  static std::vector<std::pair<void*, size_t>>& list() {
+    static auto* fl = new std::vector<std::pair<void*, size_t>>();   // outlives static destruction
+    return *fl;
+  }
+};
+
 // A host array whose elements start uninitialized: the builders write every
 // entry, so the pages are first touched by their parallel loops instead of
-// by a serial zero fill.
+// by a serial zero fill.  Arrays of a megabyte or more live in pooled
+// page-locked memory, so their uploads run at the copy engines' rate.
 template <typename T>
-struct HostBuf {
-  std::unique_ptr<T[]> p;
-  size_t n = 0;
+class HostBuf {
+ public:
   HostBuf() = default;
-  explicit HostBuf(size_t count) : p(count ? new T[count] : nullptr), n(count) {}
-  T& operator[](size_t i) { return p[i]; }
-  const T& operator[](size_t i) const { return p[i]; }
-  T* data() { return p.get(); }
-  const T* data() const { return p.get(); }
-  size_t size() const { return n; }
-  bool empty() const { return n == 0; }
+  explicit HostBuf(size_t count) : n_(count) {
+    if (!count) return;
+    if (count * sizeof(T) >= (size_t(1) << 20)) p_ = static_cast<T*>(PinnedPool::take(count * sizeof(T), &cap_));
+    if (!p_) {
+      own_.reset(new T[count]);
+      p_ = own_.get();
+      cap_ = 0;
+    }
+  }
+  ~HostBuf() {
+    if (cap_) PinnedPool::give(p_, cap_);
+  }
+  HostBuf(const HostBuf&) = delete;
+  HostBuf& operator=(const HostBuf&) = delete;
+  T& operator[](size_t i) { return p_[i]; }
+  const T& operator[](size_t i) const { return p_[i]; }
+  T* data() { return p_; }
+  const T* data() const { return p_; }
+  size_t size() const { return n_; }
+  bool empty() const { return n_ == 0; }
+
+ private:
+  size_t n_ = 0;
+  T* p_ = nullptr;
+  size_t cap_ = 0;   // page-locked capacity in bytes (0: owned pageable memory)
+  std::unique_ptr<T[]> own_;
 };
 
 // Device buffer registry.  Allocations are stream-ordered on the plan's
@@ -1900,65 +1978,6 @@ namespace {
 // Every problem's x and report in one device gather and a few copies (the
 // batch path of gba_solve_batch; the per-problem calls would synchronize the
 // stream once per problem).
-// Page-locked host staging for the x copies.  Page-locking memory is costly,
-// so released buffers are kept (up to kPinnedKeep) and reused by later
-// calls; a pageable buffer stands in when page-locked memory is refused.
-class PinnedStage {
- public:
-  explicit PinnedStage(size_t n) : n_(std::max<size_t>(n, 1)) {
-    {
-      std::lock_guard<std::mutex> g(mu());
-      auto& fl = free_list();
-      for (size_t i = 0; i < fl.size(); ++i)
-        if (fl[i].second >= n_) {
-          p_ = fl[i].first;
-          cap_ = fl[i].second;
-          fl.erase(fl.begin() + long(i));
-          return;
-        }
-    }
-    void* p = nullptr;
-    if (cudaHostAlloc(&p, n_ * sizeof(double), cudaHostAllocPortable) == cudaSuccess) {
-      p_ = static_cast<double*>(p);
-      cap_ = n_;
-    } else {
-      cudaGetLastError();
-      fallback_.resize(n_);
-    }
-  }
-  ~PinnedStage() {
-    if (!p_) return;
-    std::lock_guard<std::mutex> g(mu());
-    auto& fl = free_list();
-    fl.emplace_back(p_, cap_);
-    if (fl.size() > kPinnedKeep) {   // drop the smallest
-      size_t m = 0;
-      for (size_t i = 1; i < fl.size(); ++i)
-        if (fl[i].second < fl[m].second) m = i;
-      cudaFreeHost(fl[m].first);
-      fl.erase(fl.begin() + long(m));
-    }
-  }
-  PinnedStage(const PinnedStage&) = delete;
-  PinnedStage& operator=(const PinnedStage&) = delete;
-  double* data() { return p_ ? p_ : fallback_.data(); }
-
- private:
-  static constexpr size_t kPinnedKeep = 4;
-  static std::mutex& mu() {
-    static std::mutex m;
-    return m;
-  }
-  static std::vector<std::pair<double*, size_t>>& free_list() {
-    static auto* fl = new std::vector<std::pair<double*, size_t>>();   // outlives static destruction
-    return *fl;
-  }
-  size_t n_;
-  double* p_ = nullptr;
-  size_t cap_ = 0;
-  std::vector<double> fallback_;
-};
-
 int get_all(gba::Plan& P, double* const* xs, gba_report* reports) {
   return guarded([&] {
     GBA_CUDA(cudaStreamSynchronize(P.stream));
@@ -1966,7 +1985,7 @@ int get_all(gba::Plan& P, double* const* xs, gba_report* reports) {
     GBA_CUDA(cudaMemcpy(st.data(), P.d.state, sizeof(gba::LMState) * P.B, cudaMemcpyDeviceToHost));
     const long long np = 3LL * P.d.P, ni = 6LL * P.d.I, nc = P.d.free_cams ? 10LL * P.d.Ctot : 0;
     const size_t nx = size_t(np + ni + nc);
-    PinnedStage stage(nx);
+    gba::HostBuf<double> stage(nx);
     double* const h = stage.data();
     if (nx) {
       double* dx = P.arena.alloc<double>(nx);
@@ -2002,7 +2021,7 @@ int set_all_x0(gba::Plan& P, const double* const* xs) {
   return guarded([&] {
     const long long np = 3LL * P.d.P, ni = 6LL * P.d.I, nc = P.d.free_cams ? 10LL * P.d.Ctot : 0;
     const size_t nx = size_t(np + ni + nc);
-    PinnedStage stage(nx);
+    gba::HostBuf<double> stage(nx);
     double* const h = stage.data();
     std::fill(h + np + ni, h + nx, 0.0);   // the camera slots past each camera's parameters
     const int nth = std::min(gba::host_threads(), P.B);

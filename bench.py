@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-sample-stride", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default work-item sizes instead of gba_autotune's choice")
     ap.add_argument("--points", type=int, default=100_000)
     ap.add_argument("--images", type=int, default=200)
     ap.add_argument("--workload", default="grid",
@@ -303,8 +305,13 @@ def run_gba(args, ws, rank, local):
     precision = abi.PRECISION_MIXED if args.precision == "mixed" else abi.PRECISION_FP64
     tsz = 4 if precision == abi.PRECISION_MIXED else 8
     scene = make_scene(args, rank)
+    # work-item sizes: gba_autotune on this scene, before the timed region
+    tuning = None if args.no_autotune else gba.autotune(
+        [scene], abi.make_options(max_iterations=ITERS_PER_SOLVE, precision=precision, device=local))
+    item_sizes = {} if tuning is None else {"pair_item": tuning["pair_item"],
+                                            "image_item": tuning["image_item"]}
     opt = abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0, eps2=0.0,
-                           precision=precision, profile=0, use_cuda_graph=1, device=local)
+                           precision=precision, profile=0, use_cuda_graph=1, device=local, **item_sizes)
     plan = gba.Plan([scene], opt)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     for _ in range(args.warmup):
@@ -333,7 +340,7 @@ def run_gba(args, ws, rank, local):
     # event after every stage (those event nodes are kept out of the timed
     # plan above)
     opt_prof = abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0, eps2=0.0,
-                                precision=precision, profile=1, use_cuda_graph=1, device=local)
+                                precision=precision, profile=1, use_cuda_graph=1, device=local, **item_sizes)
     prof_plan = gba.Plan([scene], opt_prof)
     stage_tot = np.zeros(abi.NUM_STAGES)
     prof_runs = max(2, min(args.steps, 5))
@@ -410,7 +417,7 @@ def run_gba(args, ws, rank, local):
     # end to end through the C ABI with host buffers
     e2e_ms, h2d, d2h = [], 0, 0
     opt_e2e = abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0, eps2=0.0,
-                               precision=precision, device=local)
+                               precision=precision, device=local, **item_sizes)
     for _ in range(max(1, args.e2e_steps)):
         t0 = time.perf_counter()
         x, r = gba.solve(scene, opt_e2e)
@@ -447,7 +454,7 @@ def run_gba(args, ws, rank, local):
         secondary = {
             "windows": {k: w[k] for k in ("metric", "value", "unit", "ms_per_step",
                                           "speedup_vs_per_problem_fp64",
-                                          "final_cost_max_rel_diff_vs_fp64")},
+                                          "final_cost_max_rel_diff_vs_fp64", "tuning")},
             "windows_per_problem_fp64": w["per_problem_fp64"],
             "serving": {"metric": sv["metric"], "value": sv["value"], "unit": sv["unit"],
                         "p50_ms": sv["p50_ms"], "p99_ms": sv["p99_ms"],
@@ -481,6 +488,7 @@ def run_gba(args, ws, rank, local):
             "roofline_fp32": roofline_fp32,
             "roofline_hbm": roofline_hbm,
             "roofline_iteration": roofline_iteration,
+            "tuning": tuning,
             "stages": stages,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms))},
@@ -510,8 +518,13 @@ def run_windows(args, ws, rank, local):
     torch.cuda.set_device(local)
     wins = synthetic.window_batch(num_windows=args.windows, seed=3 + rank)
     K = sum(w.number_of_keys for w in wins)
+    # work-item sizes: gba_autotune on this batch, before the timed region
+    tuning = None if getattr(args, "no_autotune", False) else gba.autotune(
+        wins, abi.make_options(max_iterations=WINDOW_ITERS, precision=abi.PRECISION_MIXED, device=local))
+    item_sizes = {} if tuning is None else {"pair_item": tuning["pair_item"],
+                                            "image_item": tuning["image_item"]}
     opt = abi.make_options(max_iterations=WINDOW_ITERS, eps1=0.0, eps2=0.0,
-                           precision=abi.PRECISION_MIXED, profile=1, device=local)
+                           precision=abi.PRECISION_MIXED, profile=1, device=local, **item_sizes)
     t0 = time.perf_counter()
     plan = gba.Plan(wins, opt)
     setup_s = time.perf_counter() - t0
@@ -537,7 +550,7 @@ def run_windows(args, ws, rank, local):
     # e2e of the batch: gba_solve_batch with host buffers (structure build,
     # copies, solve, copies back)
     opt_e2e = abi.make_options(max_iterations=WINDOW_ITERS, eps1=0.0, eps2=0.0,
-                               precision=abi.PRECISION_MIXED, device=local)
+                               precision=abi.PRECISION_MIXED, device=local, **item_sizes)
     t0 = time.perf_counter()
     xs, reps = gba.solve_batch(wins, opt_e2e)
     e2e_s = time.perf_counter() - t0
@@ -571,7 +584,7 @@ def run_windows(args, ws, rank, local):
         "e2e": {"value": len(wins) / e2e_s, "unit": "solves/s", "seconds": e2e_s},
         "final_cost_max_rel_diff_vs_fp64": float(rel.max()),
         "setup_s": setup_s, "stage_ms_per_run": stages, "gpu_launches": int(launches * args.steps),
-        "clocks": clk,
+        "clocks": clk, "tuning": tuning,
     }
     del h2d
     return out

@@ -637,6 +637,9 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     std::vector<double> prior_y, prior_info;
     long long n_pairs = 0;             // key pairs (blocks built on the device)
   };
+  // work-item sizes of the Schur assembly and the image reduction
+  const int pair_item = opt.pair_item > 0 ? opt.pair_item : kPairItem;
+  const int image_item = opt.image_item > 0 ? opt.image_item : kImageItem;
   // plans without free cameras count, number and place their key pairs on
   // the device (GBA_HOST_PAIRS=1 keeps the host build, for comparison); the
   // per-code tables take 12 bytes per (image, image) entry of every problem
@@ -792,8 +795,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       out.img_item_cnt.assign(ni, 0);
       for (int i = 0; i < ni; ++i) {
         const int q0 = int(kb + ic[i]), q1 = int(kb + ic[i + 1]);
-        for (int qq = q0; qq < q1; qq += kImageItem) {
-          out.img_items.push_back(make_int4(int(ib + i), qq, std::min(q1, qq + kImageItem), q));
+        for (int qq = q0; qq < q1; qq += image_item) {
+          out.img_items.push_back(make_int4(int(ib + i), qq, std::min(q1, qq + image_item), q));
           out.img_item_cnt[i]++;
         }
       }
@@ -1124,7 +1127,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     b.blocks += nblk;
     for (long long t = 0; t < nblk; ++t) {
       const long long cntp = pc.blk_off[t + 1] - pc.blk_off[t];
-      b.items += std::max<long long>(1, (cntp + kPairItem - 1) / kPairItem);
+      b.items += std::max<long long>(1, (cntp + pair_item - 1) / pair_item);
     }
     b.blk_map += (long long)pc.blk_map.size();
     b.key_chunks += (nk + kKeyChunk - 1) / kKeyChunk;
@@ -1222,7 +1225,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       const long long s0 = b.pairs + pc.blk_off[t], s1 = b.pairs + pc.blk_off[t + 1];
       long long s_ = s0;
       do {
-        const long long e = std::min(s1, s_ + kPairItem);
+        const long long e = std::min(s1, s_ + pair_item);
         items[it++] = make_int4(block_begin + t, int(s_), int(e), q);
         s_ = e;
       } while (s_ < s1);
@@ -1867,6 +1870,9 @@ int gba_plan_create(const gba_problem* problems, const double* const* near_ys, i
   if (options->precision != GBA_PRECISION_FP64 && options->precision != GBA_PRECISION_MIXED)
     return GBA_ERR_INVALID;
   if (options->max_iterations < 0 || !(options->function_tolerance >= 0.0)) return GBA_ERR_INVALID;
+  if (options->pair_item < 0 || options->image_item < 0 || options->pair_item > (1 << 24) ||
+      options->image_item > (1 << 24))
+    return GBA_ERR_INVALID;
   gba_plan* p = nullptr;
   try {
     p = new gba_plan();
@@ -2176,6 +2182,68 @@ int gba_solve(const gba_problem* problem, const double* near_y, const gba_option
   double* xs[1] = {x_inout};
   gba_report local;
   return gba_solve_batch(problem, ys, 1, options, xs, report ? report : &local);
+}
+
+int gba_autotune(const gba_problem* problems, const double* const* near_ys, const double* const* x0,
+                 int32_t n, const gba_options* options, gba_tuning* out) {
+  if (!problems || !near_ys || !x0 || !options || !out || n <= 0) return GBA_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  gba_options base = *options;
+  base.max_iterations = std::min(std::max(options->max_iterations, 1), 2);
+  base.eps1 = -1.0;
+  base.eps2 = -1.0;
+  base.function_tolerance = 0.0;
+  base.profile = 0;
+  base.use_cuda_graph = 1;
+  int timed = 0;
+  // one candidate: a plan, a warm-up run (graph capture), the best of three
+  // timed replays, per LM iteration
+  auto time_one = [&](int pair_item, int image_item, double* ms_per_it) -> int {
+    gba_options o = base;
+    o.pair_item = pair_item;
+    o.image_item = image_item;
+    gba_plan* plan = nullptr;
+    int err = gba_plan_create(problems, near_ys, n, &o, &plan);
+    if (err) return err;
+    err = set_all_x0(plan->impl, x0);
+    double best = 0.0;
+    for (int r = 0; r < 4 && !err; ++r) {
+      err = gba_plan_run(plan);
+      if (!err) err = gba_plan_synchronize(plan);
+      float ms = 0.0f;
+      if (!err && r > 0 && cudaEventElapsedTime(&ms, plan->impl.ev0, plan->impl.ev1) == cudaSuccess)
+        best = best > 0.0 ? std::min(best, double(ms)) : double(ms);
+    }
+    gba_plan_destroy(plan);
+    if (err) return err;
+    ++timed;
+    *ms_per_it = best / base.max_iterations;
+    return GBA_OK;
+  };
+  double t_default = 0.0;
+  if (int e = time_one(gba::kPairItem, gba::kImageItem, &t_default)) return e;
+  int best_pair = gba::kPairItem, best_image = gba::kImageItem;
+  double t_best = t_default;
+  for (int pi : {256, 512, 2048, 4096}) {
+    double t = 0.0;
+    if (time_one(pi, gba::kImageItem, &t) == GBA_OK && t < t_best) {
+      t_best = t;
+      best_pair = pi;
+    }
+  }
+  for (int ii : {256, 1024}) {
+    double t = 0.0;
+    if (time_one(best_pair, ii, &t) == GBA_OK && t < t_best) {
+      t_best = t;
+      best_image = ii;
+    }
+  }
+  out->pair_item = best_pair;
+  out->image_item = best_image;
+  out->ms_per_iteration = t_best;
+  out->default_ms_per_iteration = t_default;
+  out->candidates = timed;
+  return GBA_OK;
 }
 
 // ---- single-stage entry points ---------------------------------------------

@@ -50,6 +50,7 @@ def lib():
     L.gba_default_options.argtypes = [O]
     L.gba_solve.argtypes = [P, d, O, d, R]
     L.gba_solve_batch.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(d), R]
+    L.gba_autotune.argtypes = [P, C.POINTER(d), C.POINTER(d), C.c_int32, O, C.POINTER(abi.Tuning)]
     L.gba_plan_create.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(vp)]
     L.gba_plan_destroy.argtypes = [vp]
     L.gba_plan_number_of_problems.argtypes = [vp]
@@ -127,6 +128,27 @@ def solve_batch(scenes, options=None):
     st = L.gba_solve_batch(arr, yp, len(scenes), C.byref(opt), xp, reps)
     _check(st, "gba_solve_batch")
     return xs, list(reps)
+
+
+def autotune(scenes, options=None):
+    """gba_autotune: the work-item sizes (pair_item, image_item) that run the
+    batch fastest, timed on the device; returns a dict with the choice, its
+    time per LM iteration and that of the defaults."""
+    L = lib()
+    if not isinstance(scenes, (list, tuple)):
+        scenes = [scenes]
+    cps = [abi.CProblem(s) for s in scenes]
+    arr = (abi.Problem * len(cps))(*[c.problem for c in cps])
+    ys = [_f64(s.near_y) for s in scenes]
+    x0 = [_f64(s.x0) for s in scenes]
+    yp = (C.POINTER(C.c_double) * len(ys))(*[abi.dptr(y) for y in ys])
+    xp = (C.POINTER(C.c_double) * len(x0))(*[abi.dptr(x) for x in x0])
+    opt = options if options is not None else abi.make_options()
+    t = abi.Tuning()
+    _check(L.gba_autotune(arr, yp, xp, len(scenes), C.byref(opt), C.byref(t)), "gba_autotune")
+    return {"pair_item": t.pair_item, "image_item": t.image_item,
+            "ms_per_iteration": t.ms_per_iteration,
+            "default_ms_per_iteration": t.default_ms_per_iteration, "candidates": t.candidates}
 
 
 class Plan:

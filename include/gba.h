@@ -176,8 +176,36 @@ typedef struct gba_options {
    * fraction of the cost before it (Ceres' function_tolerance,
    * camera_shared_ceres_optimizor.hpp:478); 0 disables the test. */
   double function_tolerance;
-  int32_t reserved_[4];
+  /* Work-item sizes of the two reductions split into per-warp items: key
+   * pairs per Schur-assembly item (0: 1024) and keys per image-reduction
+   * item (0: 512).  They change the grouping (and so the rounding) of the
+   * block sums, not the model; gba_autotune picks them for a batch. */
+  int32_t pair_item;
+  int32_t image_item;
+  int32_t reserved_[2];
 } gba_options;
+
+/* Autotuning of the work-item sizes (gba_options.pair_item / image_item)
+ * for a batch: every candidate builds a plan of the given problems (initial
+ * x0 per problem) with the given options (at most two LM iterations,
+ * stopping tests off, graph replay), runs it
+ * once to warm up and is timed over three graph replays (CUDA events on the
+ * plan's stream); pair_item is searched first over {256, 512, 1024, 2048,
+ * 4096} with the default image_item, then image_item over {256, 512, 1024}
+ * with the best pair_item.  out receives the fastest pair and its time per
+ * LM iteration beside that of the defaults.  A status code. */
+typedef struct gba_tuning {
+  int32_t pair_item;
+  int32_t image_item;
+  double ms_per_iteration;           /* the chosen item sizes              */
+  double default_ms_per_iteration;   /* pair_item 1024, image_item 512     */
+  int32_t candidates;                /* configurations timed               */
+  int32_t reserved_[3];
+} gba_tuning;
+
+GBA_API int gba_autotune(const gba_problem* problems, const double* const* near_ys,
+                         const double* const* x0, int32_t n, const gba_options* options,
+                         gba_tuning* out);
 
 /* Fills the defaults used by the reference's relative-pair test
  * (test_camera_shared_relative_pair.cpp:976-979): 50 iterations,

@@ -56,6 +56,7 @@ def _c_layout(tmp_path):
         "gba_options": [f for f, _ in abi.Options._fields_],
         "gba_report": [f for f, _ in abi.Report._fields_],
         "gba_triangulation": [f for f, _ in abi.Triangulation._fields_],
+        "gba_tuning": [f for f, _ in abi.Tuning._fields_],
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/gba.h"',
              'int main(void) {']
@@ -75,7 +76,8 @@ def _c_layout(tmp_path):
 def test_struct_layouts_match_header(tmp_path):
     lay = _c_layout(tmp_path)
     for name, cls in (("gba_problem", abi.Problem), ("gba_options", abi.Options),
-                      ("gba_report", abi.Report), ("gba_triangulation", abi.Triangulation)):
+                      ("gba_report", abi.Report), ("gba_triangulation", abi.Triangulation),
+                      ("gba_tuning", abi.Tuning)):
         assert int(lay[name]) == C.sizeof(cls), name
         for f, _ in cls._fields_:
             assert int(lay[f"{name}.{f}"]) == getattr(cls, f).offset, (name, f)

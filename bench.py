@@ -454,7 +454,8 @@ def run_gba(args, ws, rank, local):
         secondary = {
             "windows": {k: w[k] for k in ("metric", "value", "unit", "ms_per_step",
                                           "speedup_vs_per_problem_fp64",
-                                          "final_cost_max_rel_diff_vs_fp64", "tuning")},
+                                          "final_cost_max_rel_diff_vs_fp64", "tuning",
+                                          "stage_roofline_hbm")},
             "windows_per_problem_fp64": w["per_problem_fp64"],
             "serving": {"metric": sv["metric"], "value": sv["value"], "unit": sv["unit"],
                         "p50_ms": sv["p50_ms"], "p99_ms": sv["p99_ms"],
@@ -570,6 +571,20 @@ def run_windows(args, ws, rank, local):
     per_problem = len(sample) / per_s
     rel = np.abs(batch_costs[:len(sample)] - np.array(per_costs)) / np.array(per_costs)
     stages = {abi.STAGE_NAMES[i]: stage_tot[i] / args.steps for i in range(abi.NUM_STAGES)}
+    # per-stage HBM roofline at this scale (the same algorithmic bytes as the
+    # grid's stage table, summed over the windows; per LM iteration)
+    P_all = sum(w.number_of_points for w in wins)
+    I_all = sum(w.number_of_images for w in wins)
+    pairs_all = sum(pair_count(w) for w in wins)
+    peak, peak_kind = load_peaks()
+    sb = stage_bytes(K, P_all, I_all, pairs_all, int(np.ceil(pairs_all / 1024)) + len(wins) * 400, 4)
+    stage_roof = {}
+    for name, ms in stages.items():
+        if name in sb and ms > 0:
+            it_ms = ms / WINDOW_ITERS
+            gbs = sb[name] / (it_ms / 1e3) / 1e9
+            stage_roof[name] = {"ms_per_iteration": it_ms, "algorithmic_bytes": sb[name],
+                                "achieved_gbs": gbs, "frac": gbs / peak}
     out = {
         "metric": "batched BA solves/s", "value": batched, "unit": "solves/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)),
@@ -585,6 +600,8 @@ def run_windows(args, ws, rank, local):
         "final_cost_max_rel_diff_vs_fp64": float(rel.max()),
         "setup_s": setup_s, "stage_ms_per_run": stages, "gpu_launches": int(launches * args.steps),
         "clocks": clk, "tuning": tuning,
+        "stage_roofline_hbm": {"peak_gbs": peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                               "stages": stage_roof},
     }
     del h2d
     return out

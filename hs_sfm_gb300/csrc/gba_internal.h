@@ -142,6 +142,11 @@ struct DevPlan {
   unsigned* df_sync;         // [0] epoch of the last launch, [1] finished CTAs, [2] aborted epoch
   unsigned long long* df_trace; // optional task timeline: [grid][kDfTraceCap][4], or null
   long long df_spin_limit;   // idle polls before a CTA gives up (GBA_ERR_TIMEOUT)
+  // cluster backward solve: polls of a step's mbarrier before a warp gives
+  // up (GBA_ERR_TIMEOUT), and a step whose delta is never sent (-1: none;
+  // set only by tests, through GBA_SOLVE_DROP_STEP)
+  long long solve_spin_limit;
+  int solve_drop_step;
   // block-Jacobi PCG on the block-sparse reduced system (linear_solver PCG)
   int pcg;                   // 1: PCG instead of the dense factorization
   int pcg_max_iterations;

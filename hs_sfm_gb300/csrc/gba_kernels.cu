@@ -2238,12 +2238,13 @@ __device__ __forceinline__ void chol_solve_body(const DevPlan& d, int q) {
 // fence, no separate arrival).  Every warp waits on its own rank's
 // mbarrier j (acquire), then subtracts L_ji^T delta_j from its rows i < j,
 // the highest one (the next diagonal step's row when this warp owns it)
-// from registers loaded one step ahead.  The per-row arithmetic is that of the single-CTA body.
-// Slots are not reused within a launch; waits are bounded (a warp that
-// gives up records a timeout in the problem's factor flag and stops), and a
-// cluster barrier before the exit keeps every rank alive until the others
-// are done with its shared memory.
-constexpr long long kSolveSpin = 1LL << 22;
+// from registers loaded one step ahead.  The per-row arithmetic is that of
+// the single-CTA body.  Slots are not reused within a launch.  Waits are bounded
+// (DevPlan::solve_spin_limit polls): a warp that gives up records a timeout
+// in the problem's factor flag (the solve is void) and stops updating, but
+// still sends its own deltas of the later steps; after a cluster barrier
+// (every store issued) it waits, bounded again, for the stores into its rank
+// that are still landing, so no CTA leaves while another writes into it.
 
 template <typename T>
 __host__ __device__ constexpr size_t solve_smem_bytes(int max_nt) {
@@ -2294,10 +2295,16 @@ __device__ __forceinline__ void cluster_sync_acq_rel() {
   asm volatile("barrier.cluster.arrive.aligned;\nbarrier.cluster.wait.aligned;\n" ::: "memory");
 }
 
-template <typename T>
+constexpr long long kSolveSpin = 1LL << 22;   // polls of a step's mbarrier (production)
+
+// kProbe: the instantiation that reads the test controls of DevPlan
+// (solve_spin_limit, solve_drop_step); production plans launch the other.
+template <typename T, bool kProbe>
 __global__ void __cluster_dims__(kSolveRanks, 1, 1) __launch_bounds__(256)
 k_chol_solve(DevPlan d) {
   constexpr int R = kSolveRanks;
+  const long long spin_limit = kProbe ? d.solve_spin_limit : kSolveSpin;
+  const int drop_step = kProbe ? d.solve_drop_step : -1;
   extern __shared__ __align__(16) unsigned char solve_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int q = int(cluster.block_rank());
@@ -2354,7 +2361,7 @@ k_chol_solve(DevPlan d) {
   fetch_linv(lt_top);
   fetch_cur(nt - 1);
   int next_diag = lt_top;   // the warp's next diagonal row (local index)
-  bool ok = true;
+  int j_fail = -1;
   for (int j = nt - 1; j >= 0; --j) {
     if (next_diag >= 0 && q + R * next_diag == j) {
       __syncwarp();   // y_j's entries are this warp's own, written in step j+1
@@ -2362,17 +2369,18 @@ k_chol_solve(DevPlan d) {
       T sj = T(0);
 #pragma unroll
       for (int r = 0; r < kTile; ++r) sj += lv[r] * y[r];
-      for (int rk = 0; rk < R; ++rk) st_async_rank(xs + (size_t)j * kTile + lane, bar + j, rk, sj);
+      if (j != drop_step)
+        for (int rk = 0; rk < R; ++rk) st_async_rank(xs + (size_t)j * kTile + lane, bar + j, rk, sj);
       if (kTile * j + lane < n) b[kTile * j + lane] = sj;
       next_diag -= 8;
       fetch_linv(next_diag);
     }
     long long spin = 0;
     while (!mbar_try_wait_cluster(bar + j, 0u))
-      if (++spin > kSolveSpin) break;
-    if (spin > kSolveSpin) {   // delta_j never came
+      if (++spin > spin_limit) break;
+    if (spin > spin_limit) {   // delta_j did not come: the solve is void
       if (lane == 0) d.factor_flag[p] = 2;
-      ok = false;
+      j_fail = j;
       break;
     }
     const T* xj = xs + (size_t)j * kTile;
@@ -2391,9 +2399,28 @@ k_chol_solve(DevPlan d) {
     }
     fetch_cur(j - 1);
   }
-  (void)ok;
+  if (j_fail >= 0) {
+    // the warp gave up at step j_fail: it still sends its own deltas of the
+    // steps below (void values), so every delta another warp waits for is sent
+    for (int j = j_fail - 1; j >= 0; --j) {
+      if (next_diag >= 0 && q + R * next_diag == j) {
+        if (j != drop_step)
+          for (int rk = 0; rk < R; ++rk) st_async_rank(xs + (size_t)j * kTile + lane, bar + j, rk, T(0));
+        next_diag -= 8;
+      }
+    }
+  }
   __syncthreads();
-  cluster_sync_acq_rel();   // no rank leaves while another may still write into it
+  cluster_sync_acq_rel();   // every rank has issued all of its stores
+  if (j_fail >= 0) {
+    // wait (bounded) for the stores into this rank that are still landing
+    // before the CTA may leave
+    for (int j = 0; j < nt; ++j) {
+      long long spin = 0;
+      while (!mbar_try_wait_cluster(bar + j, 0u) && ++spin <= spin_limit) {
+      }
+    }
+  }
 }
 
 template <typename T>
@@ -3080,8 +3107,10 @@ template <typename T>
 int run_cholesky_solve(const DevPlan& d, cudaStream_t s) {
   if (d.max_nt <= kSolveSmallTiles)
     k_chol_solve_small<T><<<dim3(1u, unsigned(d.B)), 256, 0, s>>>(d);
+  else if (d.solve_drop_step >= 0 || d.solve_spin_limit != kSolveSpin)
+    k_chol_solve<T, true><<<dim3(unsigned(kSolveRanks), unsigned(d.B)), 256, solve_smem_bytes<T>(d.max_nt), s>>>(d);
   else
-    k_chol_solve<T><<<dim3(unsigned(kSolveRanks), unsigned(d.B)), 256, solve_smem_bytes<T>(d.max_nt), s>>>(d);
+    k_chol_solve<T, false><<<dim3(unsigned(kSolveRanks), unsigned(d.B)), 256, solve_smem_bytes<T>(d.max_nt), s>>>(d);
   return 1;
 }
 
@@ -3224,12 +3253,15 @@ int prepare_cholesky_solve(int max_nt, int precision) {
   const bool mixed = precision == GBA_PRECISION_MIXED;
   const size_t bytes = mixed ? solve_smem_bytes<float>(max_nt) : solve_smem_bytes<double>(max_nt);
   if (bytes <= 48 * 1024) return GBA_OK;
-  const void* f = mixed ? reinterpret_cast<const void*>(&k_chol_solve<float>)
-                        : reinterpret_cast<const void*>(&k_chol_solve<double>);
-  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)) != cudaSuccess) {
-    cudaGetLastError();
-    return GBA_ERR_UNSUPPORTED;
-  }
+  const void* f[2] = {mixed ? reinterpret_cast<const void*>(&k_chol_solve<float, false>)
+                            : reinterpret_cast<const void*>(&k_chol_solve<double, false>),
+                      mixed ? reinterpret_cast<const void*>(&k_chol_solve<float, true>)
+                            : reinterpret_cast<const void*>(&k_chol_solve<double, true>)};
+  for (const void* fn : f)
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)) != cudaSuccess) {
+      cudaGetLastError();
+      return GBA_ERR_UNSUPPORTED;
+    }
   return GBA_OK;
 }
 

@@ -1445,6 +1445,19 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   }
   if (!pcg)
     if (int e = prepare_cholesky_solve(max_nt, opt.precision)) return e;
+  // bounded waits of the cluster backward solve; GBA_SOLVE_SPIN_LIMIT lowers
+  // the limit and GBA_SOLVE_DROP_STEP withholds one step's delta, to test
+  // that path
+  D.solve_spin_limit = 1LL << 22;
+  D.solve_drop_step = -1;
+  if (const char* sl = std::getenv("GBA_SOLVE_SPIN_LIMIT")) {
+    const long long v = std::atoll(sl);
+    if (v > 0) D.solve_spin_limit = v;
+  }
+  if (const char* ds = std::getenv("GBA_SOLVE_DROP_STEP")) {
+    const int v = std::atoi(ds);
+    if (v >= 0) D.solve_drop_step = v;
+  }
   if (!pcg && nprob == 1 && !opt.shared_device && max_nt >= 2) {
     int grid = 0, mo = 0;
     std::vector<int> own_off;

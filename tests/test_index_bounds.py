@@ -77,29 +77,36 @@ class Batch:
             if i == c:
                 self.check_linv(p, c)
 
-    def solve(self, p, ranks=8, max_rows=(6 * 2048 // TILE + 7) // 8):
-        n, nt = self.n[p], self.nt[p]
+    def solve(self, p, ranks=8, warps=8):
+        """k_chol_solve: rank q owns tile rows t = q (mod ranks), local row
+        lt = t // ranks; warp w owns the local rows lt = w (mod warps).  The
+        dynamic shared memory holds max_nt mbarriers, max_nt delta slots of
+        TILE entries and ceil(max_nt / ranks) rows of y."""
+        n, nt, mt = self.n[p], self.nt[p], self.max_nt
+        slots, y_rows = mt, (mt + ranks - 1) // ranks
+        owner = {}
         for q in range(ranks):
             nown = (nt - q + ranks - 1) // ranks if nt > q else 0
-            assert nown <= max_rows
+            assert nown <= y_rows
             for lt in range(nown):                    # ys load
                 t = q + ranks * lt
                 self.check_b(p, TILE * t, rows(n, t))
-            jown = nt - 1 - ((nt - 1 - q) % ranks)
-            owned = []
-            while jown >= 0:
-                owned.append(jown)
-                jown -= ranks
-            assert all(j % ranks == q for j in owned)
-            for j in owned:                           # delta_j and L_jj^-1
-                self.check_linv(p, j)
-                self.check_b(p, TILE * j, rows(n, j))
-            for j in range(nt - 1, -1, -1):
-                nact = (j - q + ranks - 1) // ranks if j > q else 0
-                for lt in range(nact):
-                    i = q + ranks * lt
-                    assert i < j and lt < nown
-                    self.check_S(p, TILE * j, rows(n, j), TILE * i, TILE)
+            for w in range(warps):
+                mine = [lt for lt in range(w, nown, warps)]
+                for lt in mine:                       # delta of the warp's rows
+                    t = q + ranks * lt
+                    assert t not in owner
+                    owner[t] = (q, w)
+                    self.check_linv(p, t)
+                    self.check_b(p, TILE * t, rows(n, t))
+                for j in range(nt - 1, -1, -1):
+                    assert j < slots                  # slot j and mbarrier j
+                    below = [lt for lt in mine if q + ranks * lt < j]
+                    for lt in below:                  # L_ji^T delta_j into row i
+                        i = q + ranks * lt
+                        assert lt < y_rows and i < j and i <= nt - 2   # tile i is full
+                        self.check_S(p, TILE * j, rows(n, j), TILE * i, TILE)
+        assert sorted(owner) == list(range(nt))       # every step has one owner
 
     def run(self):
         touched = 0

@@ -365,6 +365,8 @@ struct Plan {
   std::vector<int64_t> x_size;
   // run state
   cudaGraphExec_t graph_exec = nullptr;
+  cudaGraphExec_t iter_exec = nullptr;   // one LM iteration (one-shot solves)
+  long long iter_launches = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ran = false;
   long long launches_last_run = 0;
@@ -403,6 +405,7 @@ struct Plan {
 
   ~Plan() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (iter_exec) cudaGraphExecDestroy(iter_exec);
     for (cudaEvent_t e : prof_events) cudaEventDestroy(e);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -412,7 +415,10 @@ struct Plan {
 
   int build(const gba_problem* problems, const double* const* near_ys, int nprob,
             const gba_options* options);
-  void enqueue(bool profile);
+  // parts of the launch sequence: everything, the prologue (initial cost
+  // and linearization) or one LM iteration
+  enum Part { kAll, kPrologue, kIteration };
+  void enqueue(bool profile, Part part = kAll);
   int run();
   int sync();
 };
@@ -1597,9 +1603,11 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
 
 // The launch sequence of one solve.  When profiling, an event is recorded
 // after each stage and tagged with it.
-void Plan::enqueue(bool profile) {
+void Plan::enqueue(bool profile, Part part) {
   cudaStream_t s = stream;
   long long n = 0;
+  const bool prologue = part != kIteration;
+  const int iterations = part == kAll ? opt.max_iterations : (part == kIteration ? 1 : 0);
   size_t ev_i = 0;
   auto mark = [&](int stage) {
     if (!profile) return;
@@ -1612,22 +1620,24 @@ void Plan::enqueue(bool profile) {
     prof_stage[ev_i] = stage;
     ++ev_i;
   };
-  mark(-1);
-  n += launch_init(d, s);
-  mark(GBA_STAGE_CONTROL);
-  n += launch_image_prep(d, 0, s);
-  mark(GBA_STAGE_IMAGE_PREP);
-  n += launch_cost(d, 0, s);
-  mark(GBA_STAGE_COST);
-  n += launch_ctrl_initial_cost(d, s);
-  mark(GBA_STAGE_CONTROL);
-  n += launch_linearize(d, s);
-  mark(GBA_STAGE_LINEARIZE);
-  n += launch_image_reduce(d, s);
-  mark(GBA_STAGE_IMAGE_REDUCE);
-  n += launch_ctrl_after_linearize(d, s);
-  mark(GBA_STAGE_CONTROL);
-  for (int it = 0; it < opt.max_iterations; ++it) {
+  if (prologue) {
+    mark(-1);
+    n += launch_init(d, s);
+    mark(GBA_STAGE_CONTROL);
+    n += launch_image_prep(d, 0, s);
+    mark(GBA_STAGE_IMAGE_PREP);
+    n += launch_cost(d, 0, s);
+    mark(GBA_STAGE_COST);
+    n += launch_ctrl_initial_cost(d, s);
+    mark(GBA_STAGE_CONTROL);
+    n += launch_linearize(d, s);
+    mark(GBA_STAGE_LINEARIZE);
+    n += launch_image_reduce(d, s);
+    mark(GBA_STAGE_IMAGE_REDUCE);
+    n += launch_ctrl_after_linearize(d, s);
+    mark(GBA_STAGE_CONTROL);
+  }
+  for (int it = 0; it < iterations; ++it) {
     n += launch_point_schur(d, s);
     mark(GBA_STAGE_POINT_SCHUR);
     n += launch_assemble_items(d, s);
@@ -1697,6 +1707,28 @@ int Plan::run() {
       cudaGraphDestroy(g);
     }
     GBA_CUDA(cudaGraphLaunch(graph_exec, stream));
+  } else if (!profile && opt.max_iterations > 0) {
+    // one-shot: the prologue launched directly, then one LM iteration
+    // captured once (its launches do not depend on the iteration) and
+    // replayed max_iterations times
+    enqueue(false, kPrologue);
+    const long long pro = launches_last_run;
+    if (!iter_exec) {
+      cudaGraph_t g;
+      GBA_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        enqueue(false, kIteration);
+      } catch (...) {
+        cudaStreamEndCapture(stream, &g);
+        throw;
+      }
+      GBA_CUDA(cudaStreamEndCapture(stream, &g));
+      GBA_CUDA(cudaGraphInstantiate(&iter_exec, g, 0));
+      cudaGraphDestroy(g);
+      iter_launches = launches_last_run;
+    }
+    for (int it = 0; it < opt.max_iterations; ++it) GBA_CUDA(cudaGraphLaunch(iter_exec, stream));
+    launches_last_run = pro + iter_launches * opt.max_iterations;
   } else {
     enqueue(profile);
   }
@@ -2154,8 +2186,9 @@ int gba_batch_destroy(gba_batch* b) { return gba_plan_destroy(b); }
 int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, int32_t n,
                     const gba_options* options, double* const* x_inout, gba_report* reports) {
   if (!x_inout || !options) return GBA_ERR_INVALID;
-  // A one-shot solve runs its launch sequence once: capturing it into a
-  // CUDA graph would cost more than it saves, so it is launched directly.
+  // A one-shot solve runs its launch sequence once: capturing all of it into
+  // a CUDA graph would cost more than it saves, so the plan captures one LM
+  // iteration and replays it.
   gba_options once = *options;
   once.use_cuda_graph = 0;
   // GBA_BUILD_TIMING=1 prints the phases of the call to stderr

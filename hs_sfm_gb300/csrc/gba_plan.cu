@@ -2185,7 +2185,13 @@ int gba_batch_destroy(gba_batch* b) { return gba_plan_destroy(b); }
 
 int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, int32_t n,
                     const gba_options* options, double* const* x_inout, gba_report* reports) {
-  if (!x_inout || !options) return GBA_ERR_INVALID;
+  return gba_solve_batch_into(problems, near_ys, n, options, x_inout, x_inout, reports);
+}
+
+int gba_solve_batch_into(const gba_problem* problems, const double* const* near_ys, int32_t n,
+                         const gba_options* options, const double* const* x0, double* const* x_out,
+                         gba_report* reports) {
+  if (!x0 || !x_out || !options) return GBA_ERR_INVALID;
   // A one-shot solve runs its launch sequence once: capturing all of it into
   // a CUDA graph would cost more than it saves, so the plan captures one LM
   // iteration and replays it.
@@ -2204,14 +2210,14 @@ int gba_solve_batch(const gba_problem* problems, const double* const* near_ys, i
   if (err) return err;
   phase("plan built");
   for (int q = 0; q < n && !err; ++q)
-    if (!x_inout[q] && plan->impl.x_size[q] > 0) err = GBA_ERR_INVALID;
-  if (!err) err = set_all_x0(plan->impl, x_inout);
+    if ((!x0[q] || !x_out[q]) && plan->impl.x_size[q] > 0) err = GBA_ERR_INVALID;
+  if (!err) err = set_all_x0(plan->impl, x0);
   phase("x0 uploaded");
   if (!err) err = gba_plan_run(plan);
   phase("launched");
   if (!err) err = gba_plan_synchronize(plan);
   phase("solved");
-  if (!err) err = get_all(plan->impl, x_inout, reports);
+  if (!err) err = get_all(plan->impl, x_out, reports);
   phase("x read back");
   int first_status = GBA_OK;
   if (!err && reports)

@@ -50,6 +50,7 @@ def lib():
     L.gba_default_options.argtypes = [O]
     L.gba_solve.argtypes = [P, d, O, d, R]
     L.gba_solve_batch.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(d), R]
+    L.gba_solve_batch_into.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(d), C.POINTER(d), R]
     L.gba_autotune.argtypes = [P, C.POINTER(d), C.POINTER(d), C.c_int32, O, C.POINTER(abi.Tuning)]
     L.gba_plan_create.argtypes = [P, C.POINTER(d), C.c_int32, O, C.POINTER(vp)]
     L.gba_plan_destroy.argtypes = [vp]
@@ -120,13 +121,17 @@ def solve_batch(scenes, options=None):
     cps = [abi.CProblem(s) for s in scenes]
     arr = (abi.Problem * len(cps))(*[c.problem for c in cps])
     ys = [_f64(s.near_y) for s in scenes]
-    xs = [_f64(s.x0).copy() for s in scenes]
+    x0 = [_f64(s.x0) for s in scenes]
+    # results in fresh arrays (the library's parallel scatter touches them
+    # first); the scenes' x0 are read in place
+    xs = [np.empty(c.x_size) for c in cps]
     yp = (C.POINTER(C.c_double) * len(ys))(*[abi.dptr(y) for y in ys])
+    x0p = (C.POINTER(C.c_double) * len(x0))(*[abi.dptr(x) for x in x0])
     xp = (C.POINTER(C.c_double) * len(xs))(*[abi.dptr(x) for x in xs])
     reps = (abi.Report * len(scenes))()
     opt = options if options is not None else abi.make_options()
-    st = L.gba_solve_batch(arr, yp, len(scenes), C.byref(opt), xp, reps)
-    _check(st, "gba_solve_batch")
+    st = L.gba_solve_batch_into(arr, yp, len(scenes), C.byref(opt), x0p, xp, reps)
+    _check(st, "gba_solve_batch_into")
     return xs, list(reps)
 
 

@@ -318,6 +318,11 @@ GBA_API int gba_plan_device_bytes(gba_plan* plan, int64_t* bytes);
 GBA_API int gba_solve_batch(const gba_problem* problems, const double* const* near_ys,
                     int32_t number_of_problems, const gba_options* options,
                     double* const* x_inout, gba_report* reports);
+/* The same with the initial x and the result in separate buffers (x_out[q]
+ * may be x0[q]): a caller that keeps its x0 needs no copy of it. */
+GBA_API int gba_solve_batch_into(const gba_problem* problems, const double* const* near_ys,
+                                 int32_t number_of_problems, const gba_options* options,
+                                 const double* const* x0, double* const* x_out, gba_report* reports);
 
 /* ---- single-stage entry points (the trait plug-ins of
  * camera_shared_nllso_meta_levenberg_marquardt.hpp:33-106), used for parity

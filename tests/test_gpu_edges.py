@@ -93,3 +93,28 @@ def test_dense_size_limit(gba):
     assert e.value.status == abi.GBA_ERR_UNSUPPORTED
     _, rp = gba.solve(s2, abi.make_options(linear_solver=abi.LINEAR_PCG, **opt))
     assert rp.status == abi.GBA_OK
+
+
+def test_solve_batch_into_keeps_x0_and_matches_in_place(gba):
+    # gba_solve_batch_into reads x0 and writes separate outputs: the same
+    # bits as the in-place gba_solve_batch, and the callers' x0 untouched
+    import ctypes as C
+    scenes = [synthetic.ring_scene(num_images=n, num_points=200 * n, obs_per_point=3, seed=70 + n)
+              for n in (4, 7)]
+    keep = [s.x0.copy() for s in scenes]
+    opt = abi.make_options(**OPT)
+    xs, reps = gba.solve_batch(scenes, opt)              # through gba_solve_batch_into
+    for s, k in zip(scenes, keep):
+        np.testing.assert_array_equal(s.x0, k)
+    L = gba.lib()
+    cps = [abi.CProblem(s) for s in scenes]
+    arr = (abi.Problem * len(cps))(*[c.problem for c in cps])
+    ys = [np.ascontiguousarray(s.near_y, dtype=np.float64) for s in scenes]
+    xi = [np.ascontiguousarray(s.x0, dtype=np.float64).copy() for s in scenes]
+    yp = (C.POINTER(C.c_double) * 2)(*[abi.dptr(y) for y in ys])
+    xp = (C.POINTER(C.c_double) * 2)(*[abi.dptr(x) for x in xi])
+    reps2 = (abi.Report * 2)()
+    assert L.gba_solve_batch(arr, yp, 2, C.byref(opt), xp, reps2) == abi.GBA_OK
+    for a, b, r, r2 in zip(xs, xi, reps, reps2):
+        np.testing.assert_array_equal(a, b)
+        assert r.final_cost == r2.final_cost

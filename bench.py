@@ -624,6 +624,11 @@ def run_walk(args, ws, rank, local):
     common = dict(max_iterations=WALK_ITERS, eps1=0.0, eps2=0.0, loss=abi.LOSS_HUBER, huber_delta=1.0,
                   linear_solver=abi.LINEAR_PCG, pcg_relative_tolerance=1e-6, pcg_max_iterations=100,
                   device=local)
+    # work-item sizes: gba_autotune on this scene, before the timed region
+    tuning = None if getattr(args, "no_autotune", False) else gba.autotune(
+        [scene], abi.make_options(precision=abi.PRECISION_MIXED, **common))
+    if tuning is not None:
+        common.update(pair_item=tuning["pair_item"], image_item=tuning["image_item"])
     plan = gba.Plan(scene, abi.make_options(precision=abi.PRECISION_MIXED, profile=1, **common))
     dev_bytes = plan.device_bytes()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -668,7 +673,7 @@ def run_walk(args, ws, rank, local):
         "stage_ms_per_iteration": stages,
         "e2e": {"value": WALK_ITERS / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(re2e.h2d_bytes),
                 "d2h_bytes_per_step": int(re2e.d2h_bytes), "ms_per_step": 1e3 * e2e_s},
-        "gpu_launches": int(launches * args.steps), "clocks": clk,
+        "gpu_launches": int(launches * args.steps), "clocks": clk, "tuning": tuning,
         "cpu_baseline": None,
         "cpu_baseline_note": ("the reference's O(I^2 P) reduced-system loop is not timeable at 2000 "
                               "images (about 2e12 block lookups per iteration)"),

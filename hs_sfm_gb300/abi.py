@@ -129,6 +129,15 @@ class Report(C.Structure):
         return d
 
 
+class PlanStructure(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "problems", "keys", "points", "images", "key_pairs", "pair_items", "blocks",
+        "image_items", "camera_records", "max_reduced_size")] + [("reserved_", C.c_int64 * 4)]
+
+    def as_dict(self):
+        return {name: int(getattr(self, name)) for name, _ in self._fields_ if name != "reserved_"}
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("solve", Options), ("memory_budget_bytes", C.c_int64), ("max_batch", C.c_int32),
                 ("max_in_flight", C.c_int32), ("reserved_", C.c_int32 * 6)]

@@ -6,9 +6,10 @@
 // or an arena it accounts for), code paths between a framework's allocator
 // teardown and process exit, or hosts that forbid device allocations after
 // start-up.  The caller passes device pointers for every input and for the
-// output; the temporaries of the computation (one rotation matrix per image
-// and one partial sum per block) live in the fixed array g_noalloc_scratch
-// below, which every GPU that loads libgba.so holds until the process exits.
+// output; the temporaries of the computation (one rotation matrix per image,
+// one partial sum per block and a count of rejected keys) live in the fixed
+// array g_noalloc_scratch below, which every GPU that loads libgba.so holds
+// until the process exits.
 //
 // Limits and sharing rules:
 //   - at most GBA_NOALLOC_MAX_IMAGES images per call; larger problems are
@@ -16,13 +17,16 @@
 //   - every call on a device uses the same scratch array, and it keeps the
 //     last call's contents.  Calls whose kernels overlap on the GPU (two
 //     streams, or two host threads) race on it: serialize them;
-//   - the first call on a device resolves the scratch array's device address
-//     with cudaGetSymbolAddress (once per device, with that device current);
-//     make that first call before any stream capture.
+//   - every call looks up the scratch array's device address with
+//     cudaGetSymbolAddress on the current device (so a device reset or a new
+//     primary context never leaves a stale address behind); the first call
+//     on a device also loads the library's kernels there, so make it before
+//     any stream capture;
+//   - a key whose image, point or camera id is out of range is skipped and
+//     counted on the device, and the cost written is then NaN.
 #include "gba_internal.h"
 
 #include <cmath>
-#include <mutex>
 
 namespace gba {
 namespace {
@@ -30,13 +34,11 @@ namespace {
 constexpr int kNoAllocBlocks = 1024;     // grid of the cost kernel (partials)
 constexpr int kNoAllocThreads = 256;
 constexpr long long kRotDoubles = 12LL * GBA_NOALLOC_MAX_IMAGES;
-constexpr long long kScratchDoubles = kRotDoubles + kNoAllocBlocks;
+// rotations, block partials, then one word counting the rejected keys
+constexpr long long kScratchDoubles = kRotDoubles + kNoAllocBlocks + 1;
 
-// The scratch: image rotations [12 * max images] then block partials.
+// The scratch: image rotations [12 * max images], block partials, bad-key count.
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
-
-double* g_scratch_ptr[64] = {};
-std::mutex g_scratch_mutex;
 
 __device__ __forceinline__ double na_warp_sum(double v) {
 #pragma unroll
@@ -44,8 +46,9 @@ __device__ __forceinline__ double na_warp_sum(double v) {
   return v;
 }
 
-__global__ void k_na_rotations(gba_device_problem p, double* rot) {
+__global__ void k_na_rotations(gba_device_problem p, double* rot, unsigned long long* bad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *bad = 0ull;  // cleared before the cost kernel runs (same stream)
   if (i >= p.number_of_images) return;
   const double* x = p.images + 6LL * i;
   const double r0 = x[0], r1 = x[1], r2 = x[2];
@@ -64,19 +67,32 @@ __global__ void k_na_rotations(gba_device_problem p, double* rot) {
   R[9] = x[3]; R[10] = x[4]; R[11] = x[5];
 }
 
-// Grid-stride variant of the cost kernel: one FP64 partial per block.
+// Grid-stride variant of the cost kernel: one FP64 partial per block.  Every
+// index read from the caller's arrays is checked before it is used; a key
+// that fails is skipped and counted in *bad.
 __global__ void __launch_bounds__(kNoAllocThreads) k_na_cost(gba_device_problem p, int loss,
                                                              double delta, const double* rot,
-                                                             double* partial) {
+                                                             double* partial,
+                                                             unsigned long long* bad) {
   __shared__ double red[kNoAllocThreads / 32];
   double acc = 0.0;
+  unsigned long long rejected = 0;
   const long long K = p.number_of_keys;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < K;
        k += (long long)gridDim.x * blockDim.x) {
     const int img = p.key_image[k], pt = p.key_point[k];
+    if (img < 0 || img >= p.number_of_images || pt < 0 || pt >= p.number_of_points) {
+      ++rejected;
+      continue;
+    }
+    const int c = p.image_camera[img];
+    if (c < 0 || c >= p.number_of_cameras) {
+      ++rejected;
+      continue;
+    }
     const double* R = rot + 12LL * img;
     const double* X = p.points + 3LL * pt;
-    const double* cam = p.cameras + 10LL * p.image_camera[img];
+    const double* cam = p.cameras + 10LL * c;
     const double y0 = R[0] * X[0] + R[1] * X[1] + R[2] * X[2] + R[9];
     const double y1 = R[3] * X[0] + R[4] * X[1] + R[5] * X[2] + R[10];
     const double y2 = R[6] * X[0] + R[7] * X[1] + R[8] * X[2] + R[11];
@@ -96,6 +112,7 @@ __global__ void __launch_bounds__(kNoAllocThreads) k_na_cost(gba_device_problem 
     else
       acc += s;
   }
+  if (rejected) atomicAdd(bad, rejected);
   acc = na_warp_sum(acc);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
@@ -106,35 +123,28 @@ __global__ void __launch_bounds__(kNoAllocThreads) k_na_cost(gba_device_problem 
   }
 }
 
-__global__ void k_na_final(const double* partial, int n, double* out) {
+__global__ void k_na_final(const double* partial, int n, const unsigned long long* bad,
+                           double* out) {
   double v = 0.0;
   for (int i = threadIdx.x; i < n; i += 32) v += partial[i];
   v = na_warp_sum(v);
-  if (threadIdx.x == 0) *out = v;
+  if (threadIdx.x == 0) *out = *bad ? nan("") : v;
 }
 
-// Device address of the scratch array on the current device (resolved once
-// per device).
+// Device address of the scratch array on the current device.
 double* scratch_on_current_device(int* status) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-    cudaGetLastError();
+  if (cudaGetDevice(&dev) != cudaSuccess) {
     *status = GBA_ERR_NO_DEVICE;
     return nullptr;
   }
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) {
-      cudaGetLastError();
-      *status = GBA_ERR_CUDA;
-      return nullptr;
-    }
-    g_scratch_ptr[dev] = static_cast<double*>(ptr);
+  void* ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
+    *status = GBA_ERR_CUDA;
+    return nullptr;
   }
   *status = GBA_OK;
-  return g_scratch_ptr[dev];
+  return static_cast<double*>(ptr);
 }
 
 }  // namespace
@@ -148,8 +158,13 @@ extern "C" int gba_cost_noalloc(const gba_device_problem* problem, int32_t loss,
       p.number_of_cameras < 0)
     return GBA_ERR_INVALID;
   if (p.number_of_images > GBA_NOALLOC_MAX_IMAGES) return GBA_ERR_INVALID;
-  if (p.number_of_keys > 0 && (!p.key_image || !p.key_point || !p.keys || !p.points ||
-                               !p.images || !p.image_camera || !p.cameras))
+  // Every array a launch may read must be there: the rotations read images,
+  // the cost kernel reads the key arrays and, through them, the rest.
+  if (p.number_of_images > 0 && !p.images) return GBA_ERR_INVALID;
+  if (p.number_of_keys > 0 &&
+      (!p.key_image || !p.key_point || !p.keys || !p.points || !p.images || !p.image_camera ||
+       !p.cameras || p.number_of_images == 0 || p.number_of_points == 0 ||
+       p.number_of_cameras == 0))
     return GBA_ERR_INVALID;
   if (loss != GBA_LOSS_TRIVIAL && loss != GBA_LOSS_HUBER) return GBA_ERR_INVALID;
   int status = GBA_OK;
@@ -158,13 +173,32 @@ extern "C" int gba_cost_noalloc(const gba_device_problem* problem, int32_t loss,
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   double* rot = scratch;
   double* partial = scratch + gba::kRotDoubles;
-  if (p.number_of_images > 0)
-    gba::k_na_rotations<<<(p.number_of_images + 127) / 128, 128, 0, s>>>(p, rot);
+  unsigned long long* bad =
+      reinterpret_cast<unsigned long long*>(scratch + gba::kRotDoubles + gba::kNoAllocBlocks);
   long long need = (p.number_of_keys + gba::kNoAllocThreads - 1) / gba::kNoAllocThreads;
   int blocks = int(need < gba::kNoAllocBlocks ? need : gba::kNoAllocBlocks);
   if (blocks < 1) blocks = 1;
-  gba::k_na_cost<<<blocks, gba::kNoAllocThreads, 0, s>>>(p, loss, huber_delta, rot, partial);
-  gba::k_na_final<<<1, 32, 0, s>>>(partial, blocks, d_cost);
-  if (cudaGetLastError() != cudaSuccess) return GBA_ERR_CUDA;
+  // Each launch's own status (cudaLaunchKernel returns it) decides the
+  // result, so an earlier error of the caller's is neither reported as this
+  // call's nor cleared.
+  gba_device_problem pv = p;
+  int rot_blocks = p.number_of_images > 0 ? (p.number_of_images + 127) / 128 : 1;
+  void* a_rot[] = {&pv, &rot, &bad};
+  if (cudaLaunchKernel((const void*)gba::k_na_rotations, dim3(rot_blocks), dim3(128), a_rot, 0,
+                       s) != cudaSuccess)
+    return GBA_ERR_CUDA;
+  int lossv = loss;
+  double delta = huber_delta;
+  void* a_cost[] = {&pv, &lossv, &delta, &rot, &partial, &bad};
+  if (cudaLaunchKernel((const void*)gba::k_na_cost, dim3(blocks), dim3(gba::kNoAllocThreads),
+                       a_cost, 0, s) != cudaSuccess)
+    return GBA_ERR_CUDA;
+  const double* cpartial = partial;
+  const unsigned long long* cbad = bad;
+  void* a_fin[] = {&cpartial, &blocks, &cbad, &d_cost};
+  if (cudaLaunchKernel((const void*)gba::k_na_final, dim3(1), dim3(32), a_fin, 0, s) !=
+      cudaSuccess)
+    return GBA_ERR_CUDA;
+  gba::count_launches(3);
   return GBA_OK;
 }

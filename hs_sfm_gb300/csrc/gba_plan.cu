@@ -379,6 +379,7 @@ struct Plan {
   int stage_launches[GBA_NUM_STAGES] = {};
   double* d_rmse_scratch = nullptr;
   std::string trace_path;
+  long long n_pairs = 0;           // key pairs of the Schur assembly (all problems)
 
   // Task timeline of the last dataflow factorization as CSV:
   // cta,mode,i,j,k0,count,wait_ns,select_ns,end_ns (times from the first wait).
@@ -1146,6 +1147,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   const Bases& tot = base[nprob];
   if (tot.pairs > INT32_MAX || (long long)K + tot.recs > INT32_MAX || tot.items > INT32_MAX)
     return GBA_ERR_INVALID;
+  n_pairs = tot.pairs;
   img_items.resize(tot.img_items);
   img_item_off.assign(size_t(I) + 1, 0);
   // the pair lists (the largest array): one problem's list moves into place;
@@ -2146,6 +2148,23 @@ int gba_plan_last_run_launches(gba_plan* p, int64_t* n) {
 int gba_plan_device_bytes(gba_plan* p, int64_t* bytes) {
   if (!p || !bytes) return GBA_ERR_INVALID;
   *bytes = int64_t(p->impl.arena.bytes);
+  return GBA_OK;
+}
+
+int gba_plan_structure(gba_plan* p, gba_plan_structure_info* out) {
+  if (!p || !out) return GBA_ERR_INVALID;
+  const gba::Plan& P = p->impl;
+  std::memset(out, 0, sizeof(*out));
+  out->problems = P.B;
+  out->keys = P.d.K;
+  out->points = P.d.P;
+  out->images = P.d.I;
+  out->key_pairs = P.n_pairs;
+  out->pair_items = P.d.n_items;
+  out->blocks = P.d.n_blocks;
+  out->image_items = P.d.n_img_items;
+  out->camera_records = P.d.R;
+  out->max_reduced_size = P.d.max_n;
   return GBA_OK;
 }
 

@@ -75,6 +75,7 @@ def lib():
     L.gba_schur_step.argtypes = [P, d, d, C.c_double, O, d]
     L.gba_plan_query.argtypes = [vp]
     L.gba_plan_device_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.gba_plan_structure.argtypes = [vp, C.POINTER(abi.PlanStructure)]
     SC = C.POINTER(abi.ServerConfig)
     L.gba_default_server_config.argtypes = [SC]
     L.gba_default_server_config.restype = None
@@ -237,6 +238,12 @@ class Plan:
         v = C.c_int64()
         _check(lib().gba_plan_device_bytes(self.h, C.byref(v)), "device_bytes")
         return v.value
+
+    def structure(self):
+        """Sizes of the plan's work lists (keys, key pairs, assembly items, ...)."""
+        v = abi.PlanStructure()
+        _check(lib().gba_plan_structure(self.h, C.byref(v)), "structure")
+        return v.as_dict()
 
     def close(self):
         if getattr(self, "h", None):

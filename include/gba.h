@@ -313,6 +313,20 @@ GBA_API int gba_plan_kernel_stats(gba_plan* plan, int32_t stage, double* total_m
 GBA_API int gba_plan_last_run_launches(gba_plan* plan, int64_t* launches);
 /* Device bytes the plan holds (every buffer of its arena). */
 GBA_API int gba_plan_device_bytes(gba_plan* plan, int64_t* bytes);
+/* Sizes of a plan's work lists (no counterpart in the reference: the
+ * structure the device builds once per plan), for cost models and
+ * roofline arithmetic. */
+typedef struct gba_plan_structure_info {
+  int64_t problems, keys, points, images;
+  int64_t key_pairs;        /* (key a, key b) pairs of the Schur assembly    */
+  int64_t pair_items;       /* work items of the Schur assembly              */
+  int64_t blocks;           /* image-pair blocks of the reduced systems      */
+  int64_t image_items;      /* work items of the image reduction             */
+  int64_t camera_records;   /* per-point camera records (free cameras)       */
+  int64_t max_reduced_size; /* largest reduced system (unknowns)             */
+  int64_t reserved_[4];
+} gba_plan_structure_info;
+GBA_API int gba_plan_structure(gba_plan* plan, gba_plan_structure_info* out);
 
 /* ---- batched one-shot solve (independent problems, one plan) ----------- */
 GBA_API int gba_solve_batch(const gba_problem* problems, const double* const* near_ys,
@@ -415,9 +429,13 @@ GBA_API int64_t gba_estimate_device_bytes(const gba_problem* problem, int32_t pr
  * of libgba.so (about 1.6 MB, held on every GPU that loads the library until
  * exit), so problems are limited to GBA_NOALLOC_MAX_IMAGES images (larger
  * ones return GBA_ERR_INVALID).  Every call shares that array: calls whose
- * work overlaps on the GPU race and must be serialized.  The first call on a
- * device looks up the array's device address (once per device); make it
- * before any stream capture.  `stream` is a cudaStream_t (NULL = default
+ * work overlaps on the GPU race and must be serialized.  Each call looks up
+ * the array's device address on the current device; the first call on a
+ * device also loads the library's kernels there, so make it before any
+ * stream capture.  Null arrays that a launch would read return
+ * GBA_ERR_INVALID before anything is launched.  Ids are checked on the
+ * device: a key whose image, point or camera id is out of range is skipped
+ * and the cost written is NaN.  `stream` is a cudaStream_t (NULL = default
  * stream); the call only enqueues work. */
 #define GBA_NOALLOC_MAX_IMAGES 16384
 

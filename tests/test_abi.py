@@ -57,6 +57,7 @@ def _c_layout(tmp_path):
         "gba_report": [f for f, _ in abi.Report._fields_],
         "gba_triangulation": [f for f, _ in abi.Triangulation._fields_],
         "gba_tuning": [f for f, _ in abi.Tuning._fields_],
+        "gba_plan_structure_info": [f for f, _ in abi.PlanStructure._fields_],
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/gba.h"',
              'int main(void) {']
@@ -77,7 +78,8 @@ def test_struct_layouts_match_header(tmp_path):
     lay = _c_layout(tmp_path)
     for name, cls in (("gba_problem", abi.Problem), ("gba_options", abi.Options),
                       ("gba_report", abi.Report), ("gba_triangulation", abi.Triangulation),
-                      ("gba_tuning", abi.Tuning)):
+                      ("gba_tuning", abi.Tuning),
+                      ("gba_plan_structure_info", abi.PlanStructure)):
         assert int(lay[name]) == C.sizeof(cls), name
         for f, _ in cls._fields_:
             assert int(lay[f"{name}.{f}"]) == getattr(cls, f).offset, (name, f)

@@ -58,9 +58,10 @@ def upload(scene, x):
     return dp, t
 
 
-def noalloc_cost(L, dp, loss, delta):
+def noalloc_cost(L, dp, loss, delta, out=None):
     import torch
-    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    if out is None:
+        out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
     st = L.gba_cost_noalloc(C.byref(dp), loss, delta, C.c_void_p(out.data_ptr()), C.c_void_p(stream))
     assert st == 0, st
@@ -110,3 +111,64 @@ def test_noalloc_rejects_oversized_problem(L):
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     st = L.gba_cost_noalloc(C.byref(dp), 0, 1.0, C.c_void_p(out.data_ptr()), C.c_void_p(0))
     assert st == abi.GBA_ERR_INVALID
+
+
+def test_noalloc_allocates_nothing(L):
+    """The point of the entry point: after a first call on the device, calls
+    leave the device's free memory exactly as they found it."""
+    import torch
+    s = synthetic.ring_scene(num_images=12, num_points=2000, obs_per_point=4, seed=34)
+    dp, keep = upload(s, s.x0)
+    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    noalloc_cost(L, dp, abi.LOSS_TRIVIAL, 1.0, out)   # first call: loads the kernels
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    values = [noalloc_cost(L, dp, abi.LOSS_HUBER if i % 2 else abi.LOSS_TRIVIAL, 1.0, out)
+              for i in range(8)]
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)
+    assert values[0] == values[2] and values[1] == values[3]
+
+
+def test_noalloc_rejects_missing_images_before_any_launch(L):
+    """Zero keys but images present: the rotation pass would read images, so a
+    NULL images pointer is refused on the host."""
+    import torch
+    s = synthetic.ring_scene(num_images=4, num_points=40, obs_per_point=2, seed=35)
+    dp, keep = upload(s, s.x0)
+    dp.number_of_keys = 0
+    dp.images = None
+    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    before = L.gba_kernel_launch_count()
+    st = L.gba_cost_noalloc(C.byref(dp), 0, 1.0, C.c_void_p(out.data_ptr()), C.c_void_p(0))
+    assert st == abi.GBA_ERR_INVALID
+    assert L.gba_kernel_launch_count() == before
+    # zero keys with the images present is a valid call with cost 0
+    dp2, keep2 = upload(s, s.x0)
+    dp2.number_of_keys = 0
+    assert noalloc_cost(L, dp2, abi.LOSS_TRIVIAL, 1.0) == 0.0
+
+
+def test_noalloc_out_of_range_ids_give_nan_without_fault(L):
+    """Ids are checked on the device: a key pointing past the points (or an
+    image pointing past the cameras) is skipped and the cost is NaN; the next
+    call on the same scratch is normal again."""
+    import math
+    import torch
+    s = synthetic.ring_scene(num_images=6, num_points=300, obs_per_point=3, seed=36)
+    dp, keep = upload(s, s.x0)
+    good = noalloc_cost(L, dp, abi.LOSS_TRIVIAL, 1.0)
+    bad_pt = keep["key_point"].clone()
+    bad_pt[5] = s.number_of_points + 1000
+    dp_bad = DeviceProblem(dp.number_of_points, dp.number_of_images, dp.number_of_cameras,
+                           dp.number_of_keys, dp.key_image, bad_pt.data_ptr(), dp.keys,
+                           dp.image_camera, dp.cameras, dp.points, dp.images)
+    assert math.isnan(noalloc_cost(L, dp_bad, abi.LOSS_TRIVIAL, 1.0))
+    bad_cam = keep["image_camera"].clone()
+    bad_cam[0] = -1
+    dp_cam = DeviceProblem(dp.number_of_points, dp.number_of_images, dp.number_of_cameras,
+                           dp.number_of_keys, dp.key_image, dp.key_point, dp.keys,
+                           bad_cam.data_ptr(), dp.cameras, dp.points, dp.images)
+    assert math.isnan(noalloc_cost(L, dp_cam, abi.LOSS_TRIVIAL, 1.0))
+    assert noalloc_cost(L, dp, abi.LOSS_TRIVIAL, 1.0) == good
+    torch.cuda.synchronize()

@@ -3,8 +3,9 @@
 Workload (default): 200 cameras on a jittered grid over a 100,000-point slab,
 4-12 keys per point (~800k keys), shared intrinsics with radial distortion
 (fixed), points and images free; 20 Levenberg-Marquardt iterations per solve
-(eps1 = eps2 = 0 so every iteration runs) on the mixed FP32/FP64 path with
-the dense FP64 Cholesky of the 1,200-unknown reduced camera system.
+(eps1 = eps2 = 0 so every iteration runs) on the mixed FP32/FP64 path: FP32
+Jacobians, Schur complement and dense Cholesky of the 1,200-unknown reduced
+camera system; FP64 master x, update, cost sums and LM decisions.
 
 A step is one full solve (20 LM iterations) with the problem resident in HBM;
 `value` = LM iterations / device time over the K timed steps (CUDA events on
@@ -16,6 +17,12 @@ copies, the solve and the device->host copy of x inside the timed region.
 faithful O(I^2 P) reduced-system loop, single thread as the reference is) on a
 bounded sample of the same workload: the reduced-system double loop runs over
 every `stride`-th weighted image and its time is scaled by the stride.
+
+Parity (outside every timed region): the grid solve and every window of the
+512-window batch are solved again by the CPU FP64 oracle (point-major mode,
+host threads) and the line's `parity` object carries the relative final-cost
+and absolute RMSE differences against the acceptance rule (1e-6 relative
+cost, 1e-4 px RMSE).
 """
 from __future__ import annotations
 
@@ -60,7 +67,7 @@ def parse():
     ap.add_argument("--tri-cpu-sample", type=int, default=20_000)
     ap.add_argument("--rates", default="50,200,800,2000",
                     help="serving: Poisson arrival rates swept (req/s)")
-    ap.add_argument("--duration", type=float, default=10.0, help="serving: seconds per rate")
+    ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds per rate")
     ap.add_argument("--pool", type=int, default=256, help="serving: distinct request scenes")
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--max-in-flight", type=int, default=4)
@@ -246,6 +253,63 @@ def pair_count(scene):
 
 
 # ---------------------------------------------------------------------------
+# parity against the CPU FP64 oracle (outside the timed regions)
+# ---------------------------------------------------------------------------
+COST_RTOL = 1e-6
+RMSE_ATOL = 1e-4
+
+
+def oracle_parity(groups):
+    """Solves every job's scene with the oracle (FP64, point-major mode, the
+    same LM options) on host threads -- the oracle is a C library called
+    through ctypes, which releases the GIL -- and compares the GPU's final
+    cost and RMSE with it.  groups: {name: [(scene, options, result with
+    final_cost / final_rmse), ...]}; one summary per group."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    t0 = time.perf_counter()
+    nthreads = max(1, min(32, os.cpu_count() or 1))
+    flat = [(g, j) for g, jobs in groups.items() for j in jobs]
+    # the largest problems first, so that they do not finish last
+    order = sorted(range(len(flat)), key=lambda i: -flat[i][1][0].number_of_keys)
+    with ThreadPoolExecutor(nthreads) as ex:
+        futs = {i: ex.submit(oracle.lm_solve, flat[i][1][0], options=flat[i][1][1]) for i in order}
+        refs = {i: f.result() for i, f in futs.items()}
+    wall = time.perf_counter() - t0
+    out = {}
+    for g in groups:
+        cost_rel, rmse_abs, fails = [], [], 0
+        for i, (gg, (scene, _, rep)) in enumerate(flat):
+            if gg != g:
+                continue
+            err, _, rr = refs[i]
+            if err != 0:
+                fails += 1
+                continue
+            cost_rel.append(abs(rep.final_cost - rr.final_cost) / rr.final_cost)
+            rmse_abs.append(abs(rep.final_rmse - rr.final_rmse))
+        worst_c = max(cost_rel) if cost_rel else None
+        worst_r = max(rmse_abs) if rmse_abs else None
+        out[g] = {"comparator": "CPU FP64 oracle (point-major mode), same LM options",
+                  "problems": len(groups[g]), "oracle_errors": fails,
+                  "final_cost_rel_vs_oracle_max": worst_c,
+                  "rmse_abs_diff_vs_oracle_max": worst_r,
+                  "tolerance": {"final_cost_rel": COST_RTOL, "rmse_px": RMSE_ATOL},
+                  "pass": bool(fails == 0 and worst_c is not None and worst_c <= COST_RTOL
+                               and worst_r <= RMSE_ATOL),
+                  "oracle_threads": nthreads, "oracle_wall_s": wall}
+    return out
+
+
+class _Result:
+    """final_cost / final_rmse of a GPU result, detached from its report."""
+
+    def __init__(self, rep):
+        self.final_cost = float(rep.final_cost)
+        self.final_rmse = float(rep.final_rmse)
+
+
+# ---------------------------------------------------------------------------
 # CPU baseline (oracle, faithful loop, sampled)
 # ---------------------------------------------------------------------------
 def cpu_sample(scene, stride):
@@ -361,13 +425,12 @@ def run_gba(args, ws, rank, local):
 
     # per-stage roofline (the stage's kernels, CUDA events on the solver stream)
     K, P, I = scene.number_of_keys, scene.number_of_points, scene.number_of_images
-    pairs = pair_count(scene)
-    items = None
+    structure = plan.structure()          # the plan's real work lists
+    pairs = structure["key_pairs"]
     peak, peak_kind = load_peaks()
     names = abi.STAGE_NAMES
     per_launch_ms = {names[s]: stage_tot[s] / (prof_runs * ITERS_PER_SOLVE) for s in range(len(names))}
-    n_items_est = int(np.ceil(pairs / 256)) + I * (I + 1) // 2
-    sb = stage_bytes(K, P, I, pairs, n_items_est, tsz)
+    sb = stage_bytes(K, P, I, pairs, structure["pair_items"], tsz)
     stages = {}
     for name, ms in per_launch_ms.items():
         entry = {"ms_per_iteration": ms}
@@ -436,36 +499,51 @@ def run_gba(args, ws, rank, local):
                "seconds_per_iteration": est}
 
     secondary = None
+    parity_groups = {}
+    if rank == 0 and ws == 1:
+        parity_groups["grid"] = [(scene, abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0,
+                                                          eps2=0.0), _Result(rep))]
     if rank == 0 and ws == 1 and not args.no_secondary:
-        # the batched and the serving metrics, each on its own workload after
-        # the timed region above (summaries; the full lines come from
-        # --workload windows / serving)
+        # the batched, serving, large-scene and triangulation metrics, each on
+        # its own workload after the timed region above (summaries; the full
+        # lines come from --workload windows / serving / walk / triangulation)
         import copy
         a2 = copy.copy(args)
-        a2.windows, a2.per_problem_sample, a2.steps, a2.warmup = 512, 64, 3, 3
-        w = run_windows(a2, ws, rank, local)
-        a3 = copy.copy(args)
-        a3.rates, a3.duration, a3.pool = "100,1000", 4.0, 96
-        sv = run_serving(a3, ws, rank, local)
+        a2.windows, a2.per_problem_sample, a2.steps, a2.warmup = 512, 512, 3, 3
+        w = run_windows(a2, ws, rank, local, keep_parity=True)
+        parity_groups["windows"] = w.pop("_parity_jobs")
+        sv = run_serving(args, ws, rank, local)
         a4 = copy.copy(args)
         a4.steps, a4.warmup = 3, 1
+        wk = run_walk(a4, ws, rank, local)
         tr = run_triangulation(a4, ws, rank, local)
         gf = run_grid_free(a4, ws, rank, local)
+        parity_groups["grid_free_intrinsics"] = gf.pop("_parity_jobs")
         secondary = {
-            "windows": {k: w[k] for k in ("metric", "value", "unit", "ms_per_step",
+            "windows": {k: w[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e",
                                           "speedup_vs_per_problem_fp64",
+                                          "speedup_vs_per_problem_fp64_e2e",
                                           "final_cost_max_rel_diff_vs_fp64", "tuning",
-                                          "stage_roofline_hbm")},
+                                          "stage_roofline_hbm", "gpu_launches")},
             "windows_per_problem_fp64": w["per_problem_fp64"],
             "serving": {"metric": sv["metric"], "value": sv["value"], "unit": sv["unit"],
                         "p50_ms": sv["p50_ms"], "p99_ms": sv["p99_ms"],
-                        "sweep": [{k: r[k] for k in ("rate", "solves_per_s", "p50_ms", "p99_ms")}
+                        "duration_s_per_rate": sv["config"]["duration_s"],
+                        "sweep": [{k: r[k] for k in ("rate", "requests", "solves_per_s", "p50_ms",
+                                                     "p99_ms", "mean_batch")}
                                   for r in sv["sweep"]],
                         "final_cost_max_rel_diff_vs_fp64": sv["final_cost_max_rel_diff_vs_fp64"]},
+            "walk": {k: wk[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e", "fp64",
+                                        "solve", "gpu_launches")},
             "triangulation": {k: tr[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e",
                                                  "cpu_baseline", "max_abs_diff_vs_oracle_sample")},
             "grid_free_intrinsics": gf,
         }
+        secondary["walk"]["config"] = wk["config"]["workload"]
+    parity = oracle_parity(parity_groups) if parity_groups else None
+    if secondary is not None and parity is not None:
+        secondary["windows"]["parity"] = parity.get("windows")
+        secondary["grid_free_intrinsics"]["parity"] = parity.get("grid_free_intrinsics")
 
     if rank == 0:
         lat = sorted(step_ms)
@@ -485,6 +563,8 @@ def run_gba(args, ws, rank, local):
             "solve": {"initial_cost": rep.initial_cost, "final_cost": rep.final_cost,
                       "final_rmse": rep.final_rmse, "accepted": rep.accepted,
                       "rejected": rep.rejected, "setup_ms": rep0.setup_ms},
+            "parity": None if parity is None else parity.get("grid"),
+            "structure": structure,
             "roofline": roofline,
             "roofline_fp32": roofline_fp32,
             "roofline_hbm": roofline_hbm,
@@ -511,9 +591,12 @@ WINDOW_WORKLOAD = ("512 local-BA windows (ring geometry, I ~ U{5..40}, P ~ U{500
                    "3-8 keys/point), 10 LM iterations each")
 
 
-def run_windows(args, ws, rank, local):
+def run_windows(args, ws, rank, local, keep_parity=False):
     """Batched local BA: all windows in one plan (mixed path) against the
-    plain per-problem FP64 path (gba_solve, one window after another)."""
+    plain per-problem FP64 path (gba_solve, one window after another), on
+    like bases: device time against device time (CUDA events of the batched
+    plan; each gba_solve's own device time) and end to end against end to end
+    (gba_solve_batch with host buffers; gba_solve wall time per window)."""
     import torch
     from hs_sfm_gb300 import abi, gba, synthetic
     torch.cuda.set_device(local)
@@ -544,8 +627,10 @@ def run_windows(args, ws, rank, local):
         step_ms.append(plan.last_run_ms())
         stage_tot += np.array(plan.report(0).stage_ms)
     clk = clocks.stop()
-    batch_costs = np.array([plan.report(q).final_cost for q in range(len(wins))])
+    batch_reports = [plan.report(q) for q in range(len(wins))]
+    batch_costs = np.array([r.final_cost for r in batch_reports])
     launches = plan.launches()
+    structure = plan.structure()
     plan.close()
     batched = len(wins) * args.steps / (sum(step_ms) / 1e3)
     # e2e of the batch: gba_solve_batch with host buffers (structure build,
@@ -555,20 +640,21 @@ def run_windows(args, ws, rank, local):
     t0 = time.perf_counter()
     xs, reps = gba.solve_batch(wins, opt_e2e)
     e2e_s = time.perf_counter() - t0
-    h2d = sum(0 for _ in reps)
     # per-problem FP64 path, one window after another
     opt64 = abi.make_options(max_iterations=WINDOW_ITERS, eps1=0.0, eps2=0.0,
                              precision=abi.PRECISION_FP64, device=local)
     sample = wins[:max(1, min(args.per_problem_sample, len(wins)))]
-    per_ms, per_costs = [], []
+    per_ms, per_dev_ms, per_costs = [], [], []
     t0 = time.perf_counter()
     for w in sample:
         t1 = time.perf_counter()
         x, r = gba.solve(w, opt64)
         per_ms.append(1e3 * (time.perf_counter() - t1))
+        per_dev_ms.append(r.solve_ms)
         per_costs.append(r.final_cost)
     per_s = time.perf_counter() - t0
     per_problem = len(sample) / per_s
+    per_problem_dev = len(sample) / (sum(per_dev_ms) / 1e3)
     rel = np.abs(batch_costs[:len(sample)] - np.array(per_costs)) / np.array(per_costs)
     stages = {abi.STAGE_NAMES[i]: stage_tot[i] / args.steps for i in range(abi.NUM_STAGES)}
     # per-stage HBM roofline at this scale (the same algorithmic bytes as the
@@ -577,7 +663,7 @@ def run_windows(args, ws, rank, local):
     I_all = sum(w.number_of_images for w in wins)
     pairs_all = sum(pair_count(w) for w in wins)
     peak, peak_kind = load_peaks()
-    sb = stage_bytes(K, P_all, I_all, pairs_all, int(np.ceil(pairs_all / 1024)) + len(wins) * 400, 4)
+    sb = stage_bytes(K, P_all, I_all, structure["key_pairs"], structure["pair_items"], 4)
     stage_roof = {}
     for name, ms in stages.items():
         if name in sb and ms > 0:
@@ -592,18 +678,29 @@ def run_windows(args, ws, rank, local):
         "data": "synthetic (seeded ring windows)",
         "config": {"workload": WINDOW_WORKLOAD, "windows": len(wins), "keys": K,
                    "iterations_per_solve": WINDOW_ITERS, "l2": "flushed between steps"},
-        "per_problem_fp64": {"value": per_problem, "unit": "solves/s", "windows": len(sample),
+        "per_problem_fp64": {"value": per_problem_dev, "unit": "solves/s",
+                             "basis": "device time (each gba_solve's CUDA-event solve time)",
+                             "e2e": {"value": per_problem, "unit": "solves/s",
+                                     "basis": "wall time of gba_solve per window, host buffers"},
+                             "windows": len(sample),
                              "p50_ms": float(np.percentile(per_ms, 50)),
                              "p99_ms": float(np.percentile(per_ms, 99))},
-        "speedup_vs_per_problem_fp64": batched / per_problem,
-        "e2e": {"value": len(wins) / e2e_s, "unit": "solves/s", "seconds": e2e_s},
+        "speedup_vs_per_problem_fp64": batched / per_problem_dev,
+        "speedup_vs_per_problem_fp64_e2e": (len(wins) / e2e_s) / per_problem,
+        "e2e": {"value": len(wins) / e2e_s, "unit": "solves/s", "seconds": e2e_s,
+                "h2d_bytes_per_step": int(sum(r.h2d_bytes for r in reps[:1])),
+                "d2h_bytes_per_step": int(sum(r.d2h_bytes for r in reps[:1])),
+                "basis": "gba_solve_batch with host buffers (build, copies, solve, copies back)"},
         "final_cost_max_rel_diff_vs_fp64": float(rel.max()),
+        "structure": structure,
         "setup_s": setup_s, "stage_ms_per_run": stages, "gpu_launches": int(launches * args.steps),
         "clocks": clk, "tuning": tuning,
         "stage_roofline_hbm": {"peak_gbs": peak, "peak_kind": f"{peak_kind} hbm_gbs",
                                "stages": stage_roof},
     }
-    del h2d
+    if keep_parity:
+        o10 = abi.make_options(max_iterations=WINDOW_ITERS, eps1=0.0, eps2=0.0)
+        out["_parity_jobs"] = [(w, o10, _Result(r)) for w, r in zip(wins, batch_reports)]
     return out
 
 
@@ -668,8 +765,12 @@ def run_walk(args, ws, rank, local):
         "solve": {"initial_cost": rep.initial_cost, "final_cost": rep.final_cost,
                   "final_rmse": rep.final_rmse, "accepted": rep.accepted, "rejected": rep.rejected,
                   "pcg_iterations": rep.pcg_iterations},
-        "fp64": {"final_cost": r64.final_cost, "pcg_iterations": r64.pcg_iterations,
-                 "final_cost_rel_diff": abs(rep.final_cost - r64.final_cost) / r64.final_cost},
+        "fp64": {"final_cost": r64.final_cost, "final_rmse": r64.final_rmse,
+                 "pcg_iterations": r64.pcg_iterations,
+                 "final_cost_rel_diff": abs(rep.final_cost - r64.final_cost) / r64.final_cost,
+                 "rmse_abs_diff": abs(rep.final_rmse - r64.final_rmse),
+                 "pass": bool(abs(rep.final_cost - r64.final_cost) <= COST_RTOL * r64.final_cost
+                              and abs(rep.final_rmse - r64.final_rmse) <= RMSE_ATOL)},
         "stage_ms_per_iteration": stages,
         "e2e": {"value": WALK_ITERS / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(re2e.h2d_bytes),
                 "d2h_bytes_per_step": int(re2e.d2h_bytes), "ms_per_step": 1e3 * e2e_s},
@@ -677,9 +778,11 @@ def run_walk(args, ws, rank, local):
         "cpu_baseline": None,
         "cpu_baseline_note": ("the reference's O(I^2 P) reduced-system loop is not timeable at 2000 "
                               "images (about 2e12 block lookups per iteration)"),
+        "parity_note": ("compared with the plain FP64 GPU path (the same PCG, FP64 throughout): "
+                        "the CPU oracle's dense LDL^T of 12,000 unknowns (5.8e11 FLOP per "
+                        "iteration) does not fit a bench run"),
     }
-    print(json.dumps(out), flush=True)
-    return 0
+    return out
 
 
 SERVE_ITERS = 10
@@ -832,11 +935,20 @@ def run_grid_free(args, ws, rank, local):
         ms.append(plan.last_run_ms())
     rep = plan.report(0)
     plan.close()
+    # the plain FP64 GPU path on the same scene, and the oracle (parity phase)
+    opt64 = abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0, eps2=0.0,
+                             precision=abi.PRECISION_FP64, device=local)
+    x64, r64 = gba.solve(scene, opt64)
     return {"metric": "LM iters/s", "value": ITERS_PER_SOLVE * len(ms) / (sum(ms) / 1e3),
             "unit": "iter/s", "ms_per_step": float(np.mean(ms)),
             "config": "grid 200 cameras / 100k points, the shared camera free (radial + intrinsics, "
                       "1,212 reduced-system unknowns), 20 LM iterations, mixed",
-            "final_cost": rep.final_cost, "initial_cost": rep.initial_cost}
+            "final_cost": rep.final_cost, "initial_cost": rep.initial_cost,
+            "final_rmse": rep.final_rmse,
+            "fp64_gpu": {"final_cost": r64.final_cost,
+                         "final_cost_rel_diff": abs(rep.final_cost - r64.final_cost) / r64.final_cost},
+            "_parity_jobs": [(scene, abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0,
+                                                      eps2=0.0), _Result(rep))]}
 
 
 TRI_WORKLOAD = ("batched multi-view triangulation: 1,000,000 tracks over 200 ring views, "
@@ -906,13 +1018,16 @@ def main():
     if args.impl == "reference":
         return run_reference(args, ws, rank)
     if args.workload == "windows":
-        print(json.dumps(run_windows(args, ws, rank, local)), flush=True)
+        w = run_windows(args, ws, rank, local, keep_parity=True)
+        w["parity"] = oracle_parity({"windows": w.pop("_parity_jobs")})["windows"]
+        print(json.dumps(w), flush=True)
         return 0
     if args.workload == "serving":
         print(json.dumps(run_serving(args, ws, rank, local)), flush=True)
         return 0
     if args.workload == "walk":
-        return run_walk(args, ws, rank, local)
+        print(json.dumps(run_walk(args, ws, rank, local)), flush=True)
+        return 0
     if args.workload == "triangulation":
         print(json.dumps(run_triangulation(args, ws, rank, local)), flush=True)
         return 0

@@ -66,6 +66,13 @@ struct ProbInfo {
   // 6-wide parts of each camera's parameters (zero-padded past cps)
   int ext_begin, num_ext;
   int cam_begin, num_cams, cps, nc;
+  // fixed groups: bit 0 points, bit 1 images.  A fixed group keeps its
+  // values: its Jacobian columns are zero, so its normal blocks are mu I,
+  // its gradient and step zero, and it is left out of ||x||
+  // (camera_shared_normal_equation_solver.hpp:540-706 solve the same
+  // systems without the fixed unknowns).
+  int fix;
+  int pad_;
 };
 
 struct Chunk {       // a contiguous range of one problem's entities
@@ -161,8 +168,14 @@ struct DevPlan {
   void* pcg_z;               // T: [6I] preconditioned residual
   void* pcg_q;               // T: [6I] S p
   void* pcg_p[2];            // T: [6I] search directions (by iteration parity)
-  double* pcg_part;          // [kPcgSlots * n_img_chunks]: p.q, r.z (x2), r.r (x2), b.b, x.r
+  double* pcg_part;          // [kPcgSlots * n_ext_chunks]: p.q, r.z (x2), r.r (x2), b.b, x.r
   int* pcg_done;             // [B] 1 once a problem's inner solve has stopped
+  // PCG work chunks over reduced-system images (images, then free cameras'
+  // parts; the image chunks when no camera is free) and their problems
+  int n_ext_chunks;
+  const Chunk* ext_chunks;
+  const int* prob_ext_chunk_off;  // [B+1]
+  const int* ext_prob;            // [I_ext] problem of each reduced-system image
   // Schur assembly
   const int2* pairs;         // (key_a, key_b) per pair, grouped by block
   const int4* items;         // (block, pair_begin, pair_end, prob)

@@ -712,6 +712,7 @@ __global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
   const T* __restrict__ IL = tptr<T>(d.img_lin[par]);
   const T* __restrict__ rwb = tptr<T>(d.RW[par]);
   T* __restrict__ JR = tptr_mut<T>(d.JR);
+  const int fix = d.prob[ch.prob].fix;
   for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
     const int img = __ldg(d.key_img + k), pt = __ldg(d.key_pt + k);
     T X[3];
@@ -728,6 +729,14 @@ __global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
     load_cam<T>(d, par, ci, cam);
     T jp[6], ji[12], nrm[2];
     key_jacobian<T>(X, il, cam, jp, ji, nrm);
+    if (fix & 1) {   // fixed points: no point columns
+#pragma unroll
+      for (int m = 0; m < 6; ++m) jp[m] = T(0);
+    }
+    if (fix & 2) {   // fixed images: no image columns
+#pragma unroll
+      for (int m = 0; m < 12; ++m) ji[m] = T(0);
+    }
     T rw[4];
     load_vec<4>(rwb + 4LL * k, rw);
     const T sw = rw[2];
@@ -1332,6 +1341,38 @@ __device__ __forceinline__ double sum_items4(const double* base, int ib, int ie)
   return (s0 + s1) + (s2 + s3);
 }
 
+// The entry (row 6i + a, column 6j + bcol), i >= j, of a problem's reduced
+// system before the Schur terms and the damping (i, j local reduced-system
+// images: the images, then each free camera's parts): U_i on an image's
+// diagonal block, E_i between an image and the parts of its camera, U_c
+// between parts of one camera; zero past a camera's parameters.
+__device__ __forceinline__ double reduced_base(const DevPlan& d, const ProbInfo& pi, int i, int a, int j,
+                                               int bcol) {
+  const int ni = pi.num_images;
+  if (i < ni) return i == j ? d.U[36LL * (pi.image_begin + i) + 6 * a + bcol] : 0.0;
+  // camera part: global camera ci, parameter m of the row
+  const int ci = pi.cam_begin + (i - ni) / pi.nc;
+  const int4 cinf = d.cam_info[ci];
+  const int m = 6 * ((i - ni) % pi.nc) + a;
+  if (m >= cinf.x) return 0.0;
+  if (j >= ni) {
+    const int cj = pi.cam_begin + (j - ni) / pi.nc;
+    const int mj = 6 * ((j - ni) % pi.nc) + bcol;
+    return (cj == ci && mj < cinf.x) ? d.Uc[100LL * ci + 10 * m + mj] : 0.0;
+  }
+  const int gj = pi.image_begin + j;
+  return d.img_cam[gj] == ci ? d.Ei[60LL * gj + 10 * bcol + cam_full_col(unsigned(cinf.y), m)] : 0.0;
+}
+
+// The gradient entry of row 6i + a of the reduced system (g_i or g_c).
+__device__ __forceinline__ double reduced_grad(const DevPlan& d, const ProbInfo& pi, int i, int a) {
+  const int ni = pi.num_images;
+  if (i < ni) return d.gi[6LL * (pi.image_begin + i) + a];
+  const int ci = pi.cam_begin + (i - ni) / pi.nc;
+  const int m = 6 * ((i - ni) % pi.nc) + a;
+  return m < d.cam_info[ci].x ? d.gc[10LL * ci + m] : 0.0;
+}
+
 // Dense reduced system (lower triangle) and rhs in precision T; the block
 // sums over work items are taken in FP64.  Rows and columns run over the
 // problem's reduced-system images: its images, then with free cameras nc
@@ -1357,29 +1398,9 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
     const int ib = __ldg(d.blk_item_off + blk), ie = __ldg(d.blk_item_off + blk + 1);
     v = sum_items4(d.item_partial + 6 * bcol + a, ib, ie);
   }
-  double base = 0.0, g = 0.0;
-  if (i < ni) {
-    const int gi_img = pi.image_begin + i;
-    if (i == j) base = d.U[36LL * gi_img + 6 * a + bcol];
-    if (col == 0) g = d.gi[6LL * gi_img + a];
-  } else {
-    // camera part: global camera ci, parameter m of the row
-    const int ci = pi.cam_begin + (i - ni) / pi.nc;
-    const int4 cinf = d.cam_info[ci];
-    const int m = 6 * ((i - ni) % pi.nc) + a;
-    if (m < cinf.x) {
-      if (j >= ni) {
-        const int cj = pi.cam_begin + (j - ni) / pi.nc;
-        const int mj = 6 * ((j - ni) % pi.nc) + bcol;
-        if (cj == ci && mj < cinf.x) base = d.Uc[100LL * ci + 10 * m + mj];
-      } else {
-        const int gj = pi.image_begin + j;
-        if (d.img_cam[gj] == ci)
-          base = d.Ei[60LL * gj + 10 * bcol + cam_full_col(unsigned(cinf.y), m)];
-      }
-      if (col == 0) g = d.gc[10LL * ci + m];
-    }
-  }
+  (void)ni;
+  const double base = reduced_base(d, pi, i, a, j, bcol);
+  const double g = col == 0 ? reduced_grad(d, pi, i, a) : 0.0;
   double s = base - v;
   if (row == col) s += st.mu;
   tptr_mut<T>(d.S)[pi.s_off + (long long)row * n + col] = T(s);
@@ -2448,7 +2469,7 @@ __device__ double block_sum_all(double v, double* smem) {
 
 __device__ __forceinline__ double pcg_prob_sum(const DevPlan& d, int p, int slot, double* red) {
   double v = 0.0;
-  for (int c = d.prob_img_chunk_off[p] + threadIdx.x; c < d.prob_img_chunk_off[p + 1]; c += blockDim.x)
+  for (int c = d.prob_ext_chunk_off[p] + threadIdx.x; c < d.prob_ext_chunk_off[p + 1]; c += blockDim.x)
     v += d.pcg_part[(long long)kPcgSlots * c + slot];
   return block_sum_all(v, red);
 }
@@ -2458,23 +2479,29 @@ __global__ void __launch_bounds__(256) k_assemble_blocks(DevPlan d) {
   const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (e >= 36LL * d.n_blocks) return;
   const int blk = int(e / 36), el = int(e % 36);
-  const int2 g = __ldg(d.blk_gij + blk);
-  const int p = __ldg(d.img_prob + g.x);
+  const int2 g = __ldg(d.blk_gij + blk);   // global reduced-system images, g.x <= g.y
+  const int p = __ldg(d.ext_prob + g.x);
   const LMState& st = d.state[p];
   if (!st.active) return;
+  const ProbInfo& pi = d.prob[p];
   const int ib = __ldg(d.blk_item_off + blk), ie = __ldg(d.blk_item_off + blk + 1);
   double v = 0.0;
   for (int t = ib; t < ie; ++t) v += d.item_partial[(long long)kItemStride * t + el];
   double sv = -v;
-  if (g.x == g.y) {
-    sv += d.U[36LL * g.x + el];
-    if (el % 7 == 0) sv += st.mu;
+  // entry (component el / 6 of g.x, component el % 6 of g.y); the base of
+  // the symmetric system is read as row (g.y, el % 6), column (g.x, el / 6)
+  const int lx = g.x - pi.ext_begin, ly = g.y - pi.ext_begin;
+  if (ly < pi.num_images) {
+    if (g.x == g.y) sv += d.U[36LL * (pi.image_begin + lx) + el];
+  } else {
+    sv += reduced_base(d, pi, ly, el % 6, lx, el / 6);
   }
+  if (g.x == g.y && el % 7 == 0) sv += st.mu;
   tptr_mut<T>(d.Sblk)[36LL * blk + el] = T(sv);
   if (g.x == g.y && el < 6) {
     double rv = 0.0;
     for (int t = ib; t < ie; ++t) rv += d.item_partial[(long long)kItemStride * t + 36 + el];
-    tptr_mut<T>(d.b)[6LL * g.x + el] = T(d.gi[6LL * g.x + el] - rv);
+    tptr_mut<T>(d.b)[6LL * g.x + el] = T(reduced_grad(d, pi, lx, el) - rv);
   }
 }
 
@@ -2482,8 +2509,8 @@ __global__ void __launch_bounds__(256) k_assemble_blocks(DevPlan d) {
 template <typename T>
 __global__ void __launch_bounds__(128) k_pcg_precond(DevPlan d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.I) return;
-  const int p = d.img_prob[i];
+  if (i >= d.I_ext) return;
+  const int p = d.ext_prob[i];
   if (!d.state[p].active) return;
   const T* A = tptr<T>(d.Sblk) + 36LL * d.img_diag_blk[i];
   T L[6][6], X[6][6];
@@ -2550,7 +2577,7 @@ __device__ __forceinline__ T pcg_precond_apply(const DevPlan& d, int img, T rv, 
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_init(DevPlan d) {
   __shared__ double red[33];
-  const Chunk ch = d.img_chunks[blockIdx.x];
+  const Chunk ch = d.ext_chunks[blockIdx.x];
   const LMState& st = d.state[ch.prob];
   if (!st.active || d.factor_flag[ch.prob]) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2577,7 +2604,7 @@ __global__ void __launch_bounds__(256) k_pcg_init(DevPlan d) {
     part[3] = rr;
     part[5] = rr;
     part[6] = 0.0;
-    if (blockIdx.x == d.prob_img_chunk_off[ch.prob]) d.pcg_done[ch.prob] = 0;
+    if (blockIdx.x == d.prob_ext_chunk_off[ch.prob]) d.pcg_done[ch.prob] = 0;
   }
 }
 
@@ -2586,7 +2613,7 @@ __global__ void __launch_bounds__(256) k_pcg_init(DevPlan d) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_spmv(DevPlan d, int it) {
   __shared__ double red[33];
-  const Chunk ch = d.img_chunks[blockIdx.x];
+  const Chunk ch = d.ext_chunks[blockIdx.x];
   const int p = ch.prob;
   const LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p] || d.pcg_done[p]) return;
@@ -2648,11 +2675,11 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(DevPlan d, int it) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
   __shared__ double red[33];
-  const Chunk ch = d.img_chunks[blockIdx.x];
+  const Chunk ch = d.ext_chunks[blockIdx.x];
   const int p = ch.prob;
   LMState& st = d.state[p];
   if (!st.active || d.factor_flag[p] || d.pcg_done[p]) return;
-  const bool lead = blockIdx.x == d.prob_img_chunk_off[p];
+  const bool lead = blockIdx.x == d.prob_ext_chunk_off[p];
   const int par = it & 1;
   const double rz = pcg_prob_sum(d, p, 1 + par, red);
   const double rr = pcg_prob_sum(d, p, 3 + par, red);
@@ -2763,12 +2790,13 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       const double* x = d.x_pt[par] + 3LL * pt;
       double* xn = d.x_pt[1 - par] + 3LL * pt;
       float2* xf = d.x_ff[1 - par] ? d.x_ff[1 - par] + 3LL * pt : nullptr;
+      const bool free_pt = !(d.prob[ch.prob].fix & 1);   // a fixed point is not in x
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         xn[a] = x[a] - dp[a];
         if (xf) xf[a] = ff_split(xn[a]);
         dn2 += dp[a] * dp[a];
-        xn2 += x[a] * x[a];
+        if (free_pt) xn2 += x[a] * x[a];
         gd += double(pv[6 + a]) * dp[a];
       }
     }
@@ -2788,11 +2816,12 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
     const long long e0 = 6LL * ch.begin, e1 = 6LL * ch.end;
     const ProbInfo& pi = d.prob[ch.prob];
     const long long boff = 6LL * (pi.ext_begin - pi.image_begin);
+    const bool free_img = !(pi.fix & 2);   // fixed images are not in x
     for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
       double dv = double(tptr<T>(d.b)[e + boff]), xv = d.x_img[par][e];
       d.x_img[1 - par][e] = xv - dv;
       dn2 += dv * dv;
-      xn2 += xv * xv;
+      if (free_img) xn2 += xv * xv;
       gd += d.gi[e] * dv;
     }
     double s0 = block_sum(dn2, red), s1 = block_sum(xn2, red), s2 = block_sum(gd, red);
@@ -2929,7 +2958,7 @@ __global__ void __launch_bounds__(kCtrlThreads) k_ctrl_step(DevPlan d) {
     xn2 = sp[1] + si[1];
     gd = sp[2] + si[2];
     // PCG leaves the image rows with residual r: the model decrease gains r^T delta_i
-    if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_img_chunk_off, p, red);
+    if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_ext_chunk_off, p, red);
     if (d.free_cams) {
       double sc[3];
       prob_sums<3>(d.cam_sum, 3, d.prob_cam_off, p, red, sc);
@@ -3354,17 +3383,17 @@ int launch_assemble_blocks(const DevPlan& d, cudaStream_t s) {
 }
 
 int launch_pcg_setup(const DevPlan& d, cudaStream_t s) {
-  if (d.I <= 0) return 0;
-  GBA_DISPATCH(d, (k_pcg_precond<T><<<(d.I + 127) / 128, 128, 0, s>>>(d)));
-  GBA_DISPATCH(d, (k_pcg_init<T><<<d.n_img_chunks, 256, 0, s>>>(d)));
+  if (d.I_ext <= 0) return 0;
+  GBA_DISPATCH(d, (k_pcg_precond<T><<<(d.I_ext + 127) / 128, 128, 0, s>>>(d)));
+  GBA_DISPATCH(d, (k_pcg_init<T><<<d.n_ext_chunks, 256, 0, s>>>(d)));
   return 2;
 }
 
 int launch_pcg_iterations(const DevPlan& d, cudaStream_t s) {
-  if (d.I <= 0) return 0;
+  if (d.I_ext <= 0) return 0;
   for (int it = 0; it < d.pcg_max_iterations; ++it) {
-    GBA_DISPATCH(d, (k_pcg_spmv<T><<<d.n_img_chunks, 256, 0, s>>>(d, it)));
-    GBA_DISPATCH(d, (k_pcg_update<T><<<d.n_img_chunks, 256, 0, s>>>(d, it)));
+    GBA_DISPATCH(d, (k_pcg_spmv<T><<<d.n_ext_chunks, 256, 0, s>>>(d, it)));
+    GBA_DISPATCH(d, (k_pcg_update<T><<<d.n_ext_chunks, 256, 0, s>>>(d, it)));
   }
   return 2 * d.pcg_max_iterations;
 }

@@ -363,6 +363,20 @@ struct Plan {
   std::vector<ProbInfo> prob;
   std::vector<std::vector<int32_t>> key_sorted_to_orig;  // per problem
   std::vector<int64_t> x_size;
+  // values of fixed points / images per problem (empty when free); the
+  // caller's x holds only the free groups: [points][images][cameras]
+  std::vector<std::vector<double>> fix_pt_vals, fix_img_vals;
+  int64_t x_img_off(int q) const { return prob[q].fix & 1 ? 0 : 3LL * prob[q].num_points; }
+  int64_t x_cam_off(int q) const {
+    return x_img_off(q) + (prob[q].fix & 2 ? 0 : 6LL * prob[q].num_images);
+  }
+  // the problem's full points / images from the caller's x
+  const double* pts_of(int q, const double* x) const {
+    return prob[q].fix & 1 ? fix_pt_vals[q].data() : x;
+  }
+  const double* imgs_of(int q, const double* x) const {
+    return prob[q].fix & 2 ? fix_img_vals[q].data() : x + x_img_off(q);
+  }
   // run state
   cudaGraphExec_t graph_exec = nullptr;
   cudaGraphExec_t iter_exec = nullptr;   // one LM iteration (one-shot solves)
@@ -435,13 +449,19 @@ int validate(const gba_problem& p, bool pcg, int threads) {
     return GBA_ERR_INVALID;
   if (p.number_of_keys > 0 && !p.feature_maps) return GBA_ERR_INVALID;
   if (p.number_of_images > 0 && !p.image_camera_map) return GBA_ERR_INVALID;
-  if (p.fix_mask != GBA_FIX_CAMERAS && p.fix_mask != 0) return GBA_ERR_UNSUPPORTED;
+  // every combination of fixed groups but all three (nothing to solve)
+  if (p.fix_mask > (GBA_FIX_POINTS | GBA_FIX_IMAGES | GBA_FIX_CAMERAS)) return GBA_ERR_INVALID;
+  if (p.fix_mask == (GBA_FIX_POINTS | GBA_FIX_IMAGES | GBA_FIX_CAMERAS)) return GBA_ERR_UNSUPPORTED;
+  const bool fixP = p.fix_mask & GBA_FIX_POINTS, fixI = p.fix_mask & GBA_FIX_IMAGES;
   const int64_t cps = params_per_camera(p.intrinsic_computations_mask);
-  const bool free_cams = p.fix_mask == 0 && cps > 0 && p.number_of_cameras > 0;
-  if (free_cams && pcg) return GBA_ERR_UNSUPPORTED;
-  if (p.fix_mask == GBA_FIX_CAMERAS && p.number_of_cameras > 0 && cps > 0 && !p.fix_cameras)
+  const bool free_cams = cameras_free(p);
+  if ((p.fix_mask & GBA_FIX_CAMERAS) && p.number_of_cameras > 0 && cps > 0 && !p.fix_cameras)
     return GBA_ERR_INVALID;
-  if (p.fix_mask == 0) {
+  if (fixP && p.number_of_points > 0 && !p.fix_points) return GBA_ERR_INVALID;
+  if (fixI && p.number_of_images > 0 && !p.fix_images) return GBA_ERR_INVALID;
+  // point priors weigh free points (ba_gcp_constrained_vector_function.hpp:60-110)
+  if (fixP && p.number_of_point_priors > 0) return GBA_ERR_INVALID;
+  if (!(p.fix_mask & GBA_FIX_CAMERAS)) {
     if ((p.number_of_camera_constraints > 0 && !p.camera_constraints) ||
         p.number_of_camera_constraints < 0)
       return GBA_ERR_INVALID;
@@ -461,10 +481,11 @@ int validate(const gba_problem& p, bool pcg, int threads) {
       (p.number_of_image_constraints > 0 && !p.image_constraints) ||
       p.number_of_point_constraints < 0 || p.number_of_image_constraints < 0)
     return GBA_ERR_INVALID;
-  for (int64_t c = 0; c < p.number_of_point_constraints; ++c)
+  // constraints on a fixed group have no rows (camera_shared_vector_function.hpp:483-629)
+  for (int64_t c = 0; c < (fixP ? 0 : p.number_of_point_constraints); ++c)
     if (p.point_constraints[c].point_id < 0 || p.point_constraints[c].point_id >= p.number_of_points)
       return GBA_ERR_BAD_INDEX;
-  for (int64_t c = 0; c < p.number_of_image_constraints; ++c)
+  for (int64_t c = 0; c < (fixI ? 0 : p.number_of_image_constraints); ++c)
     if (p.image_constraints[c].image_id < 0 || p.image_constraints[c].image_id >= p.number_of_images)
       return GBA_ERR_BAD_INDEX;
   if (p.number_of_point_priors < 0 || (p.number_of_point_priors > 0 && !p.point_prior_ids))
@@ -582,6 +603,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   prob.resize(nprob);
   key_sorted_to_orig.resize(nprob);
   x_size.resize(nprob);
+  fix_pt_vals.assign(nprob, {});
+  fix_img_vals.assign(nprob, {});
 
   // ---- per-problem bases
   std::vector<int64_t> pbase(nprob + 1, 0), ibase(nprob + 1, 0), kbase(nprob + 1, 0),
@@ -615,7 +638,12 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     if (!pcg) s_off += (long long)pi.n * pi.n;   // the dense system only for the factorization
     max_n = std::max(max_n, pi.n);
     max_nt = std::max(max_nt, pi.nt);
-    x_size[q] = 3LL * np + 6LL * ni + (p.fix_mask & GBA_FIX_CAMERAS ? 0 : int64_t(cps) * pi.num_cams);
+    pi.fix = (p.fix_mask & GBA_FIX_POINTS ? 1 : 0) | (p.fix_mask & GBA_FIX_IMAGES ? 2 : 0);
+    pi.pad_ = 0;
+    if (pi.fix & 1) fix_pt_vals[q].assign(p.fix_points, p.fix_points + 3LL * np);
+    if (pi.fix & 2) fix_img_vals[q].assign(p.fix_images, p.fix_images + 6LL * ni);
+    x_size[q] = (pi.fix & 1 ? 0 : 3LL * np) + (pi.fix & 2 ? 0 : 6LL * ni) +
+                (p.fix_mask & GBA_FIX_CAMERAS ? 0 : int64_t(cps) * pi.num_cams);
     pbase[q + 1] = pbase[q] + np;
     ibase[q + 1] = ibase[q] + ni;
     kbase[q + 1] = kbase[q] + nk;
@@ -968,12 +996,13 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
                                            p.constraint_weights ? p.constraint_weights[r] : 1.0));
         ++r;
       };
-      for (int64_t c = 0; c < p.number_of_point_constraints; ++c) {
+      const bool fixP = p.fix_mask & GBA_FIX_POINTS, fixI = p.fix_mask & GBA_FIX_IMAGES;
+      for (int64_t c = 0; c < (fixP ? 0 : p.number_of_point_constraints); ++c) {
         const gba_point_constraint& pc = p.point_constraints[c];
         for (int b = 0; b < 3; ++b)
           if (pc.mask & (1u << b)) add(0, pb + pc.point_id, b);
       }
-      for (int64_t c = 0; c < p.number_of_image_constraints; ++c) {
+      for (int64_t c = 0; c < (fixI ? 0 : p.number_of_image_constraints); ++c) {
         const gba_image_constraint& ic = p.image_constraints[c];
         if (ic.mask & GBA_IMAGE_CONSTRAIN_ROTATION)
           for (int b = 0; b < 3; ++b) add(1, ib + ic.image_id, b);
@@ -1410,45 +1439,59 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.pcg_max_iterations = opt.pcg_max_iterations;
   D.pcg_tol2 = opt.pcg_relative_tolerance * opt.pcg_relative_tolerance;
   if (pcg) {
-    // block-sparse reduced system: global image pair of each block, the
-    // diagonal block of each image, and every image's blocks by neighbour
+    // block-sparse reduced system over the reduced-system images (images,
+    // then the camera parts of free cameras): the global pair of each
+    // block, the diagonal block of each, and each one's blocks by neighbour
+    const int64_t E = I_ext;
     const size_t nb = blk_ij.size();
     std::vector<int2> blk_gij(nb);
-    std::vector<int> img_diag_blk(I, -1), adj_off(I + 1, 0);
+    std::vector<int> img_diag_blk(E, -1), adj_off(E + 1, 0), ext_prob(E, 0);
+    std::vector<Chunk> ext_chunks;
+    std::vector<int> prob_ext_chunk_off(1, 0);
     for (int q = 0; q < nprob; ++q) {
       const ProbInfo& pq = prob[q];
       for (int t = pq.block_begin; t < pq.block_begin + pq.num_blocks; ++t)
-        blk_gij[t] = make_int2(pq.image_begin + blk_ij[t].x, pq.image_begin + blk_ij[t].y);
+        blk_gij[t] = make_int2(pq.ext_begin + blk_ij[t].x, pq.ext_begin + blk_ij[t].y);
+      for (int e = 0; e < pq.num_ext; ++e) ext_prob[pq.ext_begin + e] = q;
+      for (int e = 0; e < pq.num_ext; e += kImageChunk)
+        ext_chunks.push_back(Chunk{q, pq.ext_begin + e, pq.ext_begin + std::min(pq.num_ext, e + kImageChunk), 0});
+      prob_ext_chunk_off.push_back(int(ext_chunks.size()));
     }
     for (size_t t = 0; t < nb; ++t) {
       adj_off[blk_gij[t].x + 1]++;
       if (blk_gij[t].y != blk_gij[t].x) adj_off[blk_gij[t].y + 1]++;
       else img_diag_blk[blk_gij[t].x] = int(t);
     }
-    for (int64_t i = 0; i < I; ++i) adj_off[i + 1] += adj_off[i];
-    std::vector<int2> adj(adj_off[I]);
+    for (int64_t i = 0; i < E; ++i) adj_off[i + 1] += adj_off[i];
+    std::vector<int2> adj(adj_off[E]);
     std::vector<int> fill(adj_off.begin(), adj_off.end() - 1);
     for (size_t t = 0; t < nb; ++t) {
       const int a = blk_gij[t].x, c = blk_gij[t].y;
       adj[fill[a]++] = make_int2(int(t), c << 1);
       if (c != a) adj[fill[c]++] = make_int2(int(t), a << 1 | 1);
     }
-    for (int64_t i = 0; i < I; ++i)
+    for (int64_t i = 0; i < E; ++i)
       std::sort(adj.begin() + adj_off[i], adj.begin() + adj_off[i + 1],
                 [](const int2& u, const int2& v) { return (u.y >> 1) < (v.y >> 1); });
+    for (int64_t i = 0; i < E; ++i)
+      if (img_diag_blk[i] < 0) return GBA_ERR;   // every reduced-system image has its diagonal block
     D.blk_gij = arena.upload(blk_gij);
     D.img_diag_blk = arena.upload(img_diag_blk);
     D.adj_off = arena.upload(adj_off);
     D.adj = arena.upload(adj);
+    D.ext_prob = arena.upload(ext_prob);
+    D.ext_chunks = arena.upload(ext_chunks);
+    D.n_ext_chunks = int(ext_chunks.size());
+    D.prob_ext_chunk_off = arena.upload(prob_ext_chunk_off);
     D.Sblk = arena.alloc<char>(std::max<size_t>(nb, 1) * 36 * tsz);
-    D.Minv = arena.alloc<char>(size_t(std::max<int64_t>(I, 1)) * 36 * tsz);
-    const size_t v6 = size_t(std::max<int64_t>(6 * I, 1)) * tsz;
+    D.Minv = arena.alloc<char>(size_t(std::max<int64_t>(E, 1)) * 36 * tsz);
+    const size_t v6 = size_t(std::max<int64_t>(6 * E, 1)) * tsz;
     D.pcg_r = arena.alloc<char>(v6);
     D.pcg_z = arena.alloc<char>(v6);
     D.pcg_q = arena.alloc<char>(v6);
     D.pcg_p[0] = arena.alloc<char>(v6);
     D.pcg_p[1] = arena.alloc<char>(v6);
-    D.pcg_part = arena.alloc<double>(kPcgSlots * std::max<size_t>(img_chunks.size(), 1));
+    D.pcg_part = arena.alloc<double>(kPcgSlots * std::max<size_t>(ext_chunks.size(), 1));
     D.pcg_done = arena.alloc<int>(nprob);
   }
   if (!pcg)
@@ -1947,14 +1990,14 @@ int gba_plan_set_initial_x(gba_plan* p, int32_t q, const double* x0) {
   return guarded([&] {
     gba::Plan& P = p->impl;
     const gba::ProbInfo& pi = P.prob[q];
-    GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_pt) + 3LL * pi.point_begin, x0,
+    GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_pt) + 3LL * pi.point_begin, P.pts_of(q, x0),
                              sizeof(double) * 3 * pi.num_points, cudaMemcpyHostToDevice, P.stream));
     GBA_CUDA(cudaMemcpyAsync(const_cast<double*>(P.d.x0_img) + 6LL * pi.image_begin,
-                             x0 + 3LL * pi.num_points, sizeof(double) * 6 * pi.num_images,
+                             P.imgs_of(q, x0), sizeof(double) * 6 * pi.num_images,
                              cudaMemcpyHostToDevice, P.stream));
     std::vector<double> cams;
     if (pi.cps > 0) {   // free cameras: cps parameters each, ten-wide on the device
-      const double* xc = x0 + 3LL * pi.num_points + 6LL * pi.num_images;
+      const double* xc = x0 + P.x_cam_off(q);
       cams.assign(10 * size_t(pi.num_cams), 0.0);
       for (int c = 0; c < pi.num_cams; ++c)
         std::copy(xc + (size_t)pi.cps * c, xc + (size_t)pi.cps * (c + 1), cams.begin() + 10 * c);
@@ -1989,10 +2032,12 @@ int gba_plan_get_x(gba_plan* p, int32_t q, double* x) {
     const int par = P.ran ? st.parity : 0;
     const double* xp = P.ran ? P.d.x_pt[par] : P.d.x0_pt;
     const double* xi = P.ran ? P.d.x_img[par] : P.d.x0_img;
-    GBA_CUDA(cudaMemcpyAsync(x, xp + 3LL * pi.point_begin, sizeof(double) * 3 * pi.num_points,
-                             cudaMemcpyDeviceToHost, P.stream));
-    GBA_CUDA(cudaMemcpyAsync(x + 3LL * pi.num_points, xi + 6LL * pi.image_begin,
-                             sizeof(double) * 6 * pi.num_images, cudaMemcpyDeviceToHost, P.stream));
+    if (!(pi.fix & 1))
+      GBA_CUDA(cudaMemcpyAsync(x, xp + 3LL * pi.point_begin, sizeof(double) * 3 * pi.num_points,
+                               cudaMemcpyDeviceToHost, P.stream));
+    if (!(pi.fix & 2))
+      GBA_CUDA(cudaMemcpyAsync(x + P.x_img_off(q), xi + 6LL * pi.image_begin,
+                               sizeof(double) * 6 * pi.num_images, cudaMemcpyDeviceToHost, P.stream));
     std::vector<double> cams;
     if (pi.cps > 0) {
       const double* xc = P.ran ? P.d.x_cam[par] : P.d.x0_cam;
@@ -2001,7 +2046,7 @@ int gba_plan_get_x(gba_plan* p, int32_t q, double* x) {
                                cudaMemcpyDeviceToHost, P.stream));
     }
     GBA_CUDA(cudaStreamSynchronize(P.stream));
-    double* xo = x + 3LL * pi.num_points + 6LL * pi.num_images;
+    double* xo = x + P.x_cam_off(q);
     for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
       std::copy(cams.begin() + 10 * c, cams.begin() + 10 * c + pi.cps, xo + (size_t)pi.cps * c);
     P.d2h_bytes += (long long)sizeof(st) +
@@ -2055,10 +2100,12 @@ int get_all(gba::Plan& P, double* const* xs, gba_report* reports) {
       for (int q = next++; q < P.B; q = next++) {
         const gba::ProbInfo& pi = P.prob[q];
         double* x = xs[q];
-        std::copy(h + 3LL * pi.point_begin, h + 3LL * (pi.point_begin + pi.num_points), x);
-        std::copy(h + np + 6LL * pi.image_begin, h + np + 6LL * (pi.image_begin + pi.num_images),
-                  x + 3LL * pi.num_points);
-        double* xc = x + 3LL * pi.num_points + 6LL * pi.num_images;
+        if (!(pi.fix & 1))
+          std::copy(h + 3LL * pi.point_begin, h + 3LL * (pi.point_begin + pi.num_points), x);
+        if (!(pi.fix & 2))
+          std::copy(h + np + 6LL * pi.image_begin, h + np + 6LL * (pi.image_begin + pi.num_images),
+                    x + P.x_img_off(q));
+        double* xc = x + P.x_cam_off(q);
         for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
           std::copy(h + np + ni + 10LL * (pi.cam_begin + c), h + np + ni + 10LL * (pi.cam_begin + c) + pi.cps,
                     xc + (size_t)pi.cps * c);
@@ -2083,10 +2130,11 @@ int set_all_x0(gba::Plan& P, const double* const* xs) {
       for (int q = next++; q < P.B; q = next++) {
         const gba::ProbInfo& pi = P.prob[q];
         const double* x = xs[q];
-        std::copy(x, x + 3LL * pi.num_points, h + 3LL * pi.point_begin);
-        std::copy(x + 3LL * pi.num_points, x + 3LL * pi.num_points + 6LL * pi.num_images,
-                  h + np + 6LL * pi.image_begin);
-        const double* xc = x + 3LL * pi.num_points + 6LL * pi.num_images;
+        const double* xp = P.pts_of(q, x);
+        const double* xi = P.imgs_of(q, x);
+        std::copy(xp, xp + 3LL * pi.num_points, h + 3LL * pi.point_begin);
+        std::copy(xi, xi + 6LL * pi.num_images, h + np + 6LL * pi.image_begin);
+        const double* xc = x + P.x_cam_off(q);
         for (int c = 0; c < (pi.cps > 0 ? pi.num_cams : 0); ++c)
           std::copy(xc + (size_t)pi.cps * c, xc + (size_t)pi.cps * (c + 1), h + np + ni + 10LL * (pi.cam_begin + c));
       }
@@ -2371,15 +2419,17 @@ int gba_vector_function(const gba_problem* problem, const double* x, double* y, 
       y[2 * perm[t]] = ys[2 * t];
       y[2 * perm[t] + 1] = ys[2 * t + 1];
     }
-    // constraint rows copy their parameter (x = [points 3P][images 6I])
+    // constraint rows copy their parameter (x = [points 3P][images 6I]
+    // [cameras], fixed groups dropped; a fixed group has no rows)
     int64_t r = 2 * problem->number_of_keys;
-    const int64_t img0 = 3 * problem->number_of_points;
-    for (int64_t c = 0; c < problem->number_of_point_constraints; ++c) {
+    const bool fixP = problem->fix_mask & GBA_FIX_POINTS, fixI = problem->fix_mask & GBA_FIX_IMAGES;
+    const int64_t img0 = P.x_img_off(0);
+    for (int64_t c = 0; c < (fixP ? 0 : problem->number_of_point_constraints); ++c) {
       const gba_point_constraint& pc = problem->point_constraints[c];
       for (int b = 0; b < 3; ++b)
         if (pc.mask & (1u << b)) y[r++] = x[3 * pc.point_id + b];
     }
-    for (int64_t c = 0; c < problem->number_of_image_constraints; ++c) {
+    for (int64_t c = 0; c < (fixI ? 0 : problem->number_of_image_constraints); ++c) {
       const gba_image_constraint& ic = problem->image_constraints[c];
       const double* xi = x + img0 + 6 * ic.image_id;
       if (ic.mask & GBA_IMAGE_CONSTRAIN_ROTATION)
@@ -2391,7 +2441,7 @@ int gba_vector_function(const gba_problem* problem, const double* x, double* y, 
     if (!(problem->fix_mask & GBA_FIX_CAMERAS)) {
       const uint32_t m = problem->intrinsic_computations_mask;
       const int64_t cps = gba::params_per_camera(m);
-      const double* xc = x + img0 + 6 * problem->number_of_images;
+      const double* xc = x + P.x_cam_off(0);
       for (int64_t c = 0; c < problem->number_of_camera_constraints; ++c) {
         const gba_camera_constraint& cc = problem->camera_constraints[c];
         const double* xv = xc + cps * cc.camera_id;
@@ -2539,13 +2589,15 @@ int gba_schur_step(const gba_problem* problem, const double* x, const double* ne
     } else {
       GBA_CUDA(cudaMemcpy(di.data(), P.d.b, sizeof(double) * di.size(), cudaMemcpyDeviceToHost));
     }
-    for (size_t i = 0; i < x0p.size(); ++i) delta_x[i] = x0p[i] - x1p[i];
-    std::copy(di.begin(), di.end(), delta_x + x0p.size());
+    // the free groups only, in the caller's x layout
+    if (!(pi.fix & 1))
+      for (size_t i = 0; i < x0p.size(); ++i) delta_x[i] = x0p[i] - x1p[i];
+    if (!(pi.fix & 2)) std::copy(di.begin(), di.end(), delta_x + P.x_img_off(0));
     if (pi.cps > 0) {   // free cameras: x_c - (x_c - delta_c)
       std::vector<double> c0(10 * size_t(pi.num_cams)), c1(c0.size());
       GBA_CUDA(cudaMemcpy(c0.data(), P.d.x_cam[0], sizeof(double) * c0.size(), cudaMemcpyDeviceToHost));
       GBA_CUDA(cudaMemcpy(c1.data(), P.d.x_cam[1], sizeof(double) * c1.size(), cudaMemcpyDeviceToHost));
-      double* dc = delta_x + x0p.size() + di.size();
+      double* dc = delta_x + P.x_cam_off(0);
       for (int c = 0; c < pi.num_cams; ++c)
         for (int m = 0; m < pi.cps; ++m) dc[(size_t)pi.cps * c + m] = c0[10 * c + m] - c1[10 * c + m];
     }

@@ -65,6 +65,20 @@ def test_headline_grid_matches_oracle(gba, grid, precision):
         assert rep.accepted == rref.accepted
 
 
+def test_headline_free_intrinsics_grid_matches_oracle(gba):
+    """The same grid with the shared camera free (radial + intrinsic
+    parameters, 1,212 reduced-system unknowns), as bench.py times it: the
+    mixed path by the acceptance rule."""
+    s = synthetic.config(1, fix_mask=0)
+    err, _, rref = oracle.lm_solve(s, options=_opts(abi.PRECISION_FP64, GRID_ITERS))
+    assert err == 0
+    x, rep = gba.solve(s, _opts(abi.PRECISION_MIXED, GRID_ITERS))
+    assert rep.status == 0
+    rel = abs(rep.final_cost - rref.final_cost) / rref.final_cost
+    assert rel <= COST_RTOL, (rep.final_cost, rref.final_cost, rel)
+    assert abs(rep.final_rmse - rref.final_rmse) <= RMSE_ATOL
+
+
 def test_headline_windows_match_oracle(gba):
     wins = synthetic.window_batch(num_windows=512, seed=3)[::16]
     xs, reps = gba.solve_batch(wins, _opts(abi.PRECISION_MIXED, WINDOW_ITERS))

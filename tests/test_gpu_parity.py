@@ -262,10 +262,10 @@ def test_errors_are_reported(gba):
     with pytest.raises(gba.GbaError) as e:
         gba.solve(dup)
     assert e.value.status == abi.GBA_ERR_DUPLICATE
-    fixed_points = synthetic.Scene(**{**s.__dict__})
-    fixed_points.fix_mask = abi.FIX_POINTS | abi.FIX_CAMERAS
+    all_fixed = synthetic.Scene(**{**s.__dict__})
+    all_fixed.fix_mask = abi.FIX_POINTS | abi.FIX_IMAGES | abi.FIX_CAMERAS
     with pytest.raises(gba.GbaError) as e:
-        gba.solve(fixed_points, x0=s.x0[3 * s.number_of_points:])
+        gba.solve(all_fixed, x0=np.zeros(0))
     assert e.value.status == abi.GBA_ERR_UNSUPPORTED
 
 

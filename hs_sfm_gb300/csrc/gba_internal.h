@@ -22,7 +22,7 @@ constexpr int kTile = 32;          // dense Cholesky tile
 constexpr int kDfTraceCap = 1024;   // traced tasks per CTA of the dataflow factorization
 constexpr int kPcgSlots = 8;        // PCG partial sums per image chunk
 constexpr int kImgCamVals = 128;   // per image item: E (6x10), U_c upper (55), g_c (10), pad
-constexpr int kKeyChunk = 1024;    // keys per key work chunk (cost partial sums per chunk)
+constexpr int kKeyChunk = 1024;    // default keys per key work chunk (gba_options.key_item)
 constexpr int kPointChunk = 128;   // points per point work chunk
 constexpr int kImageChunk = 8;     // images per image work chunk (backsub)
 constexpr int kImageItem = 512;    // keys per image-reduce work item (warp each)
@@ -187,6 +187,7 @@ struct DevPlan {
   double* item_partial;      // [items * kItemStride]
   // work chunks and their partial sums (FP64)
   int n_key_chunks, n_pt_chunks, n_img_chunks;
+  int key_z_split;                // CTAs of 256 keys per key chunk in the Z kernel
   const Chunk* key_chunks;
   const Chunk* pt_chunks;
   const Chunk* img_chunks;

@@ -1146,21 +1146,20 @@ __global__ void __launch_bounds__(kPointChunk) k_point_factor(DevPlan d) {
   store_vec<12>(tptr_mut<T>(d.PS) + 12LL * pt, ps);
 }
 
-// Z_a = C_p^-1 J_p^T J_i per key (coalesced records).  kKeyZSplit CTAs
-// share each key chunk (one key per thread), so the grid fills the GPU in
-// even waves.
-constexpr int kKeyZSplit = kKeyChunk / 256;
-
+// Z_a = C_p^-1 J_p^T J_i per key (coalesced records).  DevPlan::key_z_split
+// CTAs share each key chunk (one key per thread), so the grid fills the GPU
+// in even waves.
 template <typename T>
 __global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
-  const Chunk ch = d.key_chunks[blockIdx.x / kKeyZSplit];
+  const int split = d.key_z_split;
+  const Chunk ch = d.key_chunks[blockIdx.x / split];
   const LMState& st = d.state[ch.prob];
   if (!st.active) return;
   const T* __restrict__ JR = tptr<T>(d.JR);
   const T* __restrict__ PS = tptr<T>(d.PS);
   T* __restrict__ Z = tptr_mut<T>(d.Z);
-  const int sub = blockIdx.x % kKeyZSplit;
-  for (int k = ch.begin + sub * 256 + threadIdx.x; k < ch.end; k += kKeyZSplit * 256) {
+  const int sub = blockIdx.x % split;
+  for (int k = ch.begin + sub * 256 + threadIdx.x; k < ch.end; k += split * 256) {
     T rec[kJRStride], ps[8];
     load_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
     load_vec<8>(PS + 12LL * __ldg(d.key_pt + k), ps);
@@ -3248,7 +3247,7 @@ int launch_point_schur(const DevPlan& d, cudaStream_t s) {
     ++n;
   }
   if (d.n_key_chunks > 0) {
-    GBA_DISPATCH(d, (k_key_z<T><<<d.n_key_chunks * kKeyZSplit, 256, 0, s>>>(d)));
+    GBA_DISPATCH(d, (k_key_z<T><<<d.n_key_chunks * d.key_z_split, 256, 0, s>>>(d)));
     ++n;
   }
   if (d.free_cams && d.R > 0) {

@@ -675,6 +675,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   // work-item sizes of the Schur assembly and the image reduction
   const int pair_item = opt.pair_item > 0 ? opt.pair_item : kPairItem;
   const int image_item = opt.image_item > 0 ? opt.image_item : kImageItem;
+  const int key_item = opt.key_item > 0 ? opt.key_item : kKeyChunk;
   // plans without free cameras count, number and place their key pairs on
   // the device (GBA_HOST_PAIRS=1 keeps the host build, for comparison); the
   // per-code tables take 12 bytes per (image, image) entry of every problem
@@ -1166,7 +1167,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       b.items += std::max<long long>(1, (cntp + pair_item - 1) / pair_item);
     }
     b.blk_map += (long long)pc.blk_map.size();
-    b.key_chunks += (nk + kKeyChunk - 1) / kKeyChunk;
+    b.key_chunks += (nk + key_item - 1) / key_item;
     b.pt_chunks += (np + kPointChunk - 1) / kPointChunk;
     b.img_chunks += (ni + kImageChunk - 1) / kImageChunk;
     b.cons += (long long)pc.cons.size();
@@ -1275,8 +1276,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
         blk_map[b.blk_map + e] = pc.blk_map[e] >= 0 ? pc.blk_map[e] + block_begin : -1;
     // work chunks
     long long c = b.key_chunks;
-    for (int s_ = 0; s_ < nk; s_ += kKeyChunk)
-      key_chunks[c++] = Chunk{q, int(kb + s_), int(kb + std::min(nk, s_ + kKeyChunk)), 0};
+    for (int s_ = 0; s_ < nk; s_ += key_item)
+      key_chunks[c++] = Chunk{q, int(kb + s_), int(kb + std::min(nk, s_ + key_item)), 0};
     c = b.pt_chunks;
     for (int s_ = 0; s_ < np; s_ += kPointChunk)
       pt_chunks[c++] = Chunk{q, int(pb + s_), int(pb + std::min(np, s_ + kPointChunk)), 0};
@@ -1571,6 +1572,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.blk_map_off = arena.upload(blk_map_off);
   D.item_partial = arena.alloc<double>(size_t(kItemStride) * std::max<size_t>(items.size(), 1));
   D.n_key_chunks = int(key_chunks.size());
+  D.key_z_split = (key_item + 255) / 256;   // one key per thread of the Z kernel
   D.n_pt_chunks = int(pt_chunks.size());
   D.n_img_chunks = int(img_chunks.size());
   D.key_chunks = arena.upload(key_chunks);
@@ -1961,7 +1963,7 @@ int gba_plan_create(const gba_problem* problems, const double* const* near_ys, i
     return GBA_ERR_INVALID;
   if (options->max_iterations < 0 || !(options->function_tolerance >= 0.0)) return GBA_ERR_INVALID;
   if (options->pair_item < 0 || options->image_item < 0 || options->pair_item > (1 << 24) ||
-      options->image_item > (1 << 24))
+      options->image_item > (1 << 24) || options->key_item < 0 || options->key_item > (1 << 24))
     return GBA_ERR_INVALID;
   gba_plan* p = nullptr;
   try {
@@ -2317,10 +2319,11 @@ int gba_autotune(const gba_problem* problems, const double* const* near_ys, cons
   int timed = 0;
   // one candidate: a plan, a warm-up run (graph capture), the best of three
   // timed replays, per LM iteration
-  auto time_one = [&](int pair_item, int image_item, double* ms_per_it) -> int {
+  auto time_one = [&](int pair_item, int image_item, int key_item, double* ms_per_it) -> int {
     gba_options o = base;
     o.pair_item = pair_item;
     o.image_item = image_item;
+    o.key_item = key_item;
     gba_plan* plan = nullptr;
     int err = gba_plan_create(problems, near_ys, n, &o, &plan);
     if (err) return err;
@@ -2340,25 +2343,33 @@ int gba_autotune(const gba_problem* problems, const double* const* near_ys, cons
     return GBA_OK;
   };
   double t_default = 0.0;
-  if (int e = time_one(gba::kPairItem, gba::kImageItem, &t_default)) return e;
-  int best_pair = gba::kPairItem, best_image = gba::kImageItem;
+  if (int e = time_one(gba::kPairItem, gba::kImageItem, gba::kKeyChunk, &t_default)) return e;
+  int best_pair = gba::kPairItem, best_image = gba::kImageItem, best_key = gba::kKeyChunk;
   double t_best = t_default;
   for (int pi : {256, 512, 2048, 4096}) {
     double t = 0.0;
-    if (time_one(pi, gba::kImageItem, &t) == GBA_OK && t < t_best) {
+    if (time_one(pi, gba::kImageItem, gba::kKeyChunk, &t) == GBA_OK && t < t_best) {
       t_best = t;
       best_pair = pi;
     }
   }
   for (int ii : {256, 1024}) {
     double t = 0.0;
-    if (time_one(best_pair, ii, &t) == GBA_OK && t < t_best) {
+    if (time_one(best_pair, ii, gba::kKeyChunk, &t) == GBA_OK && t < t_best) {
       t_best = t;
       best_image = ii;
     }
   }
+  for (int ki : {256, 512, 2048}) {
+    double t = 0.0;
+    if (time_one(best_pair, best_image, ki, &t) == GBA_OK && t < t_best) {
+      t_best = t;
+      best_key = ki;
+    }
+  }
   out->pair_item = best_pair;
   out->image_item = best_image;
+  out->key_item = best_key;
   out->ms_per_iteration = t_best;
   out->default_ms_per_iteration = t_default;
   out->candidates = timed;

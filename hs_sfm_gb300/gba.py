@@ -137,9 +137,9 @@ def solve_batch(scenes, options=None):
 
 
 def autotune(scenes, options=None):
-    """gba_autotune: the work-item sizes (pair_item, image_item) that run the
-    batch fastest, timed on the device; returns a dict with the choice, its
-    time per LM iteration and that of the defaults."""
+    """gba_autotune: the work-item sizes (pair_item, image_item, key_item)
+    that run the batch fastest, timed on the device; returns a dict with the
+    choice, its time per LM iteration and that of the defaults."""
     L = lib()
     if not isinstance(scenes, (list, tuple)):
         scenes = [scenes]
@@ -152,7 +152,7 @@ def autotune(scenes, options=None):
     opt = options if options is not None else abi.make_options()
     t = abi.Tuning()
     _check(L.gba_autotune(arr, yp, xp, len(scenes), C.byref(opt), C.byref(t)), "gba_autotune")
-    return {"pair_item": t.pair_item, "image_item": t.image_item,
+    return {"pair_item": t.pair_item, "image_item": t.image_item, "key_item": t.key_item,
             "ms_per_iteration": t.ms_per_iteration,
             "default_ms_per_iteration": t.default_ms_per_iteration, "candidates": t.candidates}
 

@@ -182,25 +182,32 @@ typedef struct gba_options {
    * block sums, not the model; gba_autotune picks them for a batch. */
   int32_t pair_item;
   int32_t image_item;
-  int32_t reserved_[2];
+  /* Keys per key work chunk (0: 1024): the unit of the cost, Jacobian and
+   * Z kernels and of the cost's partial sums (so it changes the rounding of
+   * the cost sum, not the model); gba_autotune picks it with the others. */
+  int32_t key_item;
+  int32_t reserved_[1];
 } gba_options;
 
-/* Autotuning of the work-item sizes (gba_options.pair_item / image_item)
- * for a batch: every candidate builds a plan of the given problems (initial
- * x0 per problem) with the given options (at most two LM iterations,
- * stopping tests off, graph replay), runs it
- * once to warm up and is timed over three graph replays (CUDA events on the
- * plan's stream); pair_item is searched first over {256, 512, 1024, 2048,
- * 4096} with the default image_item, then image_item over {256, 512, 1024}
- * with the best pair_item.  out receives the fastest pair and its time per
- * LM iteration beside that of the defaults.  A status code. */
+/* Autotuning of the work-item sizes (gba_options.pair_item / image_item /
+ * key_item) for a batch: every candidate builds a plan of the given
+ * problems (initial x0 per problem) with the given options (at most two LM
+ * iterations, stopping tests off, graph replay), runs it once to warm up and
+ * is timed over three graph replays (CUDA events on the plan's stream);
+ * pair_item is searched first over {256, 512, 1024, 2048, 4096} with the
+ * default image_item and key_item, then image_item over {256, 512, 1024}
+ * with the best pair_item, then key_item over {256, 512, 1024, 2048} with
+ * the best two.  out receives the fastest sizes and their time per LM
+ * iteration beside that of the defaults.  A status code. */
 typedef struct gba_tuning {
   int32_t pair_item;
   int32_t image_item;
   double ms_per_iteration;           /* the chosen item sizes              */
-  double default_ms_per_iteration;   /* pair_item 1024, image_item 512     */
+  double default_ms_per_iteration;   /* pair_item 1024, image_item 512,
+                                        key_item 1024                      */
   int32_t candidates;                /* configurations timed               */
-  int32_t reserved_[3];
+  int32_t key_item;
+  int32_t reserved_[2];
 } gba_tuning;
 
 GBA_API int gba_autotune(const gba_problem* problems, const double* const* near_ys,

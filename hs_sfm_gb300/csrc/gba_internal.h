@@ -240,6 +240,12 @@ struct DevPlan {
   double* pt_chunk_sum;           // [3 * n_pt_chunks] dn2, xn2, gd
   double* img_chunk_sum;          // [3 * n_img_chunks]
   unsigned long long* launch_counter; // device-side count (unused: host counts)
+  // LM control folded into the producers: the last CTA of a problem to
+  // finish k_backsub runs the step decision and the last of the candidate
+  // cost the accept decision (no k_ctrl_step / k_ctrl_accept launches).
+  // fold_count [2B]: per problem the arrival counters of the two kernels.
+  int fold_ctrl;
+  unsigned* fold_count;
 };
 
 // A failed CUDA call on the host side of a plan (GBA_ERR_* status).

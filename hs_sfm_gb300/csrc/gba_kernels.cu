@@ -138,6 +138,32 @@ __device__ double block_sum(double v, double* smem) {
   return r;
 }
 
+// Arrival of this CTA at problem p's counter after thread 0 has written the
+// CTA's partial sums; true in every thread of the CTA that arrives last of
+// `total` (which then runs the problem's LM control step and resets the
+// counter for the next launch).  The fence orders this CTA's partials
+// before its arrival; the last CTA reads the others' through L2.
+__device__ bool last_arrival(unsigned* counter, int total, int* flag_smem) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    const int last = prev == unsigned(total - 1);
+    if (last) {
+      atomicExch(counter, 0u);
+      __threadfence();
+    }
+    *flag_smem = last;
+  }
+  __syncthreads();
+  return *flag_smem != 0;
+}
+
+template <bool CG>
+__device__ void ctrl_step_body(const DevPlan& d, int p, double* red);
+template <bool CG>
+__device__ void ctrl_accept_body(const DevPlan& d, int p, double* red);
+
 __device__ double block_max(double v, double* smem) {
   v = warp_max(v);
   int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -611,6 +637,13 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
     d.key_chunk_sum[2LL * blockIdx.x] = tot;
     d.key_chunk_sum[2LL * blockIdx.x + 1] = tot_raw;
   }
+  if (which == 1 && d.fold_ctrl) {   // the accept decision in the last CTA of the problem
+    __shared__ int last;
+    const int p = ch.prob;
+    if (last_arrival(d.fold_count + 2 * p + 1,
+                     d.prob_key_chunk_off[p + 1] - d.prob_key_chunk_off[p], &last))
+      ctrl_accept_body<true>(d, p, red);
+  }
 }
 
 // Mixed-path cost: the projection in double-float from the double-float
@@ -695,6 +728,13 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
   if (threadIdx.x == 0) {
     d.key_chunk_sum[2LL * blockIdx.x] = tot;
     d.key_chunk_sum[2LL * blockIdx.x + 1] = tot_raw;
+  }
+  if (which == 1 && d.fold_ctrl) {   // the accept decision in the last CTA of the problem
+    __shared__ int last;
+    const int p = ch.prob;
+    if (last_arrival(d.fold_count + 2 * p + 1,
+                     d.prob_key_chunk_off[p + 1] - d.prob_key_chunk_off[p], &last))
+      ctrl_accept_body<true>(d, p, red);
   }
 }
 
@@ -2751,10 +2791,18 @@ __global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
 template <typename T>
 __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
   __shared__ double red[32];
-  if (blockIdx.x < d.n_pt_chunks) {
+  // With DevPlan::fold_ctrl the last CTA of a problem to finish runs the LM
+  // step decision (k_ctrl_step's body), so every CTA of an active problem
+  // arrives, also when the factorization failed and there is nothing to do.
+  const int prob = blockIdx.x < d.n_pt_chunks ? d.pt_chunks[blockIdx.x].prob
+                                              : d.img_chunks[blockIdx.x - d.n_pt_chunks].prob;
+  if (!d.state[prob].active) return;
+  const bool failed = d.factor_flag[prob] != 0;
+  if (failed) {
+    // nothing to compute
+  } else if (blockIdx.x < d.n_pt_chunks) {
     const Chunk ch = d.pt_chunks[blockIdx.x];
     const LMState& st = d.state[ch.prob];
-    if (!st.active || d.factor_flag[ch.prob]) return;
     const int par = st.parity;
     const int pt = ch.begin + threadIdx.x;
     double dn2 = 0.0, xn2 = 0.0, gd = 0.0;
@@ -2814,7 +2862,6 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
     const int c = blockIdx.x - d.n_pt_chunks;
     const Chunk ch = d.img_chunks[c];
     const LMState& st = d.state[ch.prob];
-    if (!st.active || d.factor_flag[ch.prob]) return;
     const int par = st.parity;
     double dn2 = 0.0, xn2 = 0.0, gd = 0.0;
     const long long e0 = 6LL * ch.begin, e1 = 6LL * ch.end;
@@ -2836,6 +2883,12 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       d.img_chunk_sum[3LL * c + 1] = s1;
       d.img_chunk_sum[3LL * c + 2] = s2;
     }
+  }
+  if (d.fold_ctrl) {
+    __shared__ int last;
+    const int total = d.prob_pt_chunk_off[prob + 1] - d.prob_pt_chunk_off[prob] +
+                      d.prob_img_chunk_off[prob + 1] - d.prob_img_chunk_off[prob];
+    if (last_arrival(d.fold_count + 2 * prob, total, &last)) ctrl_step_body<true>(d, prob, red);
   }
 }
 
@@ -2873,18 +2926,21 @@ __global__ void k_cam_backsub(DevPlan d) {
 // adds chunks t, t + blockDim, ... in order, then a fixed-shape tree):
 // deterministic, and each thread waits on a few loads instead of one warp
 // walking hundreds of chunks.  Result valid in thread 0.
+// CG: the partials were written by other CTAs of the running kernel, so
+// they are read through L2 (ld.global.cg), never from a stale L1 line.
+template <bool CG = false>
 __device__ double prob_sum(const double* v, int stride, int off, const int* chunk_off, int p,
                            double* red) {
   double s = 0.0;
   for (int c = chunk_off[p] + threadIdx.x; c < chunk_off[p + 1]; c += blockDim.x)
-    s += v[(long long)stride * c + off];
+    s += CG ? __ldcg(v + (long long)stride * c + off) : v[(long long)stride * c + off];
   return block_sum(s, red);
 }
 
 // The first NF fields of a problem's chunk partials (stride fields per
 // chunk) summed in one pass: each thread walks its chunks with NF loads per
 // chunk, four chunks in flight, then fixed-shape trees.  Results in thread 0.
-template <int NF>
+template <int NF, bool CG = false>
 __device__ void prob_sums(const double* v, int stride, const int* chunk_off, int p, double* red,
                           double* out) {
   double s[NF];
@@ -2894,7 +2950,8 @@ __device__ void prob_sums(const double* v, int stride, const int* chunk_off, int
 #pragma unroll 4
   for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
 #pragma unroll
-    for (int f = 0; f < NF; ++f) s[f] += v[(long long)stride * c + f];
+    for (int f = 0; f < NF; ++f)
+      s[f] += CG ? __ldcg(v + (long long)stride * c + f) : v[(long long)stride * c + f];
   }
 #pragma unroll
   for (int f = 0; f < NF; ++f) out[f] = block_sum(s[f], red);
@@ -2947,25 +3004,27 @@ __global__ void k_ctrl_after_linearize(DevPlan d) {
   d.factor_flag[p] = 0;
 }
 
-__global__ void __launch_bounds__(kCtrlThreads) k_ctrl_step(DevPlan d) {
-  __shared__ double red[32];
-  const int p = blockIdx.x;
+// The LM step decision of problem p from the back-substitution's partial
+// sums (every thread of the CTA takes part; thread 0 decides).  Run by
+// k_ctrl_step, or (CG = true) by the last CTA of k_backsub to finish for p.
+template <bool CG>
+__device__ void ctrl_step_body(const DevPlan& d, int p, double* red) {
   LMState& st = d.state[p];
   if (!st.active) return;
   const bool failed = d.factor_flag[p] != 0;
   double dn2 = 0, xn2 = 0, gd = 0, er = 0;
   if (!failed) {
     double sp[3], si[3];
-    prob_sums<3>(d.pt_chunk_sum, 3, d.prob_pt_chunk_off, p, red, sp);
-    prob_sums<3>(d.img_chunk_sum, 3, d.prob_img_chunk_off, p, red, si);
+    prob_sums<3, CG>(d.pt_chunk_sum, 3, d.prob_pt_chunk_off, p, red, sp);
+    prob_sums<3, CG>(d.img_chunk_sum, 3, d.prob_img_chunk_off, p, red, si);
     dn2 = sp[0] + si[0];
     xn2 = sp[1] + si[1];
     gd = sp[2] + si[2];
     // PCG leaves the image rows with residual r: the model decrease gains r^T delta_i
-    if (d.pcg) er = prob_sum(d.pcg_part, kPcgSlots, 6, d.prob_ext_chunk_off, p, red);
+    if (d.pcg) er = prob_sum<CG>(d.pcg_part, kPcgSlots, 6, d.prob_ext_chunk_off, p, red);
     if (d.free_cams) {
       double sc[3];
-      prob_sums<3>(d.cam_sum, 3, d.prob_cam_off, p, red, sc);
+      prob_sums<3, CG>(d.cam_sum, 3, d.prob_cam_off, p, red, sc);
       dn2 += sc[0];
       xn2 += sc[1];
       gd += sc[2];
@@ -2999,13 +3058,20 @@ __global__ void __launch_bounds__(kCtrlThreads) k_ctrl_step(DevPlan d) {
   }
 }
 
-__global__ void __launch_bounds__(kCtrlThreads) k_ctrl_accept(DevPlan d) {
+__global__ void __launch_bounds__(kCtrlThreads) k_ctrl_step(DevPlan d) {
   __shared__ double red[32];
-  const int p = blockIdx.x;
+  ctrl_step_body<false>(d, blockIdx.x, red);
+}
+
+// The LM accept / reject decision of problem p from the candidate cost's
+// partial sums.  Run by k_ctrl_accept, or (CG = true) by the last CTA of the
+// candidate cost kernel to finish for p.
+template <bool CG>
+__device__ void ctrl_accept_body(const DevPlan& d, int p, double* red) {
   LMState& st = d.state[p];
   if (!st.evaluate) return;
   double fr[2];
-  prob_sums<2>(d.key_chunk_sum, 2, d.prob_key_chunk_off, p, red, fr);
+  prob_sums<2, CG>(d.key_chunk_sum, 2, d.prob_key_chunk_off, p, red, fr);
   if (threadIdx.x != 0) return;
   double Fn = fr[0];
   const double raw_n = fr[1];
@@ -3036,6 +3102,11 @@ __global__ void __launch_bounds__(kCtrlThreads) k_ctrl_accept(DevPlan d) {
     st.nu *= 2.0;
     st.rejected += 1;
   }
+}
+
+__global__ void __launch_bounds__(kCtrlThreads) k_ctrl_accept(DevPlan d) {
+  __shared__ double red[32];
+  ctrl_accept_body<false>(d, blockIdx.x, red);
 }
 
 // The observed keys as double-float pairs (hi = float(v), lo = float(v - hi)).
@@ -3192,15 +3263,17 @@ int launch_image_prep(const DevPlan& d, int which, cudaStream_t s) {
 
 int launch_cost(const DevPlan& d, int which, cudaStream_t s) {
   int n = 0;
+  // constraint and prior terms first: the accept decision folded into the
+  // key cost kernel adds them
+  if (d.n_cons > 0 || d.n_priors > 0) {
+    k_cons_cost<<<d.B, 256, 0, s>>>(d, which);
+    ++n;
+  }
   if (d.n_key_chunks > 0) {
     if (d.precision == GBA_PRECISION_MIXED)
       k_cost_ff<<<d.n_key_chunks, 256, 0, s>>>(d, which);
     else
       k_cost<double><<<d.n_key_chunks, 256, 0, s>>>(d, which);
-    ++n;
-  }
-  if (d.n_cons > 0 || d.n_priors > 0) {
-    k_cons_cost<<<d.B, 256, 0, s>>>(d, which);
     ++n;
   }
   return n;
@@ -3409,18 +3482,25 @@ int launch_cholesky(const DevPlan& d, cudaStream_t s) {
 int launch_backsub(const DevPlan& d, cudaStream_t s) {
   const int g = d.n_pt_chunks + d.n_img_chunks;
   if (g <= 0) return 0;
+  int n = 0;
+  // the cameras' step first: with the control folded into k_backsub, its
+  // last CTA reads the cameras' partial sums too
+  if (d.free_cams && d.Ctot > 0) {
+    GBA_DISPATCH(d, (k_cam_backsub<T><<<(d.Ctot + 127) / 128, 128, 0, s>>>(d)));
+    ++n;
+  }
   GBA_DISPATCH(d, (k_backsub<T><<<g, kPointChunk, 0, s>>>(d)));
-  if (!d.free_cams || d.Ctot <= 0) return 1;
-  GBA_DISPATCH(d, (k_cam_backsub<T><<<(d.Ctot + 127) / 128, 128, 0, s>>>(d)));
-  return 2;
+  return n + 1;
 }
 
 int launch_ctrl_step(const DevPlan& d, cudaStream_t s) {
+  if (d.fold_ctrl) return 0;   // done by the last CTA of each problem in k_backsub
   k_ctrl_step<<<d.B, kCtrlThreads, 0, s>>>(d);
   return 1;
 }
 
 int launch_ctrl_accept(const DevPlan& d, cudaStream_t s) {
+  if (d.fold_ctrl) return 0;   // done by the last CTA of each problem in the candidate cost
   k_ctrl_accept<<<d.B, kCtrlThreads, 0, s>>>(d);
   return 1;
 }

@@ -1582,6 +1582,19 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.prob_pt_chunk_off = arena.upload(prob_pt_chunk_off);
   D.prob_img_chunk_off = arena.upload(prob_img_chunk_off);
   D.key_chunk_sum = arena.alloc<double>(2 * std::max<size_t>(key_chunks.size(), 1));
+  // the LM control folded into k_backsub and the candidate cost: every
+  // problem needs a CTA in both (keys, and points or images);
+  // GBA_CTRL_KERNELS=1 keeps the separate control launches
+  {
+    bool fold = std::getenv("GBA_CTRL_KERNELS") == nullptr;
+    for (int q = 0; q < nprob && fold; ++q)
+      fold = prob_key_chunk_off[q + 1] > prob_key_chunk_off[q] &&
+             (prob_pt_chunk_off[q + 1] > prob_pt_chunk_off[q] ||
+              prob_img_chunk_off[q + 1] > prob_img_chunk_off[q]);
+    D.fold_ctrl = fold ? 1 : 0;
+    D.fold_count = arena.alloc<unsigned>(2 * size_t(std::max(nprob, 1)));
+    GBA_CUDA(cudaMemsetAsync(D.fold_count, 0, sizeof(unsigned) * 2 * size_t(std::max(nprob, 1)), stream));
+  }
   D.n_cons = int(cons.size());
   D.cons = nullptr;
   D.pt_cons_off = nullptr;

@@ -353,3 +353,33 @@ def test_batch_create_submit_poll(gba):
             np.testing.assert_array_equal(xs[q], ref_x[q])
             assert reps[q].final_cost == ref_r[q].final_cost
     assert L.gba_batch_destroy(h) == abi.GBA_OK
+
+
+def test_folded_control_matches_control_kernels(gba, monkeypatch):
+    """The LM step and accept decisions run in the last CTA of the
+    back-substitution and of the candidate cost (no separate control
+    launches); the same solve with the separate control kernels
+    (GBA_CTRL_KERNELS=1) follows the same trajectory (the sums over chunk
+    partials are taken by CTAs of another width, so the bits may differ)."""
+    s = distorted_ring(seed=17, num_images=12, num_points=900, k=5)
+    for precision in (abi.PRECISION_FP64, abi.PRECISION_MIXED):
+        opt = _lm_opts(precision, 12)
+        x1, r1 = gba.solve(s, opt)
+        plan = gba.Plan([s], _lm_opts(precision, 12))
+        plan.run()
+        plan.synchronize()
+        launches_folded = plan.launches()
+        plan.close()
+        monkeypatch.setenv("GBA_CTRL_KERNELS", "1")
+        x2, r2 = gba.solve(s, opt)
+        plan = gba.Plan([s], _lm_opts(precision, 12))
+        plan.run()
+        plan.synchronize()
+        launches_kernels = plan.launches()
+        plan.close()
+        monkeypatch.delenv("GBA_CTRL_KERNELS")
+        assert r1.status == r2.status == abi.GBA_OK
+        assert (r1.accepted, r1.rejected, r1.iterations) == (r2.accepted, r2.rejected, r2.iterations)
+        assert abs(r1.final_cost - r2.final_cost) <= 1e-10 * r2.final_cost
+        np.testing.assert_allclose(x1, x2, rtol=1e-8, atol=1e-8)
+        assert launches_folded == launches_kernels - 2 * 12

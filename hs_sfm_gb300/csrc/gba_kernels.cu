@@ -3392,8 +3392,12 @@ bool dataflow_layout_t(int nt, int device, int* grid, int* max_own, std::vector<
   const long long ntiles = (long long)nt * (nt + 1) / 2;
   const int G = int(std::min<long long>(sms, ntiles));
   // row i's diagonal tile and its left neighbour go to CTA i mod G; the
-  // rest, heaviest first, to the CTA with the least work so far
+  // rest, heaviest first, to the CTA with the least work so far.  When
+  // there are at least twice as many CTAs as tile rows, the chain's CTAs
+  // take none of the rest: a CTA busy with an update when its row's chain
+  // task becomes ready would delay the chain by that update
   std::vector<std::vector<int2>> lists(G);
+  const int first_worker = (G >= 2 * nt) ? nt : 0;
   std::vector<long long> load(G, 0);
   for (int i = 0; i < nt; ++i) {
     const int g = i % G;
@@ -3409,8 +3413,8 @@ bool dataflow_layout_t(int nt, int device, int* grid, int* max_own, std::vector<
     for (int i = j + 2; i < nt; ++i) rest.push_back(make_int2(i, j));
   std::stable_sort(rest.begin(), rest.end(), [](const int2& a, const int2& b) { return a.y > b.y; });
   for (const int2& t : rest) {
-    int g = 0;
-    for (int h = 1; h < G; ++h)
+    int g = first_worker;
+    for (int h = first_worker + 1; h < G; ++h)
       if (load[h] < load[g]) g = h;
     lists[g].push_back(t);
     load[g] += t.y + 1;

@@ -132,7 +132,8 @@ class Report(C.Structure):
 class PlanStructure(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "problems", "keys", "points", "images", "key_pairs", "pair_items", "blocks",
-        "image_items", "camera_records", "max_reduced_size")] + [("reserved_", C.c_int64 * 4)]
+        "image_items", "camera_records", "max_reduced_size", "factor_schedule")] + \
+        [("reserved_", C.c_int64 * 3)]
 
     def as_dict(self):
         return {name: int(getattr(self, name)) for name, _ in self._fields_ if name != "reserved_"}

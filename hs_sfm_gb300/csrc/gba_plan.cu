@@ -2228,6 +2228,7 @@ int gba_plan_structure(gba_plan* p, gba_plan_structure_info* out) {
   out->image_items = P.d.n_img_items;
   out->camera_records = P.d.R;
   out->max_reduced_size = P.d.max_n;
+  out->factor_schedule = P.d.pcg ? -1 : P.d.df_grid > 0 ? 1 : 0;
   return GBA_OK;
 }
 

@@ -331,7 +331,10 @@ typedef struct gba_plan_structure_info {
   int64_t image_items;      /* work items of the image reduction             */
   int64_t camera_records;   /* per-point camera records (free cameras)       */
   int64_t max_reduced_size; /* largest reduced system (unknowns)             */
-  int64_t reserved_[4];
+  int64_t factor_schedule;  /* dense factorization: 0 one launch per tile
+                               column (batches), 1 one dataflow launch,
+                               -1 PCG                                      */
+  int64_t reserved_[3];
 } gba_plan_structure_info;
 GBA_API int gba_plan_structure(gba_plan* plan, gba_plan_structure_info* out);
 

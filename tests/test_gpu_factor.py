@@ -42,3 +42,4 @@ def test_dataflow_repeated_runs_and_graph(precision):
         assert p.report(0).status == abi.GBA_OK
     p.close()
     assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[1], xs[2])
+

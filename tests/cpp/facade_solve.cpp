@@ -12,7 +12,9 @@
 // mode 1: cameras free (x0 carries them), CameraSharedCeresOptimizor
 //         (threads 1, max_num_iterations = iters, ftol 1e-6, ptol 1e-8), as
 //         sfm_pipeline/bundle_adjustment_optimizor.hpp:200-224 calls it;
-// mode 2: as 1 with the cameras fixed (the Ceres optimizer refuses it).
+// mode 2: as 1 with the cameras fixed (the Ceres optimizer refuses it);
+// mode 3: points and cameras fixed (an images-only solve), the LM optimizer:
+//         x0 holds the images [6I] and double points[3P] follows it.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -48,8 +50,13 @@ int main(int argc, char** argv) {
   if (mode != 1 && vf.set_fix_cameras(cams) != 0) return 3;
   gba::VectorX<double> y(2 * K);
   if (std::fread(y.data(), sizeof(double), size_t(y.size()), f) != size_t(y.size())) return 2;
-  gba::VectorX<double> x0(3 * P + 6 * I + (mode == 1 ? int64_t(cams.size()) : 0));
+  gba::VectorX<double> x0((mode == 3 ? 0 : 3 * P) + 6 * I + (mode == 1 ? int64_t(cams.size()) : 0));
   if (std::fread(x0.data(), sizeof(double), size_t(x0.size()), f) != size_t(x0.size())) return 2;
+  if (mode == 3) {
+    std::vector<double> pts(size_t(3 * P));
+    if (std::fread(pts.data(), sizeof(double), pts.size(), f) != pts.size()) return 2;
+    if (vf.set_fix_points(pts) != 0) return 3;
+  }
   std::fclose(f);
   if (argc > 3 && std::strcmp(argv[3], "--bad-size") == 0) x0.resize(x0.size() - 1);
 
@@ -57,7 +64,7 @@ int main(int argc, char** argv) {
   cov.SetKeysUniformStdDev(1.0, size_t(K));
   gba::VectorX<double> x;
   int err = 0;
-  if (mode == 0) {
+  if (mode == 0 || mode == 3) {
     // (max_itr_num, tau, eps1, eps2) as the reference's relative-pair test
     gba::CameraSharedLevenbergMarquardtOptimizor<VF> optimizor(x0, size_t(iters), 1e-3, 0.0, 0.0);
     err = optimizor(vf, y, cov, x);

@@ -61,6 +61,8 @@ def write_problem(path, scene, iters, mode=0):
         np.ascontiguousarray(scene.cameras, np.float64).tofile(fh)
         np.ascontiguousarray(scene.near_y, np.float64).tofile(fh)
         np.ascontiguousarray(scene.x0, np.float64).tofile(fh)
+        if mode == 3:   # the fixed points follow x0
+            np.ascontiguousarray(scene.points, np.float64).tofile(fh)
 
 
 def write_triangulation(path, b):

@@ -152,3 +152,41 @@ def test_triangulation_facade_matches_oracle(tmp_path):
     # tests/test_gpu_triangulate.py): points within 1e-6
     assert np.max(np.abs(pts - ref)) < 1e-6
     assert np.array_equal(p0, pts[0])
+
+
+@pytest.mark.gpu
+def test_facade_images_only_solve_matches_oracle(tmp_path):
+    """The facade with points and cameras fixed (set_fix_points,
+    set_fix_cameras): x holds the images only, as the reference's
+    (camera_shared_vector_function.hpp:349-410), and the solve reaches the
+    oracle's final cost (SolveImagesCamerasOnly,
+    camera_shared_normal_equation_solver.hpp:540-706)."""
+    import oracle
+    exe = build_facade(str(tmp_path))
+    s = synthetic.ring_scene(num_images=8, num_points=300, obs_per_point=4, seed=14,
+                             fix_mask=abi.FIX_POINTS | abi.FIX_CAMERAS)
+    assert len(s.x0) == 6 * s.number_of_images
+    prob = tmp_path / "p.bin"
+    write_problem(prob, s, 10, mode=3)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    x = np.fromfile(tmp_path / "x.bin", dtype=np.float64)
+    assert len(x) == 6 * s.number_of_images
+    err, x_ref, rref = oracle.lm_solve(s, options=abi.make_options(max_iterations=10, eps1=0.0,
+                                                                    eps2=0.0))
+    assert err == 0
+    assert abs(oracle.cost(s, x, s.near_y) - rref.final_cost) <= 1e-9 * rref.final_cost
+
+
+def test_facade_images_only_rejects_bad_initial_x(tmp_path):
+    """With points and cameras fixed the facade expects x0 of 6 I values and
+    refuses one short of it, before any device work."""
+    exe = build_facade(str(tmp_path))
+    s = synthetic.ring_scene(num_images=5, num_points=60, obs_per_point=3, seed=4,
+                             fix_mask=abi.FIX_POINTS | abi.FIX_CAMERAS)
+    prob = tmp_path / "p.bin"
+    write_problem(prob, s, 5, mode=3)
+    r = subprocess.run([exe, str(prob), str(tmp_path / "x.bin"), "--bad-size"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1
+    assert r.stdout.startswith("err -1 status -2")

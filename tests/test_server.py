@@ -148,3 +148,34 @@ def test_server_free_cameras_and_priors_match_alone():
         x1, r1 = gba.solve(s, cfg.solve)
         assert rep.status == abi.GBA_OK
         assert rep.final_cost == r1.final_cost and np.array_equal(x, x1)
+
+
+def test_server_fixed_groups_and_pcg_free_cameras_match_alone():
+    """Requests with points or images fixed (every mask but all three) and a
+    PCG solve with free cameras through the server: each result has the
+    caller's x layout and equals the same request solved alone."""
+    from helpers import ALL_FIX_MASKS
+    from hs_sfm_gb300 import gba
+    scenes = [synthetic.full_model_scene(seed=40 + m, num_images=8, num_points=250, fix_mask=m,
+                                         obs_per_point=4) for m in ALL_FIX_MASKS]
+    cfg = gba.default_server_config(precision=abi.PRECISION_FP64)
+    cfg.solve.max_iterations = 6
+    cfg.solve.eps1 = 0.0
+    cfg.solve.eps2 = 0.0
+    with gba.Server(cfg) as srv:
+        tickets = [srv.submit(s) for s in scenes]
+        outs = [srv.wait(t) for t in tickets]
+    for s, (x, rep) in zip(scenes, outs):
+        assert len(x) == abi.x_size(s)
+        x1, r1 = gba.solve(s, cfg.solve)
+        assert rep.status == abi.GBA_OK
+        assert rep.final_cost == r1.final_cost and np.array_equal(x, x1)
+    free = synthetic.full_model_scene(seed=50, num_images=10, num_points=400, obs_per_point=4)
+    cfg.solve.linear_solver = abi.LINEAR_PCG
+    cfg.solve.pcg_max_iterations = 300
+    cfg.solve.pcg_relative_tolerance = 1e-12
+    with gba.Server(cfg) as srv:
+        x, rep = srv.wait(srv.submit(free))
+    x1, r1 = gba.solve(free, cfg.solve)
+    assert rep.status == abi.GBA_OK and rep.pcg_iterations > 0
+    assert rep.final_cost == r1.final_cost and np.array_equal(x, x1)

@@ -150,6 +150,7 @@ def test_server_free_cameras_and_priors_match_alone():
         assert rep.final_cost == r1.final_cost and np.array_equal(x, x1)
 
 
+@pytest.mark.gpu
 def test_server_fixed_groups_and_pcg_free_cameras_match_alone():
     """Requests with points or images fixed (every mask but all three) and a
     PCG solve with free cameras through the server: each result has the

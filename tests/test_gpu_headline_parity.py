@@ -93,3 +93,24 @@ def test_headline_windows_match_oracle(gba):
         assert rel <= COST_RTOL, (w.name, r.final_cost, rr.final_cost)
         assert abs(r.final_rmse - rr.final_rmse) <= RMSE_ATOL, w.name
     assert np.isfinite(worst)
+
+
+def test_walk_at_a_tenth_pcg_huber_matches_oracle(gba):
+    """The random-walk workload (block-Jacobi PCG, Huber 1 px, 1% outliers)
+    at a tenth of the benchmarked size -- 200 cameras, 100,000 points -- so
+    the oracle's dense solve of its 1,200 unknowns fits a test: the mixed
+    path with the bench's PCG settings (relative residual 1e-6, at most 100
+    iterations) by the acceptance rule, and an FP64 PCG solved to 1e-12
+    against the oracle's exact steps to 1e-8."""
+    s = synthetic.walk_scene(num_images=200, num_points=100_000, seed=2)
+    common = dict(max_iterations=WINDOW_ITERS, eps1=0.0, eps2=0.0, loss=abi.LOSS_HUBER, huber_delta=1.0)
+    err, _, rref = oracle.lm_solve(s, options=abi.make_options(**common))
+    assert err == 0
+    _, rep = gba.solve(s, abi.make_options(precision=abi.PRECISION_MIXED, linear_solver=abi.LINEAR_PCG,
+                                           pcg_relative_tolerance=1e-6, pcg_max_iterations=100, **common))
+    rel = abs(rep.final_cost - rref.final_cost) / rref.final_cost
+    assert rep.status == 0 and rel <= COST_RTOL, (rep.final_cost, rref.final_cost, rel)
+    assert abs(rep.final_rmse - rref.final_rmse) <= RMSE_ATOL
+    _, r64 = gba.solve(s, abi.make_options(precision=abi.PRECISION_FP64, linear_solver=abi.LINEAR_PCG,
+                                           pcg_relative_tolerance=1e-12, pcg_max_iterations=1000, **common))
+    assert abs(r64.final_cost - rref.final_cost) <= 1e-8 * rref.final_cost, (r64.final_cost, rref.final_cost)

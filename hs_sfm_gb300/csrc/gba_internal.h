@@ -246,6 +246,10 @@ struct DevPlan {
   // fold_count [2B]: per problem the arrival counters of the two kernels.
   int fold_ctrl;
   unsigned* fold_count;
+  // batched dense factorization of small systems (at most 8 tile rows,
+  // FP32): one launch of k_chol_small (factor and solve) per iteration
+  // instead of the per-column launches
+  int chol_small;
 };
 
 // A failed CUDA call on the host side of a plan (GBA_ERR_* status).
@@ -275,6 +279,9 @@ int launch_cholesky_solve(const DevPlan& d, cudaStream_t s);
 // Raises the backward solve's shared-memory limit for systems of up to
 // max_nt tile rows (before a graph capture); a GBA_* status.
 int prepare_cholesky_solve(int max_nt, int precision);
+// Readies k_chol_small for systems of up to max_nt tile rows (before a graph
+// capture); false when it does not apply (FP64, larger systems).
+bool prepare_chol_small(int max_nt, int precision);
 // Tile ownership of the dataflow factorization of an nt-tile system for this
 // device, or false when it does not fit in shared memory.
 bool dataflow_layout(int nt, bool mixed, int device, int* grid, int* max_own,

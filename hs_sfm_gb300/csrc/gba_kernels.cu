@@ -1561,10 +1561,10 @@ struct TileFetch {
 // rows a warp reads at once lie in distinct banks.  Two rows per thread halve
 // the shared-memory wavefronts per FMA against one row per thread.
 template <typename T>
-__device__ __forceinline__ void tile_xyt(const Tile<T>& X, const Tile<T>& Y, T s[8]) {
+__device__ __forceinline__ void tile_xyt_t(const Tile<T>& X, const Tile<T>& Y, T s[8], int t) {
   using V = Vec16<T>;
   constexpr int N = V::N;
-  const int r = threadIdx.x >> 3, c0 = threadIdx.x & 7;
+  const int r = t >> 3, c0 = t & 7;
 #pragma unroll
   for (int u = 0; u < 8; ++u) s[u] = T(0);
 #pragma unroll
@@ -1582,6 +1582,25 @@ __device__ __forceinline__ void tile_xyt(const Tile<T>& X, const Tile<T>& Y, T s
         s[4 + u] = fma(x1[e], y[e], s[4 + u]);
       }
     }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_xyt(const Tile<T>& X, const Tile<T>& Y, T s[8]) {
+  tile_xyt_t<T>(X, Y, s, threadIdx.x);
+}
+
+// A -= X Y^T (32x32x32) by the 128 threads t = 0..127 of a thread group, 8
+// outputs each (the same outputs and sums for every group).
+template <typename T>
+__device__ __forceinline__ void tile_sub_xyt_t(Tile<T>& A, const Tile<T>& X, const Tile<T>& Y, int t) {
+  T s[8];
+  tile_xyt_t<T>(X, Y, s, t);
+  const int r = t >> 3, c0 = t & 7;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    A[r][c0 + 8 * u] -= s[u];
+    A[r + 16][c0 + 8 * u] -= s[4 + u];
   }
 }
 
@@ -2493,6 +2512,115 @@ __global__ void __launch_bounds__(256) k_chol_solve_small(DevPlan d) {
   chol_solve_body<T, 1>(d, 0);
 }
 
+// Batched factorization and solve of small reduced systems (at most
+// kSolveSmallTiles tile rows, FP32): one CTA per problem keeps the tiles of
+// the lower triangle in shared memory and runs the schedule of the
+// per-column launches (k_chol_step) inside the CTA -- for each column c the
+// diagonal tile's factor and inverse, the panels L_ic = A_ic L_cc^-T, the
+// forward-solve updates b_i -= L_ic y_c, then the trailing updates A_ij -=
+// L_ic L_jc^T, two tiles at a time -- with the same per-element arithmetic,
+// so the result has the bits of k_chol_step and k_chol_dataflow; then the
+// backward solve of k_chol_solve_small.  One launch per LM iteration
+// instead of one per tile column plus the solve.
+template <typename T>
+__host__ __device__ constexpr size_t chol_small_smem(int max_nt) {
+  return size_t(max_nt) * (max_nt + 1) / 2 * sizeof(Tile<T>);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kCholThreads, 1) k_chol_small(DevPlan d) {
+  extern __shared__ __align__(16) unsigned char cs_raw[];
+  __shared__ __align__(16) Tile<T> Dinv;
+  __shared__ T bs[kSolveSmallTiles][kTile];   // b after the columns done so far
+  __shared__ T colbuf[4 * kTile + 8];
+  __shared__ int ok_s;
+  Tile<T>* A = reinterpret_cast<Tile<T>*>(cs_raw);   // tile (i, j), j <= i, at i (i + 1) / 2 + j
+  const int p = blockIdx.y;
+  const LMState& st = d.state[p];
+  if (!st.active || d.factor_flag[p]) return;
+  const ProbInfo pi = d.prob[p];
+  const int nt = pi.nt, n = pi.n;
+  if (nt > kSolveSmallTiles || nt > d.max_nt) return;   // (never: the planner's bound)
+  T* S = tptr_mut<T>(d.S) + pi.s_off;
+  T* b = tptr_mut<T>(d.b) + 6LL * pi.ext_begin;
+  T* Lg = tptr_mut<T>(d.Linv) + (long long)p * d.max_nt * kTile * kTile;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  auto at = [&](int i, int j) -> Tile<T>& { return A[i * (i + 1) / 2 + j]; };
+  for (int i = 0; i < nt; ++i)
+    for (int j = 0; j <= i; ++j) {
+      TileFetch<T> f;
+      if (i == j) f.diag(S, n, i); else f.rect(S, n, i, j);
+      f.store(at(i, j));
+    }
+  for (int e = tid; e < nt * kTile; e += blockDim.x) {
+    const int t = e / kTile, r = e % kTile;
+    bs[t][r] = r < tile_rows(n, t) ? b[kTile * t + r] : T(0);
+  }
+  __syncthreads();
+  for (int c = 0; c < nt; ++c) {
+    if (warp < 2) {
+      const bool ok = pair_potrf_inverse<T>(at(c, c), Dinv, colbuf, colbuf + 4 * kTile, warp, lane);
+      if (warp == 0 && lane == 0) ok_s = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (!ok_s) {
+      if (tid == 0) d.factor_flag[p] = 1;
+      return;
+    }
+    // L_cc^-1 out, y_c = L_cc^-1 b_c (b_c after the columns before c)
+    for (int e = tid; e < kTile * kTile; e += blockDim.x) Lg[(long long)c * kTile * kTile + e] = Dinv[e / kTile][e % kTile];
+    if (tid < kTile) {
+      T y = T(0);
+#pragma unroll 8
+      for (int q = 0; q < kTile; ++q) y += Dinv[tid][q] * bs[c][q];
+      colbuf[tid] = y;   // (the factor's buffers are free again)
+    }
+    // panels L_ic = A_ic L_cc^-T, two tiles at a time
+    for (int i = c + 1 + (tid >> 7); i < nt; i += 2) {
+      T sv[8];
+      tile_xyt_t<T>(at(i, c), Dinv, sv, tid & 127);
+      const int r = (tid & 127) >> 3, c0 = tid & 7;
+      // every read of this tile precedes its writes within the thread group
+      asm volatile("bar.sync %0, 128;\n" ::"r"(2 + (tid >> 7)) : "memory");
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) at(i, c)[r + 16 * h][c0 + 8 * u] = sv[4 * h + u];
+    }
+    __syncthreads();
+    if (tid < kTile) {
+      bs[c][tid] = colbuf[tid];
+      if (tid < tile_rows(n, c)) b[kTile * c + tid] = colbuf[tid];
+    }
+    for (int i = c + 1; i < nt; ++i) {   // the panels into S for the backward solve
+      const int mi = tile_rows(n, i);
+      for (int e = tid; e < kTile * kTile; e += blockDim.x) {
+        const int r = e / kTile, q = e % kTile;
+        if (r < mi) S[(long long)(kTile * i + r) * n + kTile * c + q] = at(i, c)[r][q];
+      }
+    }
+    __syncthreads();
+    // forward-solve updates of the rows below: b_i -= L_ic y_c
+    for (int e = tid; e < (nt - c - 1) * kTile; e += blockDim.x) {
+      const int i = c + 1 + e / kTile, r = e % kTile;
+      T t = bs[i][r];
+#pragma unroll 8
+      for (int q = 0; q < kTile; ++q) t -= at(i, c)[r][q] * bs[c][q];
+      bs[i][r] = t;
+    }
+    // trailing updates A_ij -= L_ic L_jc^T, c < j <= i, two tiles at a time
+    const int m = nt - c - 1, ntr = m * (m + 1) / 2;
+    for (int lin = tid >> 7; lin < ntr; lin += 2) {
+      int ti = 0;
+      while ((ti + 1) * (ti + 2) / 2 <= lin) ++ti;
+      const int i = c + 1 + ti, j = c + 1 + (lin - ti * (ti + 1) / 2);
+      tile_sub_xyt_t<T>(at(i, j), at(i, c), at(j, c), tid & 127);
+    }
+    __syncthreads();
+  }
+  chol_solve_body<T, 1>(d, 0);
+}
+
 // ---------------------------------------------------------------------------
 // Block-Jacobi PCG on the block-sparse reduced system (large scenes).  The
 // reduced system keeps one 6x6 block per co-visible image pair (first image
@@ -3182,6 +3310,11 @@ __global__ void k_jacobian_out(DevPlan d, double* jp_out, double* ji_out, double
 
 template <typename T>
 int run_cholesky_factor(const DevPlan& d, cudaStream_t s) {
+  if (d.chol_small) {   // factor and solve in one launch (small systems, FP32)
+    if constexpr (sizeof(T) == sizeof(float))
+      k_chol_small<T><<<dim3(1u, unsigned(d.B)), kCholThreads, chol_small_smem<T>(d.max_nt), s>>>(d);
+    return 1;
+  }
   if (d.df_grid > 0) {
     if (d.df_trace)
       cudaMemsetAsync(d.df_trace, 0, sizeof(unsigned long long) * 4 * kDfTraceCap * size_t(d.df_grid), s);
@@ -3209,6 +3342,7 @@ int run_cholesky_factor(const DevPlan& d, cudaStream_t s) {
 
 template <typename T>
 int run_cholesky_solve(const DevPlan& d, cudaStream_t s) {
+  if (d.chol_small) return 0;   // done by k_chol_small
   if (d.max_nt <= kSolveSmallTiles)
     k_chol_solve_small<T><<<dim3(1u, unsigned(d.B)), 256, 0, s>>>(d);
   else if (d.solve_drop_step >= 0 || d.solve_spin_limit != kSolveSpin)
@@ -3369,6 +3503,18 @@ int prepare_cholesky_solve(int max_nt, int precision) {
       return GBA_ERR_UNSUPPORTED;
     }
   return GBA_OK;
+}
+
+bool prepare_chol_small(int max_nt, int precision) {
+  if (precision != GBA_PRECISION_MIXED || max_nt < 1 || max_nt > kSolveSmallTiles) return false;
+  const size_t bytes = chol_small_smem<float>(max_nt);
+  if (bytes > 48 * 1024 &&
+      cudaFuncSetAttribute(&k_chol_small<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
 }
 
 int launch_cholesky_solve(const DevPlan& d, cudaStream_t s) {

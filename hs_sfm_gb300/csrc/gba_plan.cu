@@ -1537,6 +1537,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
       }
     }
   }
+  // batched small systems: one factor-and-solve launch (GBA_CHOL_COLUMNS=1
+  // keeps the per-column launches, for comparison)
+  D.chol_small = !pcg && D.df_grid == 0 && std::getenv("GBA_CHOL_COLUMNS") == nullptr &&
+                 prepare_chol_small(max_nt, opt.precision);
   D.blk_map = dev_blocks && !pcg ? dv_bid : arena.upload(blk_map);
   int dev_pair_bad = 0;
   int* d_pair_bad = nullptr;

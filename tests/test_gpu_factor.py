@@ -43,3 +43,25 @@ def test_dataflow_repeated_runs_and_graph(precision):
     p.close()
     assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[1], xs[2])
 
+
+
+@pytest.mark.parametrize("images", [3, 6, 11, 25, 42])
+def test_small_system_kernel_equals_per_column_launches(images, monkeypatch):
+    """Batches of small systems (at most eight tile rows, mixed precision)
+    factor and solve in one launch per iteration (k_chol_small) with the
+    per-element arithmetic of the per-column launches: the same bits as
+    those (GBA_CHOL_COLUMNS=1) and as the dataflow factorization alone."""
+    from hs_sfm_gb300 import gba
+    s = synthetic.ring_scene(num_images=images, num_points=60 * images, obs_per_point=4,
+                             seed=200 + images)
+    other = synthetic.ring_scene(num_images=7, num_points=300, seed=9)
+    opt = abi.make_options(max_iterations=6, precision=abi.PRECISION_MIXED, eps1=0.0, eps2=0.0)
+    x_df, r_df = gba.solve(s, opt)
+    xs, reps = gba.solve_batch([s, other], opt)
+    monkeypatch.setenv("GBA_CHOL_COLUMNS", "1")
+    xc, repc = gba.solve_batch([s, other], opt)
+    monkeypatch.delenv("GBA_CHOL_COLUMNS")
+    for a, b in zip(xs, xc):
+        assert np.array_equal(a, b)
+    assert np.array_equal(xs[0], x_df)
+    assert reps[0].final_cost == repc[0].final_cost == r_df.final_cost

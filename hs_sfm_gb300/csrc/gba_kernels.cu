@@ -2540,7 +2540,10 @@ __global__ void __launch_bounds__(kCholThreads, 1) k_chol_small(DevPlan d) {
   if (!st.active || d.factor_flag[p]) return;
   const ProbInfo pi = d.prob[p];
   const int nt = pi.nt, n = pi.n;
-  if (nt > kSolveSmallTiles || nt > d.max_nt) return;   // (never: the planner's bound)
+  if (nt > kSolveSmallTiles || nt > d.max_nt) {   // (never: the planner's bound) fail loudly
+    if (threadIdx.x == 0) d.factor_flag[p] = 1;
+    return;
+  }
   T* S = tptr_mut<T>(d.S) + pi.s_off;
   T* b = tptr_mut<T>(d.b) + 6LL * pi.ext_begin;
   T* Lg = tptr_mut<T>(d.Linv) + (long long)p * d.max_nt * kTile * kTile;

@@ -180,6 +180,8 @@ struct DevPlan {
   const int2* pairs;         // (key_a, key_b) per pair, grouped by block
   const int4* items;         // (block, pair_begin, pair_end, prob)
   const int2* blk_ij;        // (i, j) local image ids per block, i <= j
+  const int* blk_prob;       // [n_blocks] problem of each block (plans without free cameras), or null
+  long long s_elems;         // elements of S (all problems' dense systems)
   const int* blk_item_off;   // [num_blocks_total + 1] items of each block
   int n_items, n_blocks;
   const int* blk_map;        // per problem I*I dense map (j*I + i), j <= i -> block or -1

@@ -1460,6 +1460,39 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
   }
 }
 
+// The same dense system, block by block (plans without free cameras): S is
+// zeroed first (the entries of image pairs without a common point are 0),
+// then one thread per entry of every block writes base - sum over the
+// block's items (+ mu on the diagonal) exactly as k_assemble_S does, the 36
+// threads of a block reading its items' partials together; the threads of
+// row 0 of each diagonal block write the rhs.
+template <typename T>
+__global__ void __launch_bounds__(256) k_assemble_S_blocks(DevPlan d) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= 36LL * d.n_blocks) return;
+  const int blk = int(e / 36), el = int(e % 36);
+  const int p = __ldg(d.blk_prob + blk);
+  const LMState& st = d.state[p];
+  if (!st.active) return;
+  const ProbInfo pi = d.prob[p];
+  const int2 xy = __ldg(d.blk_ij + blk);   // column image x <= row image y
+  const int a = el % 6, bcol = el / 6;     // partial entry 6 * bcol + a = el
+  const int row = 6 * xy.y + a, col = 6 * xy.x + bcol;
+  const int2 items = make_int2(__ldg(d.blk_item_off + blk), __ldg(d.blk_item_off + blk + 1));
+  if (col <= row) {
+    const double v = sum_items4(d.item_partial + el, items.x, items.y);
+    const double base = reduced_base(d, pi, xy.y, a, xy.x, bcol);
+    double s = base - v;
+    if (row == col) s += st.mu;
+    tptr_mut<T>(d.S)[pi.s_off + (long long)row * pi.n + col] = T(s);
+  }
+  if (xy.x == xy.y && bcol == 0) {   // rhs b_y[a] = g_y[a] - sum over the diagonal block's items
+    const double rv = sum_items4(d.item_partial + 36 + a, items.x, items.y);
+    const double g = reduced_grad(d, pi, xy.y, a);
+    tptr_mut<T>(d.b)[6LL * (pi.ext_begin + xy.y) + a] = T(g - rv);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Tiled Cholesky of the reduced system S (lower, precision T), one launch per
 // column step.  Launch k (k = -1 .. nt-2) subtracts column k's rank-32
@@ -3475,6 +3508,13 @@ int launch_assemble_items(const DevPlan& d, cudaStream_t s) {
 
 int launch_assemble_S(const DevPlan& d, cudaStream_t s) {
   if (d.max_n <= 0) return 0;
+  if (d.blk_prob && d.n_blocks > 0) {
+    const size_t tsz = d.precision == GBA_PRECISION_MIXED ? sizeof(float) : sizeof(double);
+    if (cudaMemsetAsync(d.S, 0, size_t(d.s_elems) * tsz, s) != cudaSuccess) throw CudaError{GBA_ERR_CUDA};
+    const unsigned g = unsigned((36LL * d.n_blocks + 255) / 256);
+    GBA_DISPATCH(d, (k_assemble_S_blocks<T><<<g, 256, 0, s>>>(d)));
+    return 1;
+  }
   dim3 grid(unsigned((1LL * d.max_n * d.max_n + 255) / 256), unsigned(d.B));
   GBA_DISPATCH(d, (k_assemble_S<T><<<grid, 256, 0, s>>>(d)));
   return 1;

@@ -1570,6 +1570,14 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   }
   D.items = arena.upload(items);
   D.blk_ij = arena.upload(blk_ij);
+  D.s_elems = pcg ? 0 : s_off;
+  D.blk_prob = nullptr;
+  if (!pcg && !any_free && !blk_ij.empty()) {   // the dense system assembled block by block
+    std::vector<int> blk_prob(blk_ij.size());
+    for (int q = 0; q < nprob; ++q)
+      for (int t = prob[q].block_begin; t < prob[q].block_begin + prob[q].num_blocks; ++t) blk_prob[t] = q;
+    D.blk_prob = arena.upload(blk_prob);
+  }
   D.blk_item_off = arena.upload(blk_item_off);
   D.n_items = int(items.size());
   D.n_blocks = int(blk_ij.size());

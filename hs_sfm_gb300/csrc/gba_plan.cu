@@ -582,7 +582,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   bool any_weights = false;
   for (int q = 0; q < nprob; ++q) any_weights |= problems[q].key_covariance_inverse != nullptr;
   HostBuf<double> key_wl(any_weights ? 3 * K : 0);
-  std::vector<int> pt_key_off(P + 1, 0), pt_prob(P), img_key_off(I + 1, 0), img_prob(I), img_cam(I);
+  // per point (page-locked above 1 MB: uploaded without staging); every
+  // entry is written below (entry 0 with the problems' first entries)
+  HostBuf<int> pt_key_off(P + 1), pt_prob(P);
+  std::vector<int> img_key_off(I + 1, 0), img_prob(I), img_cam(I);
   std::vector<double> cam64(10 * std::max<int64_t>(C, 1), 0.0);
   std::vector<float> cam32(cam64.size(), 0.0f);
   std::vector<int2> pairs;
@@ -1040,10 +1043,16 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   if (nprob == 1) {
     build_one(0, host_threads());
   } else {
+    // the largest problems first, so no large one starts last
+    std::vector<int> by_size(nprob);
+    for (int q = 0; q < nprob; ++q) by_size[q] = q;
+    std::stable_sort(by_size.begin(), by_size.end(), [&](int a, int b) {
+      return problems[a].number_of_keys > problems[b].number_of_keys;
+    });
     const int nth = std::min(host_threads(), nprob);
     std::atomic<int> next{0};
     host_parallel(nth, nth, [&](int64_t, int64_t, int) {
-      for (int q = next++; q < nprob; q = next++) build_one(q, 1);
+      for (int u = next++; u < nprob; u = next++) build_one(by_size[u], 1);
     });
   }
   for (int q = 0; q < nprob; ++q)

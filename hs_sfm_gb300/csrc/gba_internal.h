@@ -170,6 +170,12 @@ struct DevPlan {
   void* pcg_p[2];            // T: [6I] search directions (by iteration parity)
   double* pcg_part;          // [kPcgSlots * n_ext_chunks]: p.q, r.z (x2), r.r (x2), b.b, x.r
   int* pcg_done;             // [B] 1 once a problem's inner solve has stopped
+  // the PCG iterations as a device-side loop (a CUDA-graph while node) when
+  // the plan runs from a graph: pcg_it counts its passes of two iterations;
+  // the body is captured on pcg_body_stream.  Null: one launch pair per iteration.
+  int* pcg_it;
+  unsigned long long* pcg_extra;   // passes run beyond each loop's first (all runs)
+  cudaStream_t pcg_body_stream;
   // PCG work chunks over reduced-system images (images, then free cameras'
   // parts; the image chunks when no camera is free) and their problems
   int n_ext_chunks;

@@ -2785,6 +2785,7 @@ __device__ __forceinline__ T pcg_precond_apply(const DevPlan& d, int img, T rv, 
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_init(DevPlan d) {
   __shared__ double red[33];
+  if (d.pcg_it && blockIdx.x == 0 && threadIdx.x == 0) *d.pcg_it = 0;   // the device-side loop's count
   const Chunk ch = d.ext_chunks[blockIdx.x];
   const LMState& st = d.state[ch.prob];
   if (!st.active || d.factor_flag[ch.prob]) return;
@@ -2819,8 +2820,11 @@ __global__ void __launch_bounds__(256) k_pcg_init(DevPlan d) {
 // Iteration it, part 1: beta from the last two r.z, p = z + beta p_old (own
 // images stored, neighbours' formed on the fly), q = S p, partial p.q.
 template <typename T>
-__global__ void __launch_bounds__(256) k_pcg_spmv(DevPlan d, int it) {
+__global__ void __launch_bounds__(256) k_pcg_spmv(DevPlan d, int it, int loop) {
   __shared__ double red[33];
+  // in the device-side loop `it` is the half (0, 1) of the loop body's pass
+  if (loop) it += 2 * *reinterpret_cast<volatile int*>(d.pcg_it);
+  if (it >= d.pcg_max_iterations) return;
   const Chunk ch = d.ext_chunks[blockIdx.x];
   const int p = ch.prob;
   const LMState& st = d.state[p];
@@ -2881,8 +2885,10 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(DevPlan d, int it) {
 // Iteration it, part 2: alpha = r.z / p.q, x += alpha p, r -= alpha q,
 // z = Minv r, partials of the next r.z and r.r.
 template <typename T>
-__global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
+__global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it, int loop) {
   __shared__ double red[33];
+  if (loop) it += 2 * *reinterpret_cast<volatile int*>(d.pcg_it);
+  if (it >= d.pcg_max_iterations) return;
   const Chunk ch = d.ext_chunks[blockIdx.x];
   const int p = ch.prob;
   LMState& st = d.state[p];
@@ -2946,6 +2952,29 @@ __global__ void __launch_bounds__(256) k_pcg_update(DevPlan d, int it) {
     part[3 + (par ^ 1)] = rrn;
     part[6] = xr;
     if (lead) st.pcg_iters += 1;
+  }
+}
+
+// The device-side PCG loop (a CUDA-graph while node): after each pass of
+// two iterations one warp counts the pass and ends the loop once every
+// problem's inner solve has stopped (converged, broken down, not solving)
+// or the iterations are used up.
+__global__ void __launch_bounds__(32) k_pcg_loop_ctrl(DevPlan d, cudaGraphConditionalHandle h) {
+  const int m = *reinterpret_cast<volatile int*>(d.pcg_it) + 1;
+  bool more = 2 * m < d.pcg_max_iterations;
+  if (more) {
+    bool open = false;
+    for (int p = threadIdx.x; p < d.B && !open; p += 32) {
+      const LMState& st = d.state[p];
+      open = st.active && !d.factor_flag[p] && !d.pcg_done[p];
+    }
+    more = __any_sync(0xffffffffu, open);
+  }
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    *d.pcg_it = m;
+    if (more) ++*d.pcg_extra;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
   }
 }
 
@@ -3661,9 +3690,43 @@ int launch_pcg_setup(const DevPlan& d, cudaStream_t s) {
 
 int launch_pcg_iterations(const DevPlan& d, cudaStream_t s) {
   if (d.I_ext <= 0) return 0;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (d.pcg_it && d.pcg_body_stream && cudaStreamIsCapturing(s, &cs) == cudaSuccess &&
+      cs == cudaStreamCaptureStatusActive) {
+    // in a CUDA graph: a while node whose body runs two iterations and the
+    // loop control, so the iterations after convergence are not launched
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaGraphConditionalHandle h = 0;
+    cudaGraphNodeParams cp = {};
+    cudaGraphNode_t node = nullptr;
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+        cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+      throw CudaError{GBA_ERR_CUDA};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp) != cudaSuccess) throw CudaError{GBA_ERR_CUDA};
+    cudaStream_t bs = d.pcg_body_stream;
+    if (cudaStreamBeginCaptureToGraph(bs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      throw CudaError{GBA_ERR_CUDA};
+    for (int u = 0; u < 2; ++u) {
+      GBA_DISPATCH(d, (k_pcg_spmv<T><<<d.n_ext_chunks, 256, 0, bs>>>(d, u, 1)));
+      GBA_DISPATCH(d, (k_pcg_update<T><<<d.n_ext_chunks, 256, 0, bs>>>(d, u, 1)));
+    }
+    k_pcg_loop_ctrl<<<1, 32, 0, bs>>>(d, h);
+    cudaGraph_t body = nullptr;
+    if (cudaStreamEndCapture(bs, &body) != cudaSuccess ||
+        cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+      throw CudaError{GBA_ERR_CUDA};
+    return 5;   // (one pass of the body; it runs as many passes as the solve needs)
+  }
   for (int it = 0; it < d.pcg_max_iterations; ++it) {
-    GBA_DISPATCH(d, (k_pcg_spmv<T><<<d.n_ext_chunks, 256, 0, s>>>(d, it)));
-    GBA_DISPATCH(d, (k_pcg_update<T><<<d.n_ext_chunks, 256, 0, s>>>(d, it)));
+    GBA_DISPATCH(d, (k_pcg_spmv<T><<<d.n_ext_chunks, 256, 0, s>>>(d, it, 0)));
+    GBA_DISPATCH(d, (k_pcg_update<T><<<d.n_ext_chunks, 256, 0, s>>>(d, it, 0)));
   }
   return 2 * d.pcg_max_iterations;
 }

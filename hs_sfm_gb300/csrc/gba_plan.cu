@@ -380,8 +380,13 @@ struct Plan {
   // run state
   cudaGraphExec_t graph_exec = nullptr;
   cudaGraphExec_t iter_exec = nullptr;   // one LM iteration (one-shot solves)
-  long long iter_launches = 0;
+  long long iter_launches = 0, graph_launches = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the device-side PCG loop: the stream its body is captured on and the
+  // passes it ran beyond the first of each loop (read back after each run)
+  cudaStream_t pcg_stream = nullptr;
+  unsigned long long* h_pcg_extra = nullptr;
+  unsigned long long pcg_extra_seen = 0;
   bool ran = false;
   long long launches_last_run = 0;
   double setup_ms = 0;
@@ -426,6 +431,8 @@ struct Plan {
     if (ev1) cudaEventDestroy(ev1);
     arena.release();
     if (stream) cudaStreamDestroy(stream);
+    if (pcg_stream) cudaStreamDestroy(pcg_stream);
+    if (h_pcg_extra) cudaFreeHost(h_pcg_extra);
   }
 
   int build(const gba_problem* problems, const double* const* near_ys, int nprob,
@@ -1503,6 +1510,16 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     D.pcg_p[1] = arena.alloc<char>(v6);
     D.pcg_part = arena.alloc<double>(kPcgSlots * std::max<size_t>(ext_chunks.size(), 1));
     D.pcg_done = arena.alloc<int>(nprob);
+    // GBA_PCG_UNROLLED=1 keeps one launch pair per iteration in graphs too
+    if (std::getenv("GBA_PCG_UNROLLED") == nullptr) {
+      D.pcg_it = arena.alloc<int>(4);
+      D.pcg_extra = reinterpret_cast<unsigned long long*>(D.pcg_it + 2);
+      GBA_CUDA(cudaMemsetAsync(D.pcg_it, 0, 4 * sizeof(int), stream));
+      GBA_CUDA(cudaStreamCreateWithFlags(&pcg_stream, cudaStreamNonBlocking));
+      GBA_CUDA(cudaHostAlloc(&h_pcg_extra, sizeof(unsigned long long), cudaHostAllocDefault));
+      *h_pcg_extra = 0;
+      D.pcg_body_stream = pcg_stream;
+    }
   }
   if (!pcg)
     if (int e = prepare_cholesky_solve(max_nt, opt.precision)) return e;
@@ -1786,8 +1803,10 @@ int Plan::run() {
       GBA_CUDA(cudaStreamEndCapture(stream, &g));
       GBA_CUDA(cudaGraphInstantiate(&graph_exec, g, 0));
       cudaGraphDestroy(g);
+      graph_launches = launches_last_run;
     }
     GBA_CUDA(cudaGraphLaunch(graph_exec, stream));
+    launches_last_run = graph_launches;
   } else if (!profile && opt.max_iterations > 0) {
     // one-shot: the prologue launched directly, then one LM iteration
     // captured once (its launches do not depend on the iteration) and
@@ -1813,6 +1832,11 @@ int Plan::run() {
   } else {
     enqueue(profile);
   }
+  if (h_pcg_extra) {
+    GBA_CUDA(cudaMemcpyAsync(h_pcg_extra, d.pcg_extra, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += sizeof(unsigned long long);
+  }
   GBA_CUDA(cudaEventRecord(ev1, stream));
   g_launches += launches_last_run;
   ran = true;
@@ -1822,6 +1846,14 @@ int Plan::run() {
 int Plan::sync() {
   GBA_CUDA(cudaStreamSynchronize(stream));
   GBA_CUDA(cudaGetLastError());
+  if (h_pcg_extra) {
+    // each pass of the device-side PCG loop beyond a loop's first is five
+    // launches the launch sequence did not count
+    const long long extra = 5LL * (long long)(*h_pcg_extra - pcg_extra_seen);
+    pcg_extra_seen = *h_pcg_extra;
+    launches_last_run += extra;
+    g_launches += extra;
+  }
   if (d.df_trace && !trace_path.empty()) write_trace();
   if (opt.profile) {
     std::fill(stage_ms, stage_ms + GBA_NUM_STAGES, 0.0);

@@ -125,3 +125,28 @@ def test_pcg_beyond_the_dense_limit(gba):
     x, rep = gba.solve(s, pcg_opts(abi.PRECISION_MIXED, iters=4))
     assert rep.status == abi.GBA_OK
     assert rep.final_cost < rep.initial_cost
+
+
+@pytest.mark.parametrize("pcg_iters,tol", [(200, 1e-6), (7, 1e-14)])
+def test_pcg_device_loop_equals_unrolled_launches(gba, monkeypatch, pcg_iters, tol):
+    """In a CUDA graph the PCG iterations run as a while node (two iterations
+    and a control kernel per pass, ending once every problem's inner solve
+    has stopped): the same bits as one launch pair per iteration
+    (GBA_PCG_UNROLLED=1), with fewer launches once the solves converge.  An
+    odd iteration cap ends the loop mid-pass."""
+    scenes = [small_walk(num_images=40, num_points=2000, seed=s) for s in (4, 5)]
+    opt = pcg_opts(abi.PRECISION_MIXED, iters=5, tol=tol, pcg_iters=pcg_iters)
+    k0 = gba.kernel_launch_count()
+    xs, reps = gba.solve_batch(scenes, opt)
+    k_loop = gba.kernel_launch_count() - k0
+    monkeypatch.setenv("GBA_PCG_UNROLLED", "1")
+    k0 = gba.kernel_launch_count()
+    xu, repu = gba.solve_batch(scenes, opt)
+    k_unrolled = gba.kernel_launch_count() - k0
+    monkeypatch.delenv("GBA_PCG_UNROLLED")
+    for a, b, ra, rb in zip(xs, xu, reps, repu):
+        np.testing.assert_array_equal(a, b)
+        assert ra.final_cost == rb.final_cost
+        assert ra.pcg_iterations == rb.pcg_iterations
+    if tol > 1e-10:
+        assert k_loop < k_unrolled

@@ -373,7 +373,7 @@ def run_gba(args, ws, rank, local):
     tuning = None if args.no_autotune else gba.autotune(
         [scene], abi.make_options(max_iterations=ITERS_PER_SOLVE, precision=precision, device=local))
     item_sizes = {} if tuning is None else {k: tuning[k] for k in ("pair_item", "image_item",
-                                                                   "key_item")}
+                                                                   "key_item", "z_layout")}
     opt = abi.make_options(max_iterations=ITERS_PER_SOLVE, eps1=0.0, eps2=0.0,
                            precision=precision, profile=0, use_cuda_graph=1, device=local, **item_sizes)
     plan = gba.Plan([scene], opt)
@@ -606,7 +606,7 @@ def run_windows(args, ws, rank, local, keep_parity=False):
     tuning = None if getattr(args, "no_autotune", False) else gba.autotune(
         wins, abi.make_options(max_iterations=WINDOW_ITERS, precision=abi.PRECISION_MIXED, device=local))
     item_sizes = {} if tuning is None else {k: tuning[k] for k in ("pair_item", "image_item",
-                                                                   "key_item")}
+                                                                   "key_item", "z_layout")}
     opt = abi.make_options(max_iterations=WINDOW_ITERS, eps1=0.0, eps2=0.0,
                            precision=abi.PRECISION_MIXED, profile=1, device=local, **item_sizes)
     t0 = time.perf_counter()
@@ -726,7 +726,7 @@ def run_walk(args, ws, rank, local):
         [scene], abi.make_options(precision=abi.PRECISION_MIXED, **common))
     if tuning is not None:
         common.update(pair_item=tuning["pair_item"], image_item=tuning["image_item"],
-                      key_item=tuning["key_item"])
+                      key_item=tuning["key_item"], z_layout=tuning["z_layout"])
     plan = gba.Plan(scene, abi.make_options(precision=abi.PRECISION_MIXED, profile=1, **common))
     dev_bytes = plan.device_bytes()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")

@@ -42,6 +42,7 @@ LOSS_TRIVIAL = 0
 LOSS_HUBER = 1
 LINEAR_DENSE_CHOLESKY = 0
 LINEAR_PCG = 1
+Z_AUTO, Z_RECORDS, Z_PLANES = 0, 1, 2
 
 NUM_STAGES = 12
 STOP_MAX_ITERATIONS = 0
@@ -99,14 +100,15 @@ class Options(C.Structure):
         ("use_cuda_graph", C.c_int32), ("profile", C.c_int32), ("device", C.c_int32),
         ("shared_device", C.c_int32), ("function_tolerance", C.c_double),
         ("pair_item", C.c_int32), ("image_item", C.c_int32), ("key_item", C.c_int32),
-        ("reserved_", C.c_int32 * 1),
+        ("z_layout", C.c_int32),
     ]
 
 
 class Tuning(C.Structure):
     _fields_ = [("pair_item", C.c_int32), ("image_item", C.c_int32),
                 ("ms_per_iteration", C.c_double), ("default_ms_per_iteration", C.c_double),
-                ("candidates", C.c_int32), ("key_item", C.c_int32), ("reserved_", C.c_int32 * 2)]
+                ("candidates", C.c_int32), ("key_item", C.c_int32), ("z_layout", C.c_int32),
+                ("reserved_", C.c_int32 * 1)]
 
 
 class Report(C.Structure):
@@ -191,7 +193,7 @@ def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PR
                  loss=LOSS_TRIVIAL, huber_delta=1.0, linear_solver=LINEAR_DENSE_CHOLESKY,
                  pcg_max_iterations=100, pcg_relative_tolerance=1e-6, use_cuda_graph=1,
                  profile=0, device=0, shared_device=0, function_tolerance=0.0,
-                 pair_item=0, image_item=0, key_item=0) -> Options:
+                 pair_item=0, image_item=0, key_item=0, z_layout=0) -> Options:
     """Defaults of the reference's relative-pair test
     (test_camera_shared_relative_pair.cpp:976-979)."""
     o = Options()
@@ -204,6 +206,7 @@ def make_options(max_iterations=50, tau=1e-3, eps1=1e-8, eps2=1e-8, precision=PR
     o.shared_device = shared_device
     o.function_tolerance = function_tolerance
     o.pair_item, o.image_item, o.key_item = pair_item, image_item, key_item
+    o.z_layout = z_layout
     return o
 
 

@@ -29,6 +29,8 @@ constexpr int kImageItem = 512;    // keys per image-reduce work item (warp each
 constexpr int kPairItem = 1024;    // pairs per Schur-assembly work item
 constexpr int kJRStride = 20;      // per key: Jp(6) Ji(12) rw(2)
 constexpr int kZStride = 20;       // per key: Z(18) + pad
+// Z planes from this mean share of an image's keys in a block's key pairs
+constexpr double kZPlanesDensity = 0.2;
 constexpr int kItemStride = 44;    // per work item: 36 block + 6 rhs + pad
 
 // Per-problem LM state (device).  Written only by the control kernels.
@@ -129,7 +131,9 @@ struct DevPlan {
   // per key
   void* RW[2];               // [4K] T: rw0 rw1 sqrt(w) pad  (whitened, weighted residual)
   void* JR;                  // [20K] T
-  void* Z;                   // [20K] T
+  void* Z;                   // [20(K+R)] T records, or 9 planes of z_n T pairs (z_planes)
+  int z_planes;              // 1: Z as planes, slots image by image (img_keys order)
+  long long z_n;             // plane stride in slots (>= K + R)
   // per point
   void* PV;                  // [12P] T: V(6) g(3) pad
   void* PS;                  // [12P] T: Cinv(6) h(3) pad
@@ -275,6 +279,9 @@ int launch_linearize(const DevPlan& d, cudaStream_t s);
 int launch_image_reduce(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s);
 int launch_point_schur(const DevPlan& d, cudaStream_t s);
+// plan build with Z planes: key_slot [K] = the inverse of img_keys, and the
+// assembly's pairs rewritten as slots
+int launch_z_slots(const DevPlan& d, int* key_slot, cudaStream_t s);
 int launch_assemble(const DevPlan& d, cudaStream_t s);
 int launch_assemble_items(const DevPlan& d, cudaStream_t s);
 int launch_assemble_S(const DevPlan& d, cudaStream_t s);

@@ -103,6 +103,39 @@ __device__ __forceinline__ void store_vec(double* p, const double* in) {
     reinterpret_cast<double2*>(p)[i] = make_double2(in[2 * i], in[2 * i + 1]);
 }
 
+// Z records (18 T each) at slot s: either records of kZStride T in slot
+// order, or (DevPlan::z_planes) nine planes of T pairs, plane v holding the
+// pair (z[2v], z[2v+1]) of every slot (plane stride z_n slots).
+template <typename T> struct Pair2;
+template <> struct Pair2<float> { using type = float2; };
+template <> struct Pair2<double> { using type = double2; };
+
+template <typename T>
+__device__ __forceinline__ void load_z(const DevPlan& d, const T* __restrict__ Z, long long s, T* z) {
+  if (d.z_planes) {
+    const auto* zp = reinterpret_cast<const typename Pair2<T>::type*>(Z) + s;
+#pragma unroll
+    for (int v = 0; v < 9; ++v) {
+      const auto t = __ldg(zp + v * d.z_n);
+      z[2 * v] = t.x;
+      z[2 * v + 1] = t.y;
+    }
+  } else {
+    load_vec<kZStride>(Z + (long long)kZStride * s, z);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void store_z(const DevPlan& d, T* Z, long long s, const T* z) {
+  if (d.z_planes) {
+    auto* zp = reinterpret_cast<typename Pair2<T>::type*>(Z) + s;
+#pragma unroll
+    for (int v = 0; v < 9; ++v) zp[v * d.z_n] = {z[2 * v], z[2 * v + 1]};
+  } else {
+    store_vec<kZStride>(Z + (long long)kZStride * s, z);
+  }
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -1186,9 +1219,11 @@ __global__ void __launch_bounds__(kPointChunk) k_point_factor(DevPlan d) {
   store_vec<12>(tptr_mut<T>(d.PS) + 12LL * pt, ps);
 }
 
-// Z_a = C_p^-1 J_p^T J_i per key (coalesced records).  DevPlan::key_z_split
-// CTAs share each key chunk (one key per thread), so the grid fills the GPU
-// in even waves.
+// Z_a = C_p^-1 J_p^T J_i per key, one slot per thread: slot s holds key s
+// (records) or key img_keys[s], the keys image by image (planes), so the
+// writes are coalesced either way.  DevPlan::key_z_split CTAs share each
+// key chunk (a problem's slots are its keys' range), so the grid fills the
+// GPU in even waves.
 template <typename T>
 __global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
   const int split = d.key_z_split;
@@ -1199,7 +1234,8 @@ __global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
   const T* __restrict__ PS = tptr<T>(d.PS);
   T* __restrict__ Z = tptr_mut<T>(d.Z);
   const int sub = blockIdx.x % split;
-  for (int k = ch.begin + sub * 256 + threadIdx.x; k < ch.end; k += split * 256) {
+  for (int sl = ch.begin + sub * 256 + threadIdx.x; sl < ch.end; sl += split * 256) {
+    const int k = d.z_planes ? __ldg(d.img_keys + sl) : sl;
     T rec[kJRStride], ps[8];
     load_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
     load_vec<8>(PS + 12LL * __ldg(d.key_pt + k), ps);
@@ -1218,7 +1254,7 @@ __global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
     }
     z[18] = T(0);
     z[19] = T(0);
-    store_vec<kZStride>(Z + (long long)kZStride * k, z);
+    store_z(d, Z, sl, z);
   }
 }
 
@@ -1288,8 +1324,35 @@ __global__ void __launch_bounds__(kPointChunk) k_camrec_z(DevPlan d) {
       }
       z[18] = T(0);
       z[19] = T(0);
-      store_vec<kZStride>(tptr_mut<T>(d.Z) + (long long)kZStride * r, z);
+      store_z(d, tptr_mut<T>(d.Z), r, z);
     }
+  }
+}
+
+// Plan build, Z planes: the slot of every key (the inverse of img_keys) ...
+__global__ void __launch_bounds__(256) k_key_slots(const int* __restrict__ img_keys, int K, int* __restrict__ key_slot) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < K) key_slot[img_keys[s]] = s;
+}
+
+// ... and the key pairs of the assembly's work items as slots (a camera
+// record's index, >= K, is its slot; a diagonal block's second entry is
+// the point and stays).
+__global__ void __launch_bounds__(128) k_pairs_to_slots(const int4* __restrict__ items, int n_items,
+                                                        const int2* __restrict__ blk_ij,
+                                                        const int* __restrict__ key_slot, int K,
+                                                        int2* __restrict__ pairs) {
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= n_items) return;
+  const int4 it = items[wid];
+  const int2 ij = blk_ij[it.x];
+  const bool diag = ij.x == ij.y;
+  for (int q = it.y + lane; q < it.z; q += 32) {
+    int2 pr = pairs[q];
+    pr.x = pr.x < K ? key_slot[pr.x] : pr.x;
+    if (!diag) pr.y = pr.y < K ? key_slot[pr.y] : pr.y;
+    pairs[q] = pr;
   }
 }
 
@@ -1323,7 +1386,7 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
     const int qn = q + 32;
     const int2 prn = qn < it.z ? __ldg(d.pairs + qn) : pr;
     T za[kZStride], zb[kZStride];
-    load_vec<kZStride>(Z + (long long)kZStride * pr.x, za);
+    load_z(d, Z, pr.x, za);
     if (diag) {
 #pragma unroll
       for (int e = 0; e < kZStride; ++e) zb[e] = za[e];
@@ -1332,7 +1395,7 @@ __global__ void __launch_bounds__(128) k_assemble_items(DevPlan d, int n_items) 
 #pragma unroll
       for (int r = 0; r < 6; ++r) racc[r] += za[r] * ps[6] + za[6 + r] * ps[7] + za[12 + r] * ps[8];
     } else {
-      load_vec<kZStride>(Z + (long long)kZStride * pr.y, zb);
+      load_z(d, Z, pr.y, zb);
     }
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
@@ -3002,32 +3065,49 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
     if (pt < ch.end) {
       T ps[12];
       load_vec<12>(tptr<T>(d.PS) + 12LL * pt, ps);
-      T t0 = ps[6], t1 = ps[7], t2 = ps[8];
-      const T* __restrict__ Z = tptr<T>(d.Z);
+      const T i00 = ps[0], m10 = ps[1], i11 = ps[2], m20 = ps[3], m21 = ps[4], i22 = ps[5];
+      const T* __restrict__ JR = tptr<T>(d.JR);
       const int kb = __ldg(d.pt_key_off + pt), ke = __ldg(d.pt_key_off + pt + 1);
-      // every Z record of the point: its keys, then (free cameras) its
-      // camera records, each against its reduced-system image's delta
-      const int rb = d.pt_rec_off ? __ldg(d.pt_rec_off + pt) : 0;
-      const int re = d.pt_rec_off ? ke + (__ldg(d.pt_rec_off + pt + 1) - rb) : ke;
-      for (int k = kb; k < re; ++k) {
-        const int r = k < ke ? k : rb + (k - ke);
-        T z[kZStride];
-        load_vec<kZStride>(Z + (long long)kZStride * r, z);
-        const int ext = k < ke ? (d.img_ext ? __ldg(d.img_ext + __ldg(d.key_img + k)) : __ldg(d.key_img + k))
-                               : __ldg(&d.rec_info[r - d.K].y);
+      // w = sum over the point's keys of J_p^T (J_i delta_i) from the
+      // Jacobian records (the point's keys are consecutive), then
+      // t = C^-1 (g - w) with C^-1 g = h
+      T w0 = T(0), w1 = T(0), w2 = T(0);
+      for (int k = kb; k < ke; ++k) {
+        T rec[kJRStride];
+        load_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
+        const int ext = d.img_ext ? __ldg(d.img_ext + __ldg(d.key_img + k)) : __ldg(d.key_img + k);
         const T* di = tptr<T>(d.b) + 6LL * ext;
-        T dl[6];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) dl[c] = di[c];
+        T u0 = T(0), u1 = T(0);
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-          t0 -= z[c] * dl[c];
-          t1 -= z[6 + c] * dl[c];
-          t2 -= z[12 + c] * dl[c];
+          const T dl = di[c];
+          u0 += rec[6 + c] * dl;
+          u1 += rec[12 + c] * dl;
+        }
+        w0 += rec[0] * u0 + rec[3] * u1;
+        w1 += rec[1] * u0 + rec[4] * u1;
+        w2 += rec[2] * u0 + rec[5] * u1;
+      }
+      T t0 = ps[6] - i00 * w0, t1 = ps[7] - (m10 * w0 + i11 * w1), t2 = ps[8] - (m20 * w0 + m21 * w1 + i22 * w2);
+      // free cameras: the point's camera records (Z = C^-1 W) against their
+      // reduced-system images' deltas
+      if (d.pt_rec_off) {
+        const T* __restrict__ Z = tptr<T>(d.Z);
+        const int rb = __ldg(d.pt_rec_off + pt), re = __ldg(d.pt_rec_off + pt + 1);
+        for (int r = rb; r < re; ++r) {
+          T z[kZStride];
+          load_z(d, Z, r, z);
+          const T* di = tptr<T>(d.b) + 6LL * __ldg(&d.rec_info[r - d.K].y);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            const T dl = di[c];
+            t0 -= z[c] * dl;
+            t1 -= z[6 + c] * dl;
+            t2 -= z[12 + c] * dl;
+          }
         }
       }
       // delta = C^-T t, C^-1 rows [i00 0 0; m10 i11 0; m20 m21 i22]
-      const T i00 = ps[0], m10 = ps[1], i11 = ps[2], m20 = ps[3], m21 = ps[4], i22 = ps[5];
       const double dp[3] = {double(i00 * t0 + m10 * t1 + m20 * t2), double(i11 * t1 + m21 * t2),
                             double(i22 * t2)};
       T pv[12];
@@ -3510,6 +3590,20 @@ int launch_image_reduce(const DevPlan& d, cudaStream_t s) {
 int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s) {
   k_ctrl_after_linearize<<<(d.B + 127) / 128, 128, 0, s>>>(d);
   return 1;
+}
+
+int launch_z_slots(const DevPlan& d, int* key_slot, cudaStream_t s) {
+  int n = 0;
+  if (d.K > 0) {
+    k_key_slots<<<(d.K + 255) / 256, 256, 0, s>>>(d.img_keys, d.K, key_slot);
+    ++n;
+  }
+  if (d.n_items > 0) {
+    k_pairs_to_slots<<<(d.n_items + 3) / 4, 128, 0, s>>>(d.items, d.n_items, d.blk_ij, key_slot, d.K,
+                                                        const_cast<int2*>(d.pairs));
+    ++n;
+  }
+  return n;
 }
 
 int launch_point_schur(const DevPlan& d, cudaStream_t s) {

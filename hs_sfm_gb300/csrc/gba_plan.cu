@@ -399,6 +399,7 @@ struct Plan {
   double* d_rmse_scratch = nullptr;
   std::string trace_path;
   long long n_pairs = 0;           // key pairs of the Schur assembly (all problems)
+  double z_density = 0.0;          // mean share of an image's keys in a block's pairs
 
   // Task timeline of the last dataflow factorization as CSV:
   // cta,mode,i,j,k0,count,wait_ns,select_ns,end_ns (times from the first wait).
@@ -1398,7 +1399,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   D.x0_pt = arena.alloc<double>(3 * P);
   D.x0_img = arena.alloc<double>(6 * I);
   D.JR = arena.alloc<char>(size_t(kJRStride) * K * tsz);
-  D.Z = arena.alloc<char>(size_t(kZStride) * (K + R) * tsz);
+  D.z_n = (K + R + 31) / 32 * 32;
+  D.Z = arena.alloc<char>(std::max<size_t>(size_t(kZStride) * (K + R), 18 * size_t(D.z_n)) * tsz);
   D.PV = arena.alloc<char>(12 * P * tsz);
   D.PS = arena.alloc<char>(12 * P * tsz);
   D.U = arena.alloc<double>(36 * I);
@@ -1606,6 +1608,34 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   }
   D.blk_item_off = arena.upload(blk_item_off);
   D.n_items = int(items.size());
+  // Z layout: planes in image order when the assembly's key pairs walk
+  // each image's keys densely (a block's pairs are a large share of both
+  // images' keys: the loads of a warp's 32 pairs then fall in few lines),
+  // else records in key order.  Only where the records lie changes.
+  {
+    double num = 0.0, den = 0.0;
+    for (size_t b = 0; b + 1 < blk_item_off.size(); ++b) {
+      const int t0 = blk_item_off[b], t1 = blk_item_off[b + 1];
+      if (t1 <= t0) continue;
+      const int2 ij = blk_ij[b];
+      const ProbInfo& pi = prob[items[t0].w];
+      if (ij.x == ij.y || ij.x >= pi.num_images || ij.y >= pi.num_images) continue;
+      const double nb = double(items[t1 - 1].z - items[t0].y);
+      const int gi = pi.image_begin + ij.x, gj = pi.image_begin + ij.y;
+      const double ki = std::max(1, img_key_off[gi + 1] - img_key_off[gi]);
+      const double kj = std::max(1, img_key_off[gj + 1] - img_key_off[gj]);
+      num += nb * nb * 0.5 * (1.0 / ki + 1.0 / kj);
+      den += nb;
+    }
+    z_density = den > 0 ? num / den : 0.0;
+    int layout = opt.z_layout;
+    if (const char* zl = std::getenv("GBA_Z_LAYOUT")) layout = std::atoi(zl);   // for comparisons
+    D.z_planes = layout == GBA_Z_PLANES || (layout != GBA_Z_RECORDS && z_density >= kZPlanesDensity);
+    if (D.z_planes) {   // the pairs as slots of the planes
+      int* key_slot = arena.alloc<int>(std::max<int64_t>(K, 1));
+      count_launches(launch_z_slots(D, key_slot, stream));
+    }
+  }
   D.n_blocks = int(blk_ij.size());
   D.blk_map_off = arena.upload(blk_map_off);
   D.item_partial = arena.alloc<double>(size_t(kItemStride) * std::max<size_t>(items.size(), 1));
@@ -2031,6 +2061,7 @@ int gba_plan_create(const gba_problem* problems, const double* const* near_ys, i
   if (options->pair_item < 0 || options->image_item < 0 || options->pair_item > (1 << 24) ||
       options->image_item > (1 << 24) || options->key_item < 0 || options->key_item > (1 << 24))
     return GBA_ERR_INVALID;
+  if (options->z_layout < GBA_Z_AUTO || options->z_layout > GBA_Z_PLANES) return GBA_ERR_INVALID;
   gba_plan* p = nullptr;
   try {
     p = new gba_plan();
@@ -2386,14 +2417,18 @@ int gba_autotune(const gba_problem* problems, const double* const* near_ys, cons
   int timed = 0;
   // one candidate: a plan, a warm-up run (graph capture), the best of three
   // timed replays, per LM iteration
-  auto time_one = [&](int pair_item, int image_item, int key_item, double* ms_per_it) -> int {
+  int resolved_layout = 0;   // the layout the last candidate's plan used
+  auto time_one = [&](int pair_item, int image_item, int key_item, double* ms_per_it,
+                      int z_layout) -> int {
     gba_options o = base;
     o.pair_item = pair_item;
     o.image_item = image_item;
     o.key_item = key_item;
+    o.z_layout = z_layout;
     gba_plan* plan = nullptr;
     int err = gba_plan_create(problems, near_ys, n, &o, &plan);
     if (err) return err;
+    resolved_layout = plan->impl.d.z_planes ? GBA_Z_PLANES : GBA_Z_RECORDS;
     err = set_all_x0(plan->impl, x0);
     double best = 0.0;
     for (int r = 0; r < 4 && !err; ++r) {
@@ -2410,30 +2445,40 @@ int gba_autotune(const gba_problem* problems, const double* const* near_ys, cons
     return GBA_OK;
   };
   double t_default = 0.0;
-  if (int e = time_one(gba::kPairItem, gba::kImageItem, gba::kKeyChunk, &t_default)) return e;
+  if (int e = time_one(gba::kPairItem, gba::kImageItem, gba::kKeyChunk, &t_default, base.z_layout)) return e;
   int best_pair = gba::kPairItem, best_image = gba::kImageItem, best_key = gba::kKeyChunk;
+  int best_layout = resolved_layout;
   double t_best = t_default;
   for (int pi : {256, 512, 2048, 4096}) {
     double t = 0.0;
-    if (time_one(pi, gba::kImageItem, gba::kKeyChunk, &t) == GBA_OK && t < t_best) {
+    if (time_one(pi, gba::kImageItem, gba::kKeyChunk, &t, best_layout) == GBA_OK && t < t_best) {
       t_best = t;
       best_pair = pi;
     }
   }
   for (int ii : {256, 1024}) {
     double t = 0.0;
-    if (time_one(best_pair, ii, gba::kKeyChunk, &t) == GBA_OK && t < t_best) {
+    if (time_one(best_pair, ii, gba::kKeyChunk, &t, best_layout) == GBA_OK && t < t_best) {
       t_best = t;
       best_image = ii;
     }
   }
   for (int ki : {256, 512, 2048}) {
     double t = 0.0;
-    if (time_one(best_pair, best_image, ki, &t) == GBA_OK && t < t_best) {
+    if (time_one(best_pair, best_image, ki, &t, best_layout) == GBA_OK && t < t_best) {
       t_best = t;
       best_key = ki;
     }
   }
+  if (base.z_layout == GBA_Z_AUTO) {   // the other layout of the Z records
+    const int other = best_layout == GBA_Z_PLANES ? GBA_Z_RECORDS : GBA_Z_PLANES;
+    double t = 0.0;
+    if (time_one(best_pair, best_image, best_key, &t, other) == GBA_OK && t < t_best) {
+      t_best = t;
+      best_layout = other;
+    }
+  }
+  out->z_layout = best_layout;
   out->pair_item = best_pair;
   out->image_item = best_image;
   out->key_item = best_key;

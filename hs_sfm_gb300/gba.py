@@ -138,8 +138,9 @@ def solve_batch(scenes, options=None):
 
 def autotune(scenes, options=None):
     """gba_autotune: the work-item sizes (pair_item, image_item, key_item)
-    that run the batch fastest, timed on the device; returns a dict with the
-    choice, its time per LM iteration and that of the defaults."""
+    and the Z layout that run the batch fastest, timed on the device;
+    returns a dict with the choice, its time per LM iteration and that of
+    the defaults."""
     L = lib()
     if not isinstance(scenes, (list, tuple)):
         scenes = [scenes]
@@ -153,7 +154,7 @@ def autotune(scenes, options=None):
     t = abi.Tuning()
     _check(L.gba_autotune(arr, yp, xp, len(scenes), C.byref(opt), C.byref(t)), "gba_autotune")
     return {"pair_item": t.pair_item, "image_item": t.image_item, "key_item": t.key_item,
-            "ms_per_iteration": t.ms_per_iteration,
+            "z_layout": t.z_layout, "ms_per_iteration": t.ms_per_iteration,
             "default_ms_per_iteration": t.default_ms_per_iteration, "candidates": t.candidates}
 
 

@@ -152,6 +152,10 @@ GBA_API int64_t gba_y_size(const gba_problem* problem);
 #define GBA_LINEAR_PCG            1  /* block-Jacobi PCG on the explicit
                                         block-sparse reduced system        */
 
+#define GBA_Z_AUTO    0
+#define GBA_Z_RECORDS 1  /* per-key records in key (point) order           */
+#define GBA_Z_PLANES  2  /* nine planes of value pairs, keys image by image */
+
 typedef struct gba_options {
   /* LevenbergMarquardt(max_itr_num, tau, eps1, eps2)
    * (camera_shared_levenberg_marquardt_optimizor.hpp:36-41). */
@@ -186,7 +190,12 @@ typedef struct gba_options {
    * Z kernels and of the cost's partial sums (so it changes the rounding of
    * the cost sum, not the model); gba_autotune picks it with the others. */
   int32_t key_item;
-  int32_t reserved_[1];
+  /* Layout of the Schur assembly's per-key records (GBA_Z_*): where they
+   * lie in memory, not their values or the sums' order (the same bits
+   * either way).  0 (auto): image-major planes when a block's key pairs
+   * cover a large share of its images' keys (small dense windows), else
+   * records in key order; gba_autotune times both. */
+  int32_t z_layout;
 } gba_options;
 
 /* Autotuning of the work-item sizes (gba_options.pair_item / image_item /
@@ -197,8 +206,9 @@ typedef struct gba_options {
  * pair_item is searched first over {256, 512, 1024, 2048, 4096} with the
  * default image_item and key_item, then image_item over {256, 512, 1024}
  * with the best pair_item, then key_item over {256, 512, 1024, 2048} with
- * the best two.  out receives the fastest sizes and their time per LM
- * iteration beside that of the defaults.  A status code. */
+ * the best two, then (options->z_layout auto) the other Z layout with the
+ * best sizes.  out receives the fastest sizes and layout and their time per
+ * LM iteration beside that of the defaults.  A status code. */
 typedef struct gba_tuning {
   int32_t pair_item;
   int32_t image_item;
@@ -207,7 +217,8 @@ typedef struct gba_tuning {
                                         key_item 1024                      */
   int32_t candidates;                /* configurations timed               */
   int32_t key_item;
-  int32_t reserved_[2];
+  int32_t z_layout;                  /* GBA_Z_RECORDS or GBA_Z_PLANES      */
+  int32_t reserved_[1];
 } gba_tuning;
 
 GBA_API int gba_autotune(const gba_problem* problems, const double* const* near_ys,

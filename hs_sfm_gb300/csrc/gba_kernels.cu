@@ -3274,7 +3274,6 @@ __global__ void k_ctrl_after_linearize(DevPlan d) {
     st.active = 0;
     st.stop = GBA_STOP_MAX_ITERATIONS;
   }
-  d.factor_flag[p] = 0;
 }
 
 // The LM step decision of problem p from the back-substitution's partial
@@ -3312,6 +3311,9 @@ __device__ void ctrl_step_body(const DevPlan& d, int p, double* red) {
     st.status = GBA_ERR_TIMEOUT;
     return;
   }
+  // the flag is consumed: cleared here (the next iteration's point factor
+  // may run beside the previous linearization's control, so not there)
+  d.factor_flag[p] = 0;
   if (failed) {
     st.factor_fail += 1;
     st.rejected += 1;

@@ -386,6 +386,10 @@ struct Plan {
   // passes it ran beyond the first of each loop (read back after each run)
   cudaStream_t pcg_stream = nullptr;
   unsigned long long* h_pcg_extra = nullptr;
+  // the second stream of an iteration's fork (image sums beside the point
+  // Schur and the assembly) and its fork / join events
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   unsigned long long pcg_extra_seen = 0;
   bool ran = false;
   long long launches_last_run = 0;
@@ -433,6 +437,9 @@ struct Plan {
     arena.release();
     if (stream) cudaStreamDestroy(stream);
     if (pcg_stream) cudaStreamDestroy(pcg_stream);
+    if (side_stream) cudaStreamDestroy(side_stream);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     if (h_pcg_extra) cudaFreeHost(h_pcg_extra);
   }
 
@@ -440,7 +447,10 @@ struct Plan {
             const gba_options* options);
   // parts of the launch sequence: everything, the prologue (initial cost
   // and linearization) or one LM iteration
-  enum Part { kAll, kPrologue, kIteration };
+  // kIteration starts with the previous linearization's image sums and
+  // control (beside the point Schur and the assembly, which do not need
+  // them); kEpilogue runs them for the last iteration
+  enum Part { kAll, kPrologue, kIteration, kEpilogue };
   void enqueue(bool profile, Part part = kAll);
   int run();
   int sync();
@@ -544,6 +554,11 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   GBA_CUDA(cudaSetDevice(device));
   GBA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   arena.stream = stream;
+  if (std::getenv("GBA_ONE_STREAM") == nullptr) {   // GBA_ONE_STREAM=1: no fork, for comparison
+    GBA_CUDA(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking));
+    GBA_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    GBA_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  }
   {
     // keep freed plan memory in the pool instead of returning it each time
     cudaMemPool_t pool;
@@ -1734,7 +1749,7 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
 void Plan::enqueue(bool profile, Part part) {
   cudaStream_t s = stream;
   long long n = 0;
-  const bool prologue = part != kIteration;
+  const bool prologue = part == kAll || part == kPrologue;
   const int iterations = part == kAll ? opt.max_iterations : (part == kIteration ? 1 : 0);
   size_t ev_i = 0;
   auto mark = [&](int stage) {
@@ -1766,10 +1781,30 @@ void Plan::enqueue(bool profile, Part part) {
     mark(GBA_STAGE_CONTROL);
   }
   for (int it = 0; it < iterations; ++it) {
+    // The image sums of the last linearization (nothing to do after the
+    // prologue's, or after a rejected step: they check relin) and the
+    // after-linearization control.  The point Schur and the key-pair
+    // assembly do not read them, so they run beside them on a second
+    // stream (the per-stage profile keeps one stream); a problem the control
+    // stops only wastes that scratch work, as every later stage checks it.
+    const bool side = !profile && side_stream != nullptr;
+    if (side) {
+      GBA_CUDA(cudaEventRecord(ev_fork, s));
+      GBA_CUDA(cudaStreamWaitEvent(side_stream, ev_fork, 0));
+      n += launch_image_reduce(d, side_stream);
+      n += launch_ctrl_after_linearize(d, side_stream);
+      GBA_CUDA(cudaEventRecord(ev_join, side_stream));
+    } else {
+      n += launch_image_reduce(d, s);
+      mark(GBA_STAGE_IMAGE_REDUCE);
+      n += launch_ctrl_after_linearize(d, s);
+      mark(GBA_STAGE_CONTROL);
+    }
     n += launch_point_schur(d, s);
     mark(GBA_STAGE_POINT_SCHUR);
     n += launch_assemble_items(d, s);
     mark(GBA_STAGE_ASSEMBLE);
+    if (side) GBA_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
     if (d.pcg) {
       n += launch_assemble_blocks(d, s);
       mark(GBA_STAGE_OTHER);
@@ -1797,10 +1832,14 @@ void Plan::enqueue(bool profile, Part part) {
     mark(GBA_STAGE_CONTROL);
     n += launch_linearize(d, s);
     mark(GBA_STAGE_LINEARIZE);
-    n += launch_image_reduce(d, s);
-    mark(GBA_STAGE_IMAGE_REDUCE);
-    n += launch_ctrl_after_linearize(d, s);
-    mark(GBA_STAGE_CONTROL);
+  }
+  if (part == kAll || part == kEpilogue) {
+    if (part == kEpilogue || opt.max_iterations > 0) {
+      n += launch_image_reduce(d, s);
+      mark(GBA_STAGE_IMAGE_REDUCE);
+      n += launch_ctrl_after_linearize(d, s);
+      mark(GBA_STAGE_CONTROL);
+    }
   }
   GBA_CUDA(cudaGetLastError());
   launches_last_run = n;
@@ -1858,7 +1897,8 @@ int Plan::run() {
       iter_launches = launches_last_run;
     }
     for (int it = 0; it < opt.max_iterations; ++it) GBA_CUDA(cudaGraphLaunch(iter_exec, stream));
-    launches_last_run = pro + iter_launches * opt.max_iterations;
+    enqueue(false, kEpilogue);
+    launches_last_run += pro + iter_launches * opt.max_iterations;
   } else {
     enqueue(profile);
   }

@@ -1,4 +1,5 @@
-"""The work-item sizes (gba_options.pair_item / image_item / key_item) and gba_autotune:
+"""The work-item sizes (gba_options.pair_item / image_item / key_item), the Z
+layout and gba_autotune:
 any item size gives the same model (costs within the parity tolerance of the
 default split and of the FP64 oracle, a problem's bits the same alone and in
 a batch with the same sizes), bad sizes are refused, and the tuner returns a
@@ -58,14 +59,19 @@ def test_autotune_picks_a_timed_candidate(gba):
               for n in (6, 12, 20, 30)]
     opt = abi.make_options(precision=abi.PRECISION_MIXED, max_iterations=10)
     t = gba.autotune(scenes, opt)
-    assert t["candidates"] == 10
+    assert t["candidates"] == 11   # ten item-size candidates, then the other Z layout
     assert t["pair_item"] in (256, 512, 1024, 2048, 4096)
     assert t["image_item"] in (256, 512, 1024)
     assert t["key_item"] in (256, 512, 1024, 2048)
+    assert t["z_layout"] in (abi.Z_RECORDS, abi.Z_PLANES)
     assert 0 < t["ms_per_iteration"] <= t["default_ms_per_iteration"]
+    # with the layout given, only the item sizes are searched
+    fixed = gba.autotune(scenes[:1], abi.make_options(precision=abi.PRECISION_MIXED, max_iterations=10,
+                                                      z_layout=abi.Z_RECORDS))
+    assert fixed["candidates"] == 10 and fixed["z_layout"] == abi.Z_RECORDS
     tuned = abi.make_options(precision=abi.PRECISION_MIXED, max_iterations=10, eps1=0.0, eps2=0.0,
                              pair_item=t["pair_item"], image_item=t["image_item"],
-                             key_item=t["key_item"])
+                             key_item=t["key_item"], z_layout=t["z_layout"])
     xs, reps = gba.solve_batch(scenes, tuned)
     _, _, rref = oracle.lm_solve(scenes[0], options=abi.make_options(max_iterations=10, eps1=0.0,
                                                                       eps2=0.0))

@@ -147,7 +147,6 @@ struct DevPlan {
   int* factor_flag;          // [B] 0 ok, 1 not positive definite, 2 a bounded wait ran out
   // dataflow factorization (one problem; df_grid == 0: per-column launches)
   int df_grid, df_max_own;
-  int df_assemble;           // 1: its CTAs form their tiles and rhs from the item sums (no S assembly)
   const int* df_own_off;     // [df_grid + 1] owned tiles of each CTA
   const int2* df_own;        // (i, j) per owned tile, sorted by (j, i) within a CTA
   unsigned* df_flags;        // [nt * nt] epoch at which tile (i, j) was published

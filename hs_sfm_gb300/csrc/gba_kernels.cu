@@ -1480,36 +1480,6 @@ __device__ __forceinline__ double reduced_grad(const DevPlan& d, const ProbInfo&
   return m < d.cam_info[ci].x ? d.gc[10LL * ci + m] : 0.0;
 }
 
-// Entry (row, col), col <= row, of problem p's dense reduced system: base -
-// the block's item sums (+ mu on the diagonal), in FP64, rounded to T once.
-template <typename T>
-__device__ __forceinline__ T reduced_entry(const DevPlan& d, const ProbInfo& pi, int p, double mu, int row,
-                                           int col) {
-  const int i = row / 6, a = row % 6, j = col / 6, bcol = col % 6;
-  const int blk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)j * pi.num_ext + i);
-  double v = 0.0;
-  if (blk >= 0) {   // four interleaved partial sums (loads in flight together), then in order
-    const int ib = __ldg(d.blk_item_off + blk), ie = __ldg(d.blk_item_off + blk + 1);
-    v = sum_items4(d.item_partial + 6 * bcol + a, ib, ie);
-  }
-  double s = reduced_base(d, pi, i, a, j, bcol) - v;
-  if (row == col) s += mu;
-  return T(s);
-}
-
-// Row `row` of problem p's rhs: g - the diagonal block's item sums.
-template <typename T>
-__device__ __forceinline__ T reduced_rhs(const DevPlan& d, const ProbInfo& pi, int p, int row) {
-  const int i = row / 6, a = row % 6;
-  const int dblk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)i * pi.num_ext + i);
-  double rv = 0.0;
-  if (dblk >= 0) {
-    const int ib = __ldg(d.blk_item_off + dblk), ie = __ldg(d.blk_item_off + dblk + 1);
-    rv = sum_items4(d.item_partial + 36 + a, ib, ie);
-  }
-  return T(reduced_grad(d, pi, i, a) - rv);
-}
-
 // Dense reduced system (lower triangle) and rhs in precision T; the block
 // sums over work items are taken in FP64.  Rows and columns run over the
 // problem's reduced-system images: its images, then with free cameras nc
@@ -1527,9 +1497,30 @@ __global__ void __launch_bounds__(256) k_assemble_S(DevPlan d) {
   if (idx >= (long long)n * n) return;
   const int row = int(idx / n), col = int(idx % n);
   if (col > row) return;
-  tptr_mut<T>(d.S)[pi.s_off + (long long)row * n + col] = reduced_entry<T>(d, pi, p, st.mu, row, col);
-  // rhs b_i[a] = g_i[a] - sum over the diagonal block's items
-  if (col == 0) tptr_mut<T>(d.b)[pi.ext_begin * 6LL + row] = reduced_rhs<T>(d, pi, p, row);
+  const int i = row / 6, a = row % 6, j = col / 6, bcol = col % 6;
+  const int Ie = pi.num_ext, ni = pi.num_images;
+  const int blk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)j * Ie + i);
+  double v = 0.0, rv = 0.0;
+  if (blk >= 0) {   // four interleaved partial sums (loads in flight together), then in order
+    const int ib = __ldg(d.blk_item_off + blk), ie = __ldg(d.blk_item_off + blk + 1);
+    v = sum_items4(d.item_partial + 6 * bcol + a, ib, ie);
+  }
+  (void)ni;
+  const double base = reduced_base(d, pi, i, a, j, bcol);
+  const double g = col == 0 ? reduced_grad(d, pi, i, a) : 0.0;
+  double s = base - v;
+  if (row == col) s += st.mu;
+  tptr_mut<T>(d.S)[pi.s_off + (long long)row * n + col] = T(s);
+  if (col == 0) {
+    // rhs b_i[a] = g_i[a] - sum over the diagonal block's items
+    const int dblk = __ldg(d.blk_map + d.blk_map_off[p] + (long long)i * Ie + i);
+    rv = 0.0;
+    if (dblk >= 0) {
+      const int ib = __ldg(d.blk_item_off + dblk), ie = __ldg(d.blk_item_off + dblk + 1);
+      rv = sum_items4(d.item_partial + 36 + a, ib, ie);
+    }
+    tptr_mut<T>(d.b)[6LL * (pi.ext_begin + i) + a] = T(g - rv);
+  }
 }
 
 // The same dense system, block by block (plans without free cameras): S is
@@ -1645,32 +1636,6 @@ struct TileFetch {
       T x = T(0);
       if (r < m) {
         if (c <= r) x = S[(long long)(kTile * ti + r) * n + kTile * ti + c];
-      } else if (r == c) {
-        x = T(1);
-      }
-      v[u] = x;
-    }
-  }
-  // The same tiles formed from the assembly's item sums (reduced_entry)
-  // instead of read from S.
-  __device__ __forceinline__ void rect_assembled(const DevPlan& d, const ProbInfo& pi, int p, double mu,
-                                                 int ti, int tj) {
-    const int n = pi.n, mi = tile_rows(n, ti), mj = tile_rows(n, tj);
-#pragma unroll
-    for (int u = 0; u < kPerThread; ++u) {
-      const int e = threadIdx.x + u * kCholThreads, r = e / kTile, c = e % kTile;
-      v[u] = (r < mi && c < mj) ? reduced_entry<T>(d, pi, p, mu, kTile * ti + r, kTile * tj + c) : T(0);
-    }
-  }
-  __device__ __forceinline__ void diag_assembled(const DevPlan& d, const ProbInfo& pi, int p, double mu,
-                                                 int ti) {
-    const int m = tile_rows(pi.n, ti);
-#pragma unroll
-    for (int u = 0; u < kPerThread; ++u) {
-      const int e = threadIdx.x + u * kCholThreads, r = e / kTile, c = e % kTile;
-      T x = T(0);
-      if (r < m) {
-        if (c <= r) x = reduced_entry<T>(d, pi, p, mu, kTile * ti + r, kTile * ti + c);
       } else if (r == c) {
         x = T(1);
       }
@@ -2086,21 +2051,12 @@ __global__ void __launch_bounds__(kDfThreads, 1) k_chol_dataflow(DevPlan d) {
           if (ti_s[u] == ti_s[t] && tj_s[u] == ti_s[t]) pr = u;
       pr_s[t] = pr;
     }
-    // owned tiles and rhs: read from S and b, or (df_assemble) formed here
-    // from the assembly's item sums, the chain's tiles first
-    for (int t = 0; t < nown; ++t) {
+    for (int t = 0; t < nown; ++t) {      // owned tiles and rhs
       TileFetch<T> f;
       const int i = ti_s[t], j = tj_s[t];
-      if (d.df_assemble) {
-        if (i == j) f.diag_assembled(d, pi, p, st.mu, i); else f.rect_assembled(d, pi, p, st.mu, i, j);
-      } else {
-        if (i == j) f.diag(S, n, i); else f.rect(S, n, i, j);
-      }
+      if (i == j) f.diag(S, n, i); else f.rect(S, n, i, j);
       f.store(A[t]);
-      if (i == j && tid < kTile)
-        bown[t * kTile + tid] = tid < tile_rows(n, i)
-                                    ? (d.df_assemble ? reduced_rhs<T>(d, pi, p, kTile * i + tid) : b[kTile * i + tid])
-                                    : T(0);
+      if (i == j && tid < kTile) bown[t * kTile + tid] = tid < tile_rows(n, i) ? b[kTile * i + tid] : T(0);
     }
   }
   __syncthreads();
@@ -3677,7 +3633,6 @@ int launch_assemble_items(const DevPlan& d, cudaStream_t s) {
 
 int launch_assemble_S(const DevPlan& d, cudaStream_t s) {
   if (d.max_n <= 0) return 0;
-  if (d.df_assemble) return 0;   // the dataflow factorization forms its tiles itself
   if (d.blk_prob && d.n_blocks > 0) {
     const size_t tsz = d.precision == GBA_PRECISION_MIXED ? sizeof(float) : sizeof(double);
     if (cudaMemsetAsync(d.S, 0, size_t(d.s_elems) * tsz, s) != cudaSuccess) throw CudaError{GBA_ERR_CUDA};

@@ -1468,7 +1468,6 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     GBA_CUDA(cudaMemsetAsync(D.cam_sum, 0, sizeof(double) * 3 * std::max<int64_t>(C, 1), stream));
   }
   D.df_grid = 0;
-  D.df_assemble = 0;
   D.df_trace = nullptr;
   D.pcg = pcg ? 1 : 0;
   D.pcg_max_iterations = opt.pcg_max_iterations;
@@ -1561,9 +1560,6 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     if (dataflow_layout(max_nt, mixed, device, &grid, &mo, &own_off, &own)) {
       D.df_grid = grid;
       D.df_max_own = mo;
-      // its CTAs form their own tiles from the item sums (no memset and
-      // assembly launches); GBA_DF_SEPARATE_ASSEMBLY=1 assembles S first
-      D.df_assemble = std::getenv("GBA_DF_SEPARATE_ASSEMBLY") == nullptr;
       // bounded waits: a CTA that finds nothing ready for this many polls
       // records GBA_ERR_TIMEOUT; GBA_DF_SPIN_LIMIT lowers it to test that path
       D.df_spin_limit = 1LL << 22;

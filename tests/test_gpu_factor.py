@@ -1,8 +1,7 @@
-"""The schedules of the dense factorization give the same bits: the
-single-launch dataflow factorization (one problem alone on the device, its
-tiles formed from the item sums in the kernel), the per-column launches
-(batches, or shared_device=1) and the small-system kernel, on systems of
-one to many tile columns, in both precisions."""
+"""The two schedules of the dense factorization give the same bits: the
+single-launch dataflow factorization (one problem alone on the device) and
+the per-column launches (batches, or shared_device=1), on systems of one to
+many tile columns, in both precisions."""
 import numpy as np
 import pytest
 
@@ -66,23 +65,3 @@ def test_small_system_kernel_equals_per_column_launches(images, monkeypatch):
         assert np.array_equal(a, b)
     assert np.array_equal(xs[0], x_df)
     assert reps[0].final_cost == repc[0].final_cost == r_df.final_cost
-
-
-@pytest.mark.parametrize("precision", [abi.PRECISION_MIXED, abi.PRECISION_FP64])
-def test_dataflow_forms_its_tiles_like_the_assembly(precision, monkeypatch):
-    """The dataflow factorization's CTAs form their tiles and rhs from the
-    item sums themselves (no dense assembly launch): the same bits as
-    assembling S first (GBA_DF_SEPARATE_ASSEMBLY=1), with the cameras fixed
-    and free."""
-    from hs_sfm_gb300 import gba
-    scenes = [synthetic.grid_scene(num_images=40, num_points=5000, seed=8),
-              synthetic.full_model_scene(seed=3, num_images=12, num_points=400, num_cameras=2, fix_mask=0)]
-    for s in scenes:
-        opt = abi.make_options(max_iterations=6, precision=precision, eps1=0.0, eps2=0.0)
-        x_in, r_in = gba.solve(s, opt)
-        monkeypatch.setenv("GBA_DF_SEPARATE_ASSEMBLY", "1")
-        x_sep, r_sep = gba.solve(s, opt)
-        monkeypatch.delenv("GBA_DF_SEPARATE_ASSEMBLY")
-        assert r_in.status == abi.GBA_OK
-        assert np.array_equal(x_in, x_sep)
-        assert r_in.final_cost == r_sep.final_cost

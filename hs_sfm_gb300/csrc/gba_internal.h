@@ -130,7 +130,9 @@ struct DevPlan {
   void* img_lin[2];          // [12I] T: r(3) t(3) ct s c a1 a2 pad
   // per key
   void* RW[2];               // [4K] T: rw0 rw1 sqrt(w) pad  (whitened, weighted residual)
-  void* JR;                  // [20K] T
+  void* JR[2];               // [20K] T, by parity: a candidate's records are formed
+                             // with its cost (fuse_lin) and become current if it is accepted
+  int fuse_lin;              // 1: the candidate cost kernels write the candidate's records
   void* Z;                   // [20(K+R)] T records, or 9 planes of z_n T pairs (z_planes)
   int z_planes;              // 1: Z as planes, slots image by image (img_keys order)
   long long z_n;             // plane stride in slots (>= K + R)
@@ -222,7 +224,7 @@ struct DevPlan {
   const int* prob_cam_off;        // [B + 1] cameras of each problem
   double* x_cam[2];               // [10 * Ctot] by parity
   double* x0_cam;
-  void* JC;                       // T: [20 K] camera Jacobian, 2 rows x 10 (all parameters)
+  void* JC[2];                    // T: [20 K] camera Jacobian, 2 rows x 10 (all parameters), by parity
   const int* pt_rec_off;          // [P + 1] camera records of each point (indices >= K)
   const int2* rec_info;           // [R] (global camera, ext index)
   double* img_item_cam;           // [n_img_items * kImgCamVals] partial sums of image items
@@ -275,7 +277,9 @@ int launch_init(const DevPlan& d, cudaStream_t s);
 int launch_image_prep(const DevPlan& d, int which, cudaStream_t s);
 int launch_cost(const DevPlan& d, int which, cudaStream_t s);
 int launch_ctrl_initial_cost(const DevPlan& d, cudaStream_t s);
-int launch_linearize(const DevPlan& d, cudaStream_t s);
+// keys = false: the point sums only (the records were formed with the
+// accepted candidate's cost)
+int launch_linearize(const DevPlan& d, cudaStream_t s, bool keys = true);
 int launch_image_reduce(const DevPlan& d, cudaStream_t s);
 int launch_ctrl_after_linearize(const DevPlan& d, cudaStream_t s);
 int launch_point_schur(const DevPlan& d, cudaStream_t s);

@@ -623,6 +623,106 @@ __global__ void __launch_bounds__(256) k_cons_cost(DevPlan d, int which) {
 // ---------------------------------------------------------------------------
 // cost: FP64 residual per key, whitened and weighted residual stored in T
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// linearize, one thread per key (coalesced JR records): the analytical
+// Jacobian of the key, whitened by the key weight and the IRLS weight, into
+// the records of parity `par` (and the camera block with free cameras).
+// X, il, cam are the point, the image's linearisation coefficients and the
+// camera at that parity; rw0, rw1, sw the key's weighted residual and the
+// square root of its IRLS weight.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void linearize_key(const DevPlan& d, int k, int par, int fix, const T* X, const T* il,
+                                              const T* cam, T rw0, T rw1, T sw) {
+  T jp[6], ji[12], nrm[2];
+  key_jacobian<T>(X, il, cam, jp, ji, nrm);
+  if (fix & 1) {   // fixed points: no point columns
+#pragma unroll
+    for (int m = 0; m < 6; ++m) jp[m] = T(0);
+  }
+  if (fix & 2) {   // fixed images: no image columns
+#pragma unroll
+    for (int m = 0; m < 12; ++m) ji[m] = T(0);
+  }
+  if (d.free_cams) {   // the camera block, whitened and weighted as the others
+    T jc[20];
+    camera_jacobian<T>(nrm[0], nrm[1], cam, jc);
+    T l00 = T(1), l10 = T(0), l11 = T(1);
+    if (d.key_wl) {
+      l00 = T(__ldg(d.key_wl + 3LL * k));
+      l10 = T(__ldg(d.key_wl + 3LL * k + 1));
+      l11 = T(__ldg(d.key_wl + 3LL * k + 2));
+    }
+#pragma unroll
+    for (int m = 0; m < 10; ++m) {
+      const T a = jc[m], b = jc[10 + m];
+      jc[m] = (l00 * a + l10 * b) * sw;
+      jc[10 + m] = l11 * b * sw;
+    }
+    store_vec<20>(tptr_mut<T>(d.JC[par]) + 20LL * k, jc);
+  }
+  if (d.key_wl) {
+    const T l00 = T(__ldg(d.key_wl + 3LL * k)), l10 = T(__ldg(d.key_wl + 3LL * k + 1)),
+            l11 = T(__ldg(d.key_wl + 3LL * k + 2));
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const T a = jp[m], b = jp[3 + m];
+      jp[m] = (l00 * a + l10 * b) * sw;
+      jp[3 + m] = l11 * b * sw;
+    }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const T a = ji[m], b = ji[6 + m];
+      ji[m] = (l00 * a + l10 * b) * sw;
+      ji[6 + m] = l11 * b * sw;
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < 6; ++m) jp[m] *= sw;
+#pragma unroll
+    for (int m = 0; m < 12; ++m) ji[m] *= sw;
+  }
+  T rec[kJRStride];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) rec[m] = jp[m];
+#pragma unroll
+  for (int m = 0; m < 12; ++m) rec[6 + m] = ji[m];
+  rec[18] = rw0;
+  rec[19] = rw1;
+  store_vec<kJRStride>(tptr_mut<T>(d.JR[par]) + (long long)kJRStride * k, rec);
+}
+
+// The prologue's linearization (and, with DevPlan::fuse_lin off, every
+// iteration's): the records at the problem's current parity.
+template <typename T>
+__global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
+  const Chunk ch = d.key_chunks[blockIdx.x];
+  const LMState& st = d.state[ch.prob];
+  if (!st.relin || !st.active) return;
+  const int par = st.parity;
+  const double* __restrict__ xp = d.x_pt[par];
+  const T* __restrict__ IL = tptr<T>(d.img_lin[par]);
+  const T* __restrict__ rwb = tptr<T>(d.RW[par]);
+  const int fix = d.prob[ch.prob].fix;
+  for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
+    const int img = __ldg(d.key_img + k), pt = __ldg(d.key_pt + k);
+    T X[3];
+    if (sizeof(T) == sizeof(float) && d.x_ff[par]) {   // mixed: high part of the mirror
+      const float2* xf = d.x_ff[par] + 3LL * pt;
+      X[0] = T(xf[0].x); X[1] = T(xf[1].x); X[2] = T(xf[2].x);
+    } else {
+      X[0] = T(xp[3LL * pt]); X[1] = T(xp[3LL * pt + 1]); X[2] = T(xp[3LL * pt + 2]);
+    }
+    T il[12];
+    load_vec<12>(IL + 12LL * img, il);
+    T cam[10];
+    load_cam<T>(d, par, __ldg(d.img_cam + img), cam);
+    T rw[4];
+    load_vec<4>(rwb + 4LL * k, rw);
+    linearize_key<T>(d, k, par, fix, X, il, cam, rw[0], rw[1], rw[2]);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
   __shared__ double red[32];
@@ -663,6 +763,12 @@ __global__ void __launch_bounds__(256) k_cost(DevPlan d, int which) {
     const double sw = (w == 1.0) ? 1.0 : sqrt(w);
     T out[4] = {T(e0 * sw), T(e1 * sw), T(sw), T(0)};
     store_vec<4>(rw + 4LL * k, out);
+    if (which == 1 && d.fuse_lin) {   // the candidate's Jacobian records, used if it is accepted
+      T Xl[3] = {T(X[0]), T(X[1]), T(X[2])}, il[12], cl[10];
+      load_vec<12>(tptr<T>(d.img_lin[par]) + 12LL * img, il);
+      load_cam<T>(d, par, ci, cl);
+      linearize_key<T>(d, k, par, d.prob[ch.prob].fix, Xl, il, cl, out[0], out[1], out[2]);
+    }
   }
   const double tot = block_sum(acc, red);
   const double tot_raw = block_sum(acc_raw, red);
@@ -755,6 +861,13 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
     }
     float out[4] = {e0 * sw, e1 * sw, sw, 0.0f};
     store_vec<4>(rw + 4LL * k, out);
+    if (which == 1 && d.fuse_lin) {   // the candidate's Jacobian records, used if it is accepted
+      const float Xl[3] = {X0.hi, X1.hi, X2.hi};
+      float il[12], cl[10];
+      load_vec<12>(static_cast<const float*>(d.img_lin[par]) + 12LL * img, il);
+      load_cam<float>(d, par, __ldg(d.img_cam + img), cl);
+      linearize_key<float>(d, k, par, d.prob[ch.prob].fix, Xl, il, cl, out[0], out[1], out[2]);
+    }
   }
   const double tot = block_sum(double(acc.hi) + double(acc.lo), red);
   const double tot_raw = block_sum(acc_raw, red);
@@ -771,97 +884,6 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// linearize, one thread per key (coalesced JR records): the analytical
-// Jacobian of the key, whitened by the key weight and the IRLS weight.
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
-  const Chunk ch = d.key_chunks[blockIdx.x];
-  const LMState& st = d.state[ch.prob];
-  if (!st.relin || !st.active) return;
-  const int par = st.parity;
-  const double* __restrict__ xp = d.x_pt[par];
-  const T* __restrict__ IL = tptr<T>(d.img_lin[par]);
-  const T* __restrict__ rwb = tptr<T>(d.RW[par]);
-  T* __restrict__ JR = tptr_mut<T>(d.JR);
-  const int fix = d.prob[ch.prob].fix;
-  for (int k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) {
-    const int img = __ldg(d.key_img + k), pt = __ldg(d.key_pt + k);
-    T X[3];
-    if (sizeof(T) == sizeof(float) && d.x_ff[par]) {   // mixed: high part of the mirror
-      const float2* xf = d.x_ff[par] + 3LL * pt;
-      X[0] = T(xf[0].x); X[1] = T(xf[1].x); X[2] = T(xf[2].x);
-    } else {
-      X[0] = T(xp[3LL * pt]); X[1] = T(xp[3LL * pt + 1]); X[2] = T(xp[3LL * pt + 2]);
-    }
-    T il[12];
-    load_vec<12>(IL + 12LL * img, il);
-    T cam[10];
-    const int ci = __ldg(d.img_cam + img);
-    load_cam<T>(d, par, ci, cam);
-    T jp[6], ji[12], nrm[2];
-    key_jacobian<T>(X, il, cam, jp, ji, nrm);
-    if (fix & 1) {   // fixed points: no point columns
-#pragma unroll
-      for (int m = 0; m < 6; ++m) jp[m] = T(0);
-    }
-    if (fix & 2) {   // fixed images: no image columns
-#pragma unroll
-      for (int m = 0; m < 12; ++m) ji[m] = T(0);
-    }
-    T rw[4];
-    load_vec<4>(rwb + 4LL * k, rw);
-    const T sw = rw[2];
-    if (d.free_cams) {   // the camera block, whitened and weighted as the others
-      T jc[20];
-      camera_jacobian<T>(nrm[0], nrm[1], cam, jc);
-      T l00 = T(1), l10 = T(0), l11 = T(1);
-      if (d.key_wl) {
-        l00 = T(__ldg(d.key_wl + 3LL * k));
-        l10 = T(__ldg(d.key_wl + 3LL * k + 1));
-        l11 = T(__ldg(d.key_wl + 3LL * k + 2));
-      }
-#pragma unroll
-      for (int m = 0; m < 10; ++m) {
-        const T a = jc[m], b = jc[10 + m];
-        jc[m] = (l00 * a + l10 * b) * sw;
-        jc[10 + m] = l11 * b * sw;
-      }
-      store_vec<20>(tptr_mut<T>(d.JC) + 20LL * k, jc);
-    }
-    if (d.key_wl) {
-      const T l00 = T(__ldg(d.key_wl + 3LL * k)), l10 = T(__ldg(d.key_wl + 3LL * k + 1)),
-              l11 = T(__ldg(d.key_wl + 3LL * k + 2));
-#pragma unroll
-      for (int m = 0; m < 3; ++m) {
-        const T a = jp[m], b = jp[3 + m];
-        jp[m] = (l00 * a + l10 * b) * sw;
-        jp[3 + m] = l11 * b * sw;
-      }
-#pragma unroll
-      for (int m = 0; m < 6; ++m) {
-        const T a = ji[m], b = ji[6 + m];
-        ji[m] = (l00 * a + l10 * b) * sw;
-        ji[6 + m] = l11 * b * sw;
-      }
-    } else {
-#pragma unroll
-      for (int m = 0; m < 6; ++m) jp[m] *= sw;
-#pragma unroll
-      for (int m = 0; m < 12; ++m) ji[m] *= sw;
-    }
-    T rec[kJRStride];
-#pragma unroll
-    for (int m = 0; m < 6; ++m) rec[m] = jp[m];
-#pragma unroll
-    for (int m = 0; m < 12; ++m) rec[6 + m] = ji[m];
-    rec[18] = rw[0];
-    rec[19] = rw[1];
-    store_vec<kJRStride>(JR + (long long)kJRStride * k, rec);
-  }
-}
-
 // Per point: V_p = sum J_p^T J_p, g_p = sum J_p^T r from its keys' records.
 template <typename T>
 __global__ void __launch_bounds__(kPointChunk) k_point_reduce(DevPlan d) {
@@ -872,7 +894,7 @@ __global__ void __launch_bounds__(kPointChunk) k_point_reduce(DevPlan d) {
   const int pt = ch.begin + threadIdx.x;
   double vmax = 0.0, gmax = 0.0;
   if (pt < ch.end) {
-    const T* __restrict__ JR = tptr<T>(d.JR);
+    const T* __restrict__ JR = tptr<T>(d.JR[st.parity]);
     T V[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0};
     const int kb = __ldg(d.pt_key_off + pt), ke = __ldg(d.pt_key_off + pt + 1);
     for (int k = kb; k < ke; ++k) {
@@ -946,7 +968,7 @@ __global__ void __launch_bounds__(256) k_image_reduce(DevPlan d) {
   const int4 it = __ldg(d.img_items + wid);   // (image, q begin, q end, prob)
   const LMState& st = d.state[it.w];
   if (!st.relin || !st.active) return;
-  const T* __restrict__ JR = tptr<T>(d.JR);
+  const T* __restrict__ JR = tptr<T>(d.JR[st.parity]);
   T acc[27], cmp[27];
 #pragma unroll
   for (int e = 0; e < 27; ++e) { acc[e] = T(0); cmp[e] = T(0); }
@@ -1051,8 +1073,8 @@ __global__ void __launch_bounds__(128) k_image_cam_reduce(DevPlan d) {
   const LMState& st = d.state[it.w];
   if (!st.relin || !st.active) return;
   if (d.cam_info[d.img_cam[it.x]].x == 0) return;
-  const T* __restrict__ JR = tptr<T>(d.JR);
-  const T* __restrict__ JC = tptr<T>(d.JC);
+  const T* __restrict__ JR = tptr<T>(d.JR[st.parity]);
+  const T* __restrict__ JC = tptr<T>(d.JC[st.parity]);
   const int e = threadIdx.x;
   int ca = 0, cb = 0;
   if (e < 60) {
@@ -1230,7 +1252,7 @@ __global__ void __launch_bounds__(256) k_key_z(DevPlan d) {
   const Chunk ch = d.key_chunks[blockIdx.x / split];
   const LMState& st = d.state[ch.prob];
   if (!st.active) return;
-  const T* __restrict__ JR = tptr<T>(d.JR);
+  const T* __restrict__ JR = tptr<T>(d.JR[st.parity]);
   const T* __restrict__ PS = tptr<T>(d.PS);
   T* __restrict__ Z = tptr_mut<T>(d.Z);
   const int sub = blockIdx.x % split;
@@ -1272,8 +1294,8 @@ __global__ void __launch_bounds__(kPointChunk) k_camrec_z(DevPlan d) {
   if (pt >= ch.end) return;
   const int rb = d.pt_rec_off[pt], re = d.pt_rec_off[pt + 1];
   if (rb == re) return;
-  const T* __restrict__ JR = tptr<T>(d.JR);
-  const T* __restrict__ JC = tptr<T>(d.JC);
+  const T* __restrict__ JR = tptr<T>(d.JR[st.parity]);
+  const T* __restrict__ JC = tptr<T>(d.JC[st.parity]);
   T ps[8];
   load_vec<8>(tptr<T>(d.PS) + 12LL * pt, ps);
   const T i00 = ps[0], m10 = ps[1], i11 = ps[2], m20 = ps[3], m21 = ps[4], i22 = ps[5];
@@ -3066,7 +3088,7 @@ __global__ void __launch_bounds__(kPointChunk) k_backsub(DevPlan d) {
       T ps[12];
       load_vec<12>(tptr<T>(d.PS) + 12LL * pt, ps);
       const T i00 = ps[0], m10 = ps[1], i11 = ps[2], m20 = ps[3], m21 = ps[4], i22 = ps[5];
-      const T* __restrict__ JR = tptr<T>(d.JR);
+      const T* __restrict__ JR = tptr<T>(d.JR[st.parity]);
       const int kb = __ldg(d.pt_key_off + pt), ke = __ldg(d.pt_key_off + pt + 1);
       // w = sum over the point's keys of J_p^T (J_i delta_i) from the
       // Jacobian records (the point's keys are consecutive), then
@@ -3565,9 +3587,9 @@ int launch_ctrl_initial_cost(const DevPlan& d, cudaStream_t s) {
   return 1;
 }
 
-int launch_linearize(const DevPlan& d, cudaStream_t s) {
+int launch_linearize(const DevPlan& d, cudaStream_t s, bool keys) {
   int n = 0;
-  if (d.n_key_chunks > 0) {
+  if (keys && d.n_key_chunks > 0) {
     GBA_DISPATCH(d, (k_linearize_keys<T><<<d.n_key_chunks, 256, 0, s>>>(d)));
     ++n;
   }

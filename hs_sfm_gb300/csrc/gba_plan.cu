@@ -1413,7 +1413,10 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   }
   D.x0_pt = arena.alloc<double>(3 * P);
   D.x0_img = arena.alloc<double>(6 * I);
-  D.JR = arena.alloc<char>(size_t(kJRStride) * K * tsz);
+  D.JR[0] = arena.alloc<char>(size_t(kJRStride) * K * tsz);
+  D.JR[1] = arena.alloc<char>(size_t(kJRStride) * K * tsz);
+  // GBA_SEPARATE_LINEARIZE=1: every iteration relinearizes in its own launch
+  D.fuse_lin = std::getenv("GBA_SEPARATE_LINEARIZE") == nullptr;
   D.z_n = (K + R + 31) / 32 * 32;
   D.Z = arena.alloc<char>(std::max<size_t>(size_t(kZStride) * (K + R), 18 * size_t(D.z_n)) * tsz);
   D.PV = arena.alloc<char>(12 * P * tsz);
@@ -1456,7 +1459,8 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     D.x_cam[1] = arena.alloc<double>(10 * C);
     D.x0_cam = arena.alloc<double>(10 * C);
     GBA_CUDA(cudaMemsetAsync(D.x0_cam, 0, sizeof(double) * 10 * std::max<int64_t>(C, 1), stream));
-    D.JC = arena.alloc<char>(size_t(20) * K * tsz);
+    D.JC[0] = arena.alloc<char>(size_t(20) * K * tsz);
+    D.JC[1] = arena.alloc<char>(size_t(20) * K * tsz);
     D.pt_rec_off = arena.upload(pt_rec_off);
     D.rec_info = arena.upload(rec_info);
     D.img_item_cam = arena.alloc<double>(size_t(kImgCamVals) * std::max<size_t>(img_items.size(), 1));
@@ -1830,7 +1834,7 @@ void Plan::enqueue(bool profile, Part part) {
     mark(GBA_STAGE_COST);
     n += launch_ctrl_accept(d, s);
     mark(GBA_STAGE_CONTROL);
-    n += launch_linearize(d, s);
+    n += launch_linearize(d, s, !d.fuse_lin);
     mark(GBA_STAGE_LINEARIZE);
   }
   if (part == kAll || part == kEpilogue) {

@@ -269,7 +269,7 @@ int64_t gba_estimate_device_bytes(const gba_problem* p, int32_t precision) {
   const int64_t blocks = Ie * (Ie + 1) / 2;
   const int64_t items = pairs / 1024 + blocks + 1;
   int64_t b = 0;
-  b += K * (4 + 4 + 16 + 4 + 8 * tsz + 20 * tsz + 20 * tsz);   // indices, obs, RW, JR, Z
+  b += K * (4 + 4 + 16 + 4 + 8 * tsz + 40 * tsz + 20 * tsz);   // indices, obs, RW, JR (x2), Z
   if (p->key_covariance_inverse) b += K * 24;
   if (precision == GBA_PRECISION_MIXED) b += K * 16 + P * 48 + I * 192;   // double-float mirrors
   b += P * (4 + 4 + 48 + 24 + 24 * tsz + 24);                 // offsets, x, x0, PV, PS, sums
@@ -280,7 +280,7 @@ int64_t gba_estimate_device_bytes(const gba_problem* p, int32_t precision) {
   b += pairs * 8 + items * (16 + 352) + blocks * 12 + Ie * Ie * 4;
   if (free_cams) {
     b += recs * (20 * tsz + 12) + P * 4;                        // camera Z records, offsets
-    b += K * 20 * tsz + (K / 512 + 1) * 128 * 8 + I * (60 * 8 + 128 * 8 + 4);   // J_c, sums, E, ext
+    b += K * 40 * tsz + (K / 512 + 1) * 128 * 8 + I * (60 * 8 + 128 * 8 + 4);   // J_c (x2), sums, E, ext
     b += C * (3 * 80 + 100 * 8 + 10 * 8 + 3 * 8 + 2 * (80 + 40 + 80) + 16 + 8) + I * 4;
   }
   const int64_t rows = gba_y_size(p) - 2 * K;                   // constraint and prior rows

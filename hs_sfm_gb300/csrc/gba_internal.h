@@ -31,6 +31,8 @@ constexpr int kJRStride = 20;      // per key: Jp(6) Ji(12) rw(2)
 constexpr int kZStride = 20;       // per key: Z(18) + pad
 // Z planes from this mean share of an image's keys in a block's key pairs
 constexpr double kZPlanesDensity = 0.2;
+// Plans with at least this many keys fork each LM iteration (two streams)
+constexpr long long kForkMinKeys = 300000;
 constexpr int kItemStride = 44;    // per work item: 36 block + 6 rhs + pad
 
 // Per-problem LM state (device).  Written only by the control kernels.

@@ -554,11 +554,6 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
   GBA_CUDA(cudaSetDevice(device));
   GBA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   arena.stream = stream;
-  if (std::getenv("GBA_ONE_STREAM") == nullptr) {   // GBA_ONE_STREAM=1: no fork, for comparison
-    GBA_CUDA(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking));
-    GBA_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-    GBA_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-  }
   {
     // keep freed plan memory in the pool instead of returning it each time
     cudaMemPool_t pool;
@@ -599,6 +594,20 @@ int Plan::build(const gba_problem* problems, const double* const* near_ys, int n
     C += problems[q].number_of_cameras;
   }
   if (P > INT32_MAX / 4 || K > INT32_MAX / 4 || I > INT32_MAX / 64) return GBA_ERR_INVALID;
+  // The iteration's fork (image sums beside the point Schur and the
+  // assembly) pays where one plan's stages leave the GPU partly idle; small
+  // plans (a server's micro-batches, several in flight) lose more to the
+  // fork's setup and joins than they gain.  GBA_ONE_STREAM=1: never fork;
+  // GBA_FORK=1: always.
+  {
+    const bool fork = std::getenv("GBA_ONE_STREAM") == nullptr &&
+                      (K >= kForkMinKeys || std::getenv("GBA_FORK") != nullptr);
+    if (fork) {
+      GBA_CUDA(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking));
+      GBA_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      GBA_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    }
+  }
 
   HostBuf<int> key_img(K), key_pt(K), img_keys(K);
   HostBuf<double2> key_obs(K);

@@ -1,7 +1,8 @@
 """Two changes of an LM iteration's schedule that change no arithmetic:
 * the fork: the image sums and the after-linearization control of the
   previous linearization run on a second stream beside the point Schur and
-  the key-pair assembly (GBA_ONE_STREAM=1 keeps one stream);
+  the key-pair assembly (plans of 300k keys or more; GBA_FORK=1 forks these
+  small test plans too, GBA_ONE_STREAM=1 keeps one stream);
 * the candidate's Jacobian records are formed by the candidate cost kernel
   into the other parity's buffer and become current when the step is
   accepted (GBA_SEPARATE_LINEARIZE=1 relinearizes in its own launch after
@@ -18,7 +19,8 @@ from hs_sfm_gb300 import abi, synthetic
 
 pytestmark = pytest.mark.gpu
 
-SWITCHES = ["GBA_ONE_STREAM", "GBA_SEPARATE_LINEARIZE"]
+# (environment of the first run, of the second run)
+SWITCHES = [("GBA_FORK", "GBA_ONE_STREAM"), (None, "GBA_SEPARATE_LINEARIZE")]
 
 
 @pytest.fixture(scope="module")
@@ -29,10 +31,15 @@ def gba():
 
 
 def _both(gba, monkeypatch, env, scenes, opt):
+    first, second = env
+    if first:
+        monkeypatch.setenv(first, "1")
     xs, reps = gba.solve_batch(scenes, opt)
-    monkeypatch.setenv(env, "1")
+    if first:
+        monkeypatch.delenv(first)
+    monkeypatch.setenv(second, "1")
     xo, repo = gba.solve_batch(scenes, opt)
-    monkeypatch.delenv(env)
+    monkeypatch.delenv(second)
     for a, b, ra, rb in zip(xs, xo, reps, repo):
         np.testing.assert_array_equal(a, b)
         assert ra.final_cost == rb.final_cost
@@ -60,10 +67,14 @@ def test_same_bits_with_rejected_steps(gba, monkeypatch, env, precision):
                                                               precision=precision))
     assert reps[0].rejected > 0 and reps[0].accepted > 0
     # alone (one-problem dense plan: the dataflow factorization) as well
+    if env[0]:
+        monkeypatch.setenv(env[0], "1")
     x1, r1 = gba.solve(s, abi.make_options(max_iterations=12, eps1=0.0, eps2=0.0, precision=precision))
-    monkeypatch.setenv(env, "1")
+    if env[0]:
+        monkeypatch.delenv(env[0])
+    monkeypatch.setenv(env[1], "1")
     x2, r2 = gba.solve(s, abi.make_options(max_iterations=12, eps1=0.0, eps2=0.0, precision=precision))
-    monkeypatch.delenv(env)
+    monkeypatch.delenv(env[1])
     np.testing.assert_array_equal(x1, x2)
     assert (r1.accepted, r1.rejected) == (r2.accepted, r2.rejected)
 

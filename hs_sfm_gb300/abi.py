@@ -134,8 +134,8 @@ class Report(C.Structure):
 class PlanStructure(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "problems", "keys", "points", "images", "key_pairs", "pair_items", "blocks",
-        "image_items", "camera_records", "max_reduced_size", "factor_schedule")] + \
-        [("reserved_", C.c_int64 * 3)]
+        "image_items", "camera_records", "max_reduced_size", "factor_schedule", "z_layout",
+        "forked")] + [("reserved_", C.c_int64 * 1)]
 
     def as_dict(self):
         return {name: int(getattr(self, name)) for name, _ in self._fields_ if name != "reserved_"}

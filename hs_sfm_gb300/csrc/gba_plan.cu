@@ -2365,7 +2365,9 @@ int gba_plan_structure(gba_plan* p, gba_plan_structure_info* out) {
   out->image_items = P.d.n_img_items;
   out->camera_records = P.d.R;
   out->max_reduced_size = P.d.max_n;
-  out->factor_schedule = P.d.pcg ? -1 : P.d.df_grid > 0 ? 1 : 0;
+  out->factor_schedule = P.d.pcg ? -1 : P.d.df_grid > 0 ? 1 : P.d.chol_small ? 2 : 0;
+  out->z_layout = P.d.z_planes ? GBA_Z_PLANES : GBA_Z_RECORDS;
+  out->forked = P.side_stream != nullptr ? 1 : 0;
   return GBA_OK;
 }
 

@@ -344,8 +344,12 @@ typedef struct gba_plan_structure_info {
   int64_t max_reduced_size; /* largest reduced system (unknowns)             */
   int64_t factor_schedule;  /* dense factorization: 0 one launch per tile
                                column (batches), 1 one dataflow launch,
-                               -1 PCG                                      */
-  int64_t reserved_[3];
+                               2 one small-system launch (batches of
+                               systems of at most 8 tile rows), -1 PCG     */
+  int64_t z_layout;         /* the Schur assembly's records: GBA_Z_RECORDS
+                               or GBA_Z_PLANES                             */
+  int64_t forked;           /* 1: each LM iteration runs on two streams    */
+  int64_t reserved_[1];
 } gba_plan_structure_info;
 GBA_API int gba_plan_structure(gba_plan* plan, gba_plan_structure_info* out);
 

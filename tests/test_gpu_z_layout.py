@@ -73,3 +73,25 @@ def test_invalid_layout_is_refused(gba):
     with pytest.raises(gba.GbaError) as e:
         gba.solve(s, abi.make_options(z_layout=3))
     assert e.value.status == abi.GBA_ERR_INVALID
+
+
+def test_structure_reports_the_layout_and_the_fork(gba):
+    """gba_plan_structure says which layout and schedule a plan took: planes
+    for dense windows, records for the sparse grid; the iteration forks
+    only in plans of at least 300k keys; small batches factor in the
+    small-system kernel, one problem in the dataflow launch."""
+    wins = [synthetic.ring_scene(num_images=12, num_points=1500, obs_range=(3, 8), seed=s) for s in (5, 6)]
+    grid = synthetic.grid_scene(num_images=100, num_points=60000, seed=9)
+    opt = abi.make_options(max_iterations=2, precision=abi.PRECISION_MIXED)
+    p = gba.Plan(wins, opt)
+    st = p.structure()
+    p.close()
+    assert st["z_layout"] == abi.Z_PLANES and st["forked"] == 0 and st["factor_schedule"] == 2
+    assert grid.number_of_keys >= 300_000
+    p = gba.Plan(grid, opt)
+    st = p.structure()
+    p.close()
+    assert st["z_layout"] == abi.Z_RECORDS and st["forked"] == 1 and st["factor_schedule"] == 1
+    p = gba.Plan(grid, abi.make_options(max_iterations=2, precision=abi.PRECISION_MIXED, z_layout=abi.Z_PLANES))
+    assert p.structure()["z_layout"] == abi.Z_PLANES
+    p.close()

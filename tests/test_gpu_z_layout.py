@@ -81,7 +81,7 @@ def test_structure_reports_the_layout_and_the_fork(gba):
     only in plans of at least 300k keys; small batches factor in the
     small-system kernel, one problem in the dataflow launch."""
     wins = [synthetic.ring_scene(num_images=12, num_points=1500, obs_range=(3, 8), seed=s) for s in (5, 6)]
-    grid = synthetic.grid_scene(num_images=100, num_points=60000, seed=9)
+    grid = synthetic.grid_scene(num_images=200, num_points=100000, seed=1)   # the bench's grid
     opt = abi.make_options(max_iterations=2, precision=abi.PRECISION_MIXED)
     p = gba.Plan(wins, opt)
     st = p.structure()

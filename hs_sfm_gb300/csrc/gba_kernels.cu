@@ -692,14 +692,9 @@ __device__ __forceinline__ void linearize_key(const DevPlan& d, int k, int par, 
   store_vec<kJRStride>(tptr_mut<T>(d.JR[par]) + (long long)kJRStride * k, rec);
 }
 
-// The prologue's linearization (and, with DevPlan::fuse_lin off, every
-// iteration's): the records at the problem's current parity.
+// The records of a key chunk at parity par, one key per thread.
 template <typename T>
-__global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
-  const Chunk ch = d.key_chunks[blockIdx.x];
-  const LMState& st = d.state[ch.prob];
-  if (!st.relin || !st.active) return;
-  const int par = st.parity;
+__device__ __forceinline__ void linearize_chunk(const DevPlan& d, const Chunk& ch, int par) {
   const double* __restrict__ xp = d.x_pt[par];
   const T* __restrict__ IL = tptr<T>(d.img_lin[par]);
   const T* __restrict__ rwb = tptr<T>(d.RW[par]);
@@ -721,6 +716,16 @@ __global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
     load_vec<4>(rwb + 4LL * k, rw);
     linearize_key<T>(d, k, par, fix, X, il, cam, rw[0], rw[1], rw[2]);
   }
+}
+
+// The prologue's linearization (and, with DevPlan::fuse_lin off, every
+// iteration's): the records at the problem's current parity.
+template <typename T>
+__global__ void __launch_bounds__(256) k_linearize_keys(DevPlan d) {
+  const Chunk ch = d.key_chunks[blockIdx.x];
+  const LMState& st = d.state[ch.prob];
+  if (!st.relin || !st.active) return;
+  linearize_chunk<T>(d, ch, st.parity);
 }
 
 template <typename T>
@@ -861,14 +866,11 @@ __global__ void __launch_bounds__(256) k_cost_ff(DevPlan d, int which) {
     }
     float out[4] = {e0 * sw, e1 * sw, sw, 0.0f};
     store_vec<4>(rw + 4LL * k, out);
-    if (which == 1 && d.fuse_lin) {   // the candidate's Jacobian records, used if it is accepted
-      const float Xl[3] = {X0.hi, X1.hi, X2.hi};
-      float il[12], cl[10];
-      load_vec<12>(static_cast<const float*>(d.img_lin[par]) + 12LL * img, il);
-      load_cam<float>(d, par, __ldg(d.img_cam + img), cl);
-      linearize_key<float>(d, k, par, d.prob[ch.prob].fix, Xl, il, cl, out[0], out[1], out[2]);
-    }
   }
+  // the candidate's Jacobian records, used if it is accepted: a second pass
+  // over the chunk (each thread its own keys and the residuals it just
+  // wrote), so the cost loop keeps its register count
+  if (which == 1 && d.fuse_lin) linearize_chunk<float>(d, ch, par);
   const double tot = block_sum(double(acc.hi) + double(acc.lo), red);
   const double tot_raw = block_sum(acc_raw, red);
   if (threadIdx.x == 0) {
